@@ -1,0 +1,375 @@
+#!/usr/bin/env python
+"""Benchmark of the PBF step: particle-updates/s on the 1M-particle large sweep.
+
+Workload: 1,048,576 particles (128 x 64 x 128 lattice, spacing 0.05, seeded
++-0.005 jitter) in a 12.8 x 6.4 x 6.4 box whose x-max wall moves as
+x_w(t) = 12.8 - 1.6 (1 - cos(2 pi t / 4 s)); h = 0.1, 4 solver iterations,
+dt = 1/120 s (one 1/60 s frame = 2 steps).  A step is one Simulator::step
+over all particles; particle-updates/s = particles x steps / second.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+ours:       W untimed steps, then K steps timed with CUDA events on the
+            launching stream, L2 flushed (a 512 MB write) before every timed
+            step, inputs resident in HBM.  Prints one JSON line (rank 0).
+reference:  the reference has no CPU implementation, so its CPU arm is the
+            float OpenMP port of its kernels (oracle/), on all host threads,
+            same workload, each step a full 1M-particle step, bounded to a few
+            minutes in total.
+N > 1 runs N independent replicas (one per GPU); the path does not shard.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import re
+import shutil
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "particle-updates/s at 1M (4 iters)"
+UNIT = "particle-updates/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def load_pkg():
+    import __graft_entry__
+
+    return __graft_entry__.load()
+
+
+def measured_peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(n: int, cells: int) -> dict:
+    """Algorithmic HBM bytes per launch of the two solver passes: each array a
+    pass logically uses is read or written once; c = cells per particle.
+    lambda: R x* 16, W lambda 4, cell table 8c;  delta_p: R x* 16, R lambda 4,
+    W x 16, cell table 8c."""
+    c = cells / max(n, 1)
+    return {"lambda": n * (20 + 8 * c), "delta_p": n * (36 + 8 * c)}
+
+
+def ncu_traffic(kernel: str):
+    """dram bytes per launch of ``kernel`` from the committed ncu summary, scaled
+    to the full workload there (line: 'traffic_bytes_per_launch <kernel>: <bytes>')."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        m = re.search(rf"traffic_bytes_per_launch {kernel}: ([0-9.eE+]+)", f.read_text())
+        if m:
+            return float(m.group(1))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.proc = None
+        self.lines = []
+        exe = shutil.which("nvidia-smi")
+        if exe:
+            self.proc = subprocess.Popen([exe, f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        rows = [r.split(",") for r in out.strip().splitlines() if r.count(",") >= 8]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if "Active" in r[5 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(pkg, name: str, params: str):
+    scene = getattr(pkg.scenes, name)(seed=0)
+    if params == "reference":
+        p = pkg.default_params()
+        p.up[0], p.up[1], p.up[2] = 0.0, 1.0, 0.0
+        p.dt = scene.params.dt
+        scene.params = p
+    return scene
+
+
+def cpu_port_rate(oracle, scene, pos, vel, iid, t0: float, budget_s: float, max_steps: int):
+    """Run the float OpenMP port from (pos, vel, iid) at time t0 for up to
+    max_steps steps or budget_s seconds; returns (updates/s, steps, seconds)."""
+    p = scene.params
+    steps, spent = 0, 0.0
+    t = t0
+    while steps < max_steps and (spent < budget_s or steps == 0):
+        ulim, llim = scene.limits_at(t)
+        a = time.perf_counter()
+        r = oracle.step(p, ulim, llim, pos, vel, iid, prec="f32")
+        spent += time.perf_counter() - a
+        pos, vel, iid = r["npos"], r["nvel"], r["iid"]
+        t += p.dt
+        steps += 1
+    return scene.n * steps / spent, steps, spent
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    pkg = load_pkg()
+    from oracle import oracle
+
+    scene = make_scene(pkg, args.scene, args.params)
+    iid = np.arange(scene.n, dtype=np.uint32)
+    # warm-up, bounded: the CPU arm cannot afford the GPU arm's 60 warm-up frames
+    pos, vel = scene.pos, scene.vel
+    t = 0.0
+    w_done = 0
+    a = time.perf_counter()
+    while w_done < args.warmup and (time.perf_counter() - a < args.cpu_warmup_budget or w_done < 3):
+        ulim, llim = scene.limits_at(t)
+        r = oracle.step(scene.params, ulim, llim, pos, vel, iid, prec="f32")
+        pos, vel, iid = r["npos"], r["nvel"], r["iid"]
+        t += scene.params.dt
+        w_done += 1
+    rate, steps, spent = cpu_port_rate(oracle, scene, pos, vel, iid, t, args.cpu_budget, args.steps)
+    cores = oracle.threads()
+    sample = (f"{scene.n} particles per step, {steps} of {args.steps} timed steps after {w_done} of "
+              f"{args.warmup} warm-up steps (time-bounded)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
+        "steps": steps, "warmup": w_done, "ms_per_step": 1e3 * spent / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(scene, args),
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def workload_config(scene, args) -> dict:
+    p = scene.params
+    return {
+        "workload": f"{scene.name}: {scene.n} particles, 128x64x128 lattice (d=0.05, +-0.005 jitter) in a "
+                    f"12.8x6.4x6.4 box, x-max wall x_w(t)=12.8-1.6(1-cos(2 pi t/4s)), h=0.1, "
+                    f"{p.niter} solver iterations, dt=1/120 s (2 steps per 1/60 s frame)",
+        "particles": scene.n, "niter": p.niter, "params": args.params,
+        "pho0": round(float(p.pho0), 3), "lambda_eps": float(p.lambda_eps), "k_corr": round(float(p.k_corr), 6),
+        "delta_q": round(float(p.delta_q), 6), "n_corr": float(p.n_corr), "c_XSPH": round(float(p.c_XSPH), 6),
+        "parallelism": "replicas" if args.gpus > 1 else "single",
+        "l2": f"flushed before every timed step ({L2_FLUSH_BYTES >> 20} MB write, outside the timed events)",
+    }
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    pkg = load_pkg()
+    scene = make_scene(pkg, args.scene, args.params)
+    p = scene.params
+    n = scene.n
+    stream = torch.cuda.current_stream()
+    st = pkg.ParticleState(scene.pos, scene.vel)
+    ulim0, llim0 = scene.limits_at(0.0)
+    sim = pkg.Simulator(p, scene.ulim, scene.llim, n)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    t = 0.0
+
+    def one_step():
+        nonlocal t
+        ulim, llim = scene.limits_at(t)
+        sim.setLim(ulim, llim)
+        st.step(sim)
+        t += p.dt
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    state0 = (st.pos.cpu().numpy(), st.vel.cpu().numpy(), st.iid[:n].cpu().numpy().astype(np.uint32), t)
+    sim.profile(True)
+    if dist is not None:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    profs = []
+    ev = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)                      # evict L2 (outside the timed events)
+        torch.cuda._sleep(2_000_000)          # let the host enqueue the whole step ahead of the GPU
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        one_step()
+        e1.record(stream)
+        ev.append((e0, e1))
+        profs.append(sim.last_profile())      # waits for this step's last phase event
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(step_ms)
+    if dist is not None:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        dist.barrier()
+    sim.profile(False)
+
+    # -- end to end through the public API with host buffers ------------------------
+    e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps, stream)
+
+    value = world * n * args.steps / (total_ms / 1e3)
+    if rank != 0:
+        sim.close()
+        if dist is not None:
+            dist.destroy_process_group()
+        return
+
+    # -- roofline of the dominant kernel --------------------------------------------
+    dims = sim.grid_dims()
+    cells = dims[0] * dims[1] * dims[2]
+    lam_ms = statistics.mean(pr["lambda_ms"] / pr["iterations"] for pr in profs)
+    dp_ms = statistics.mean(pr["delta_p_ms"] / pr["iterations"] for pr in profs)
+    alg = algorithmic_bytes(n, cells)
+    kernel = "delta_p" if dp_ms >= lam_ms else "lambda"
+    launch_ms = dp_ms if kernel == "delta_p" else lam_ms
+    peak, peak_kind = measured_peaks()
+    achieved = alg[kernel] / (launch_ms / 1e3) / 1e9
+    phases = {k: round(statistics.mean(pr[k] for pr in profs), 4)
+              for k in ("grid_ms", "reorder_ms", "lambda_ms", "delta_p_ms", "xsph_ms", "total_ms")}
+    # the kernels time far above HBM: an FP32 figure explains them (pair work)
+    launches = profs[-1]["launches"]
+
+    # -- CPU baseline: the float OpenMP port on the same state, bounded ---------------
+    from oracle import oracle
+
+    pos0, vel0, iid0, t0 = state0
+    cpu_rate, cpu_steps, cpu_s = cpu_port_rate(oracle, scene, pos0, vel0, iid0, t0, args.cpu_budget,
+                                               max(args.steps, 1))
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(scene, args),
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg[kernel], "launch_ms": launch_ms,
+                     "traffic": ncu_traffic(kernel)},
+        "phases_ms": phases,
+        "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
+                         "sample": f"{n} particles from the state at the first timed step, {cpu_steps} steps "
+                                   f"({cpu_s:.1f} s)"},
+        "e2e": e2e,
+        "gpu_launches": launches * args.steps,
+        "clocks": clk,
+        "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+    }
+    print(json.dumps(line), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def measure_e2e(pkg, torch, sim, scene, state0, steps, stream):
+    """Same metric through Simulator.step with HOST buffers: every step copies
+    pos/vel/iid host->device from pinned memory, steps, and reads npos/nvel/iid
+    back; the copies are inside the timed region."""
+    pos0, vel0, iid0, t = state0
+    n = scene.n
+    p = scene.params
+    h_pos = torch.from_numpy(pos0.copy()).pin_memory()
+    h_vel = torch.from_numpy(vel0.copy()).pin_memory()
+    h_iid = torch.from_numpy(iid0.astype(np.int32)).pin_memory()
+    d = {k: torch.empty(n, 4, device="cuda") for k in ("pos", "vel", "npos", "nvel")}
+    d_iid = torch.empty(n, dtype=torch.int32, device="cuda")
+    h2d = h_pos.numel() * 4 + h_vel.numel() * 4 + h_iid.numel() * 4
+    d2h = h2d
+    for k in range(2):  # warm-up
+        d["pos"].copy_(h_pos, non_blocking=True)
+        d["vel"].copy_(h_vel, non_blocking=True)
+        d_iid.copy_(h_iid, non_blocking=True)
+        sim.step(d["pos"], d["npos"], d["vel"], d["nvel"], d_iid, n)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ulim, llim = scene.limits_at(t)
+        sim.setLim(ulim, llim)
+        d["pos"].copy_(h_pos, non_blocking=True)
+        d["vel"].copy_(h_vel, non_blocking=True)
+        d_iid.copy_(h_iid, non_blocking=True)
+        sim.step(d["pos"], d["npos"], d["vel"], d["nvel"], d_iid, n)
+        h_pos.copy_(d["npos"], non_blocking=True)
+        h_vel.copy_(d["nvel"], non_blocking=True)
+        h_iid.copy_(d_iid, non_blocking=True)
+        t += p.dt
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    return {"value": n * steps / (ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": steps, "ms_per_step": ms / steps}
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=240, help="timed steps (default: 120 frames x 2 steps)")
+    ap.add_argument("--warmup", type=int, default=120, help="untimed steps (default: 60 frames x 2 steps)")
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--scene", default="large_sweep", choices=("large_sweep", "double_dam", "dam_break"))
+    ap.add_argument("--params", choices=("scene", "reference"), default="scene",
+                    help="scene: the dam-break parameter set; reference: the reference's own defaults")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
+    ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,164 @@
+/*
+ * pbf.h — C ABI of the GB300-native Position Based Fluids step.
+ *
+ * This is the drop-in boundary for the per-frame simulation path of
+ * naeioi/PBF-CUDA's `Simulator` class (fluids/Simulator.h:7-61).  Every entry
+ * point takes plain pointers and sizes; device pointers are CUDA global-memory
+ * addresses, streams are `cudaStream_t` passed as `void*`.  No call allocates
+ * on the caller's behalf except pbf_create, which owns all solver scratch.
+ *
+ * Differences from the reference interface, all deliberate:
+ *  - buffers are device pointers to float4 (x, y, z, w) instead of OpenGL
+ *    buffer names of float3 (fluids/Simulator.cpp:20-36); w is carried through
+ *    the permutation untouched on pos and written as 0 on outputs;
+ *  - every call returns a pbf_status instead of exit()ing inside
+ *    checkCudaErrors (common/cuda_inc/helper_cuda.h:1000-1014);
+ *  - pbf_step is asynchronous on the given stream (the reference synchronises
+ *    the device between phases, fluids/Simulator.cpp:44-79);
+ *  - gravity acts along -up (the reference hard-codes up = +z,
+ *    fluids/Simulator.cu:174).
+ */
+#ifndef PBF_H_
+#define PBF_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBF_ABI_VERSION 1
+
+typedef enum pbf_status {
+  PBF_OK = 0,
+  PBF_ERR_INVALID_ARG = 1, /* null pointer, n < 0, aliasing buffers, bad params */
+  PBF_ERR_CAPACITY = 2,    /* n > max_particles, or the box needs more cells than allocated */
+  PBF_ERR_CUDA = 3,        /* a CUDA runtime call failed; see pbf_last_error() */
+  PBF_ERR_TIMEOUT = 4,     /* a bounded device-side wait gave up */
+  PBF_ERR_NOT_READY = 5    /* the solver has no step results yet */
+} pbf_status;
+
+/*
+ * Solver parameters.  Field names and meaning follow the reference's
+ * GUIParams solver fields (fluids/GUIParams.h:6-17); the last four fields
+ * make the reference's hard-coded gravity axis and compile-time constants
+ * (fluids/helper.h:4-9) explicit.
+ */
+typedef struct pbf_params {
+  int niter;                 /* solver iterations per step            GUIParams::niter */
+  float pho0;                /* rest density (mass 1 per particle)    GUIParams::pho0 */
+  float g;                   /* gravity magnitude                     GUIParams::g */
+  float h;                   /* kernel radius = grid cell size        GUIParams::h */
+  float dt;                  /* time step of one pbf_step             GUIParams::dt */
+  float lambda_eps;          /* constraint relaxation epsilon         GUIParams::lambda_eps */
+  float delta_q;             /* s_corr reference distance             GUIParams::delta_q */
+  float k_corr;              /* s_corr strength                       GUIParams::k_corr */
+  float n_corr;              /* s_corr exponent                       GUIParams::n_corr */
+  float k_boundaryDensity;   /* wall density weight                   GUIParams::k_boundaryDensity */
+  float c_XSPH;              /* XSPH viscosity                        GUIParams::c_XSPH */
+  float up[3];               /* gravity acts along -up; reference: (0,0,1) */
+  float lim_eps;             /* wall clamp inset; reference LIM_EPS = 1e-3 */
+  float kernel_eps;          /* spiky-gradient cutoff; reference KERNAL_EPS = 1e-4 */
+  float max_dp;              /* per-component delta_p clamp; reference MAX_DP = 0.1 */
+} pbf_params;
+
+typedef struct pbf_solver pbf_solver;
+
+/* Reference defaults (fluids/FluidSystem.cpp:15-25, fluids/helper.h:4-9). */
+void pbf_params_default(pbf_params* out);
+
+const char* pbf_status_string(pbf_status s);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* pbf_last_error(void);
+int pbf_abi_version(void);
+
+/*
+ * Replaces Simulator::Simulator(const GUIParams&, float3 ulim, float3 llim)
+ * (fluids/Simulator.h:10-26).  Allocates scratch for up to max_particles
+ * particles and for a cell grid of 4x the cells of [llim, ulim] at cell size
+ * h (the reference allocates 4 * prod((ulim - llim) / 0.1) cells,
+ * fluids/Simulator.h:13-14).  Must be called with the target device current.
+ */
+pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float llim[3],
+                      int max_particles, pbf_solver** out);
+
+/* Replaces Simulator::~Simulator (fluids/Simulator.h:27-34). Accepts NULL. */
+pbf_status pbf_destroy(pbf_solver* s);
+
+/* Replace Simulator::loadParams / saveParams (fluids/Simulator.cpp:101-130):
+ * the reference copies from/to the GUIParams singleton; here the caller owns
+ * the struct.  Takes effect at the next pbf_step. */
+pbf_status pbf_set_params(pbf_solver* s, const pbf_params* params);
+pbf_status pbf_get_params(const pbf_solver* s, pbf_params* out);
+
+/* Replaces Simulator::setLim(ulim, llim) (fluids/Simulator.cpp:132-136).
+ * PBF_ERR_CAPACITY if the new box needs more cells than were allocated. */
+pbf_status pbf_set_limits(pbf_solver* s, const float ulim[3], const float llim[3]);
+pbf_status pbf_get_limits(const pbf_solver* s, float ulim[3], float llim[3]);
+
+/*
+ * Replaces Simulator::step(pos, npos, vel, nvel, iid, nparticle)
+ * (fluids/Simulator.h:37, fluids/Simulator.cpp:10-99).  One time step dt.
+ * Same contract as the reference:
+ *   in : pos, vel, iid       state at t (any order)
+ *   out: pos, iid            permuted in place into cell order (stable sort by
+ *                            cell id of the predicted position)
+ *        vel                 (npos - pos) / dt, before XSPH, in cell order
+ *        npos, nvel          state at t + dt, in cell order
+ * All five buffers hold n entries (float4, except iid), must be distinct and
+ * 16-byte aligned.  Asynchronous on `stream` (a cudaStream_t, NULL = legacy
+ * default stream).  A handle is not thread-safe: one step in flight per handle.
+ */
+pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
+                    uint32_t* iid, int n, void* stream);
+
+/*
+ * Density rho_i of the last step's final lambda pass (fluids/Simulator_kernel.cuh:123-124),
+ * in the cell order of that step, copied into the device buffer rho (n floats).
+ * Used for the density-constraint error statistics.
+ */
+pbf_status pbf_get_density(const pbf_solver* s, float* rho, int n, void* stream);
+
+/*
+ * The neighbour grid of the reference (fluids/Simulator.cu:178-211) for the
+ * given predicted positions xstar (device, n float4), exported in the
+ * reference's formats:
+ *   keys  [n]      cell id of each particle, input order (getGridId)
+ *   perm  [n]      input index of the k-th particle in cell order (stable)
+ *   start [cells]  first sorted index of each cell, 0 if empty (computeGridRange)
+ *   end   [cells]  one past the last sorted index, 0 if empty
+ *   dims  [3]      host out: cells per axis, ceil((ulim - llim) / h)
+ * cells = dims[0]*dims[1]*dims[2]; start/end must hold that many entries
+ * (query dims first with start = end = NULL).  Uses the solver's limits and h.
+ */
+pbf_status pbf_build_grid(pbf_solver* s, const void* xstar, int n, uint32_t* keys,
+                          uint32_t* perm, uint32_t* start, uint32_t* end, int dims[3],
+                          void* stream);
+
+/*
+ * Per-phase device times of the last pbf_step, from CUDA events recorded on
+ * the step's stream while profiling is enabled.  Replaces the reference's
+ * Logger phase timing (fluids/Logger.cpp:27-45, fluids/Simulator.cpp:44-79),
+ * which brackets phases with cudaDeviceSynchronize; here nothing synchronises
+ * until pbf_profile_read, which waits for the step's last event.
+ */
+typedef struct pbf_step_profile {
+  float grid_ms;      /* predict + hash + cell counts + radix sort */
+  float reorder_ms;   /* gather into cell order */
+  float lambda_ms;    /* all lambda passes */
+  float delta_p_ms;   /* all position-correction passes (+ velocity update) */
+  float xsph_ms;      /* XSPH pass */
+  float total_ms;     /* whole step */
+  int iterations;     /* solver iterations timed (up to 64) */
+  int launches;       /* kernels launched by the step (also without profiling) */
+  int grid_launches;  /* of which in the grid build */
+} pbf_step_profile;
+
+pbf_status pbf_profile_enable(pbf_solver* s, int on);
+pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF_H_ */

@@ -1,0 +1,177 @@
+"""ctypes binding of the CPU oracle (oracle/pbf_oracle.c).
+
+TEST INFRASTRUCTURE, NOT PRODUCT CODE: imported only by tests/,
+__graft_entry__.smoke() and bench.py's CPU-baseline leg, as the checker or the
+timed CPU baseline.
+
+The oracle is a CPU restatement of naeioi/PBF-CUDA's Simulator::step
+(fluids/Simulator.cpp:10-99, fluids/Simulator.cu:165-273,
+fluids/Simulator_kernel.cuh:7-239) in two arithmetics: ``"f32"`` (float, in
+the reference's operation order, OpenMP-parallel: the CPU port) and ``"f64"``
+(double: the FP64 oracle).  It defines its own mirror of ``pbf_params`` from
+include/pbf.h so that it depends on nothing in the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+import numpy as np
+
+from . import build_oracle
+
+_lock = threading.Lock()
+_lib = None
+
+
+class OracleParams(ctypes.Structure):
+    """Field-for-field mirror of ``pbf_params`` (include/pbf.h)."""
+
+    _fields_ = [
+        ("niter", ctypes.c_int),
+        ("pho0", ctypes.c_float),
+        ("g", ctypes.c_float),
+        ("h", ctypes.c_float),
+        ("dt", ctypes.c_float),
+        ("lambda_eps", ctypes.c_float),
+        ("delta_q", ctypes.c_float),
+        ("k_corr", ctypes.c_float),
+        ("n_corr", ctypes.c_float),
+        ("k_boundaryDensity", ctypes.c_float),
+        ("c_XSPH", ctypes.c_float),
+        ("up", ctypes.c_float * 3),
+        ("lim_eps", ctypes.c_float),
+        ("kernel_eps", ctypes.c_float),
+        ("max_dp", ctypes.c_float),
+    ]
+
+
+def to_oracle_params(p) -> OracleParams:
+    """Copy any object with pbf_params' field names into an OracleParams."""
+    out = OracleParams()
+    for name, _ in OracleParams._fields_:
+        v = getattr(p, name)
+        if name == "up":
+            for a in range(3):
+                out.up[a] = float(v[a])
+        else:
+            setattr(out, name, v)
+    return out
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = build_oracle.build()
+            L = ctypes.CDLL(str(path))
+            f3 = ctypes.POINTER(ctypes.c_float)
+            u32 = ctypes.POINTER(ctypes.c_uint32)
+            i32 = ctypes.POINTER(ctypes.c_int)
+            for tag, rp in (("f32", ctypes.POINTER(ctypes.c_float)), ("f64", ctypes.POINTER(ctypes.c_double))):
+                fn = getattr(L, f"oracle_step_{tag}")
+                fn.argtypes = [ctypes.POINTER(OracleParams), f3, f3, rp, rp, rp, rp, u32, ctypes.c_int, rp, rp]
+                fn.restype = ctypes.c_int
+                fn = getattr(L, f"oracle_grid_{tag}")
+                fn.argtypes = [ctypes.POINTER(OracleParams), f3, f3, rp, ctypes.c_int, u32, u32, u32, u32, i32]
+                fn.restype = ctypes.c_int
+                fn = getattr(L, f"oracle_predict_{tag}")
+                fn.argtypes = [ctypes.POINTER(OracleParams), rp, rp, ctypes.c_int, rp]
+                fn.restype = ctypes.c_int
+                fn = getattr(L, f"oracle_threads_{tag}")
+                fn.argtypes = []
+                fn.restype = ctypes.c_int
+            _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray, ctype):
+    return a.ctypes.data_as(ctypes.POINTER(ctype))
+
+
+def _dtype(prec: str):
+    if prec == "f32":
+        return np.float32, ctypes.c_float
+    if prec == "f64":
+        return np.float64, ctypes.c_double
+    raise ValueError(f"precision must be 'f32' or 'f64', not {prec!r}")
+
+
+def _lim(v) -> ctypes.Array:
+    return (ctypes.c_float * 3)(*[float(x) for x in v])
+
+
+def threads() -> int:
+    return int(lib().oracle_threads_f32())
+
+
+def step(params, ulim, llim, pos, vel, iid, prec: str = "f32"):
+    """One reference step on host arrays.
+
+    pos, vel: (n, 4) arrays (converted to the precision's dtype), iid: (n,) uint32.
+    Returns a dict with the reference's outputs: pos, vel, iid (permuted into
+    cell order; vel = (npos - pos) / dt), npos, nvel, rho and lambda of the last
+    lambda pass.  Inputs are not modified.
+    """
+    dt, ct = _dtype(prec)
+    pos = np.ascontiguousarray(pos, dtype=dt).copy()
+    vel = np.ascontiguousarray(vel, dtype=dt).copy()
+    iid = np.ascontiguousarray(iid, dtype=np.uint32).copy()
+    n = pos.shape[0]
+    assert pos.shape == (n, 4) and vel.shape == (n, 4) and iid.shape == (n,)
+    npos = np.zeros_like(pos)
+    nvel = np.zeros_like(vel)
+    rho = np.zeros(n, dtype=dt)
+    lam = np.zeros(n, dtype=dt)
+    op = to_oracle_params(params)
+    fn = getattr(lib(), f"oracle_step_{prec}")
+    rc = fn(ctypes.byref(op), _lim(ulim), _lim(llim), _ptr(pos, ct), _ptr(npos, ct), _ptr(vel, ct),
+            _ptr(nvel, ct), _ptr(iid, ctypes.c_uint32), n, _ptr(rho, ct), _ptr(lam, ct))
+    if rc != 0:
+        raise ValueError(f"oracle_step_{prec} rejected its arguments (rc={rc})")
+    return {"pos": pos, "vel": vel, "iid": iid, "npos": npos, "nvel": nvel, "rho": rho, "lambda": lam}
+
+
+def grid(params, ulim, llim, xstar, prec: str = "f32"):
+    """The reference's neighbour grid for predicted positions xstar ((n, 4)).
+
+    Returns keys (input order), perm (input index per sorted slot), start/end
+    per cell (0/0 for empty cells) and dims.
+    """
+    dt, ct = _dtype(prec)
+    xs = np.ascontiguousarray(xstar, dtype=dt)
+    n = xs.shape[0]
+    op = to_oracle_params(params)
+    dims = np.zeros(3, dtype=np.int32)
+    fn = getattr(lib(), f"oracle_grid_{prec}")
+    keys = np.zeros(max(n, 1), dtype=np.uint32)
+    perm = np.zeros(max(n, 1), dtype=np.uint32)
+    # first call: dims only
+    null = ctypes.POINTER(ctypes.c_uint32)()
+    fn(ctypes.byref(op), _lim(ulim), _lim(llim), _ptr(xs, ct), 0, null, null, null, null,
+       _ptr(dims, ctypes.c_int))
+    cells = int(np.prod(dims.astype(np.int64)))
+    start = np.zeros(cells, dtype=np.uint32)
+    end = np.zeros(cells, dtype=np.uint32)
+    rc = fn(ctypes.byref(op), _lim(ulim), _lim(llim), _ptr(xs, ct), n, _ptr(keys, ctypes.c_uint32),
+            _ptr(perm, ctypes.c_uint32), _ptr(start, ctypes.c_uint32), _ptr(end, ctypes.c_uint32),
+            _ptr(dims, ctypes.c_int))
+    if rc != 0:
+        raise ValueError(f"oracle_grid_{prec} rejected its arguments (rc={rc})")
+    return {"keys": keys[:n], "perm": perm[:n], "start": start, "end": end, "dims": tuple(int(d) for d in dims)}
+
+
+def predict(params, pos, vel, prec: str = "f32"):
+    """advect_kernel's predicted positions (fluids/Simulator_kernel.cuh:14-15),
+    with the fused multiply-adds nvcc emits: v' = fma(dt, g, v), x* = fma(dt, v', x)."""
+    dt, ct = _dtype(prec)
+    pos = np.ascontiguousarray(pos, dtype=dt)
+    vel = np.ascontiguousarray(vel, dtype=dt)
+    out = np.zeros_like(pos)
+    op = to_oracle_params(params)
+    rc = getattr(lib(), f"oracle_predict_{prec}")(ctypes.byref(op), _ptr(pos, ct), _ptr(vel, ct), pos.shape[0],
+                                                  _ptr(out, ct))
+    if rc != 0:
+        raise ValueError("oracle_predict rejected its arguments")
+    return out

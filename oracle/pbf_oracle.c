@@ -1,0 +1,538 @@
+/*
+ * pbf_oracle.c — CPU restatement of naeioi/PBF-CUDA's Simulator::step.
+ *
+ * TEST INFRASTRUCTURE, NOT PRODUCT CODE.  Only tests/, __graft_entry__.smoke()
+ * and bench.py's CPU-baseline / reference leg load this library: as the checker
+ * the CUDA path is compared against, or as the timed CPU baseline.  The CUDA
+ * product path never links, loads or falls back to it.
+ *
+ * The same source is compiled twice (oracle/build_oracle.py):
+ *   ORACLE_F64 defined -> oracle_*_f64: every continuous quantity in double.
+ *                         This is the FP64 oracle.
+ *   otherwise          -> oracle_*_f32: float arithmetic in the order of the
+ *                         reference's kernels, parallel over particles with
+ *                         OpenMP.  This is the CPU port of the reference (it
+ *                         has no CPU path of its own) and the timed CPU baseline.
+ * Both are compiled with -ffp-contract=off, so the only fused multiply-adds are
+ * the explicit fma() calls of the advection step.  Those reproduce the fused
+ * multiply-adds nvcc emits for the reference's advect_kernel, which makes the
+ * predicted positions, and so the cell ids, bit-identical to the GPU's.
+ *
+ * Parity pinning: the integer outputs (cell ids, stable order, cell ranges)
+ * and the float outputs of this restatement are checked against outputs of the
+ * reference's own kernels (fluids/Simulator_kernel.cuh, fluids/Simulator.cu),
+ * built unmodified for sm_103a and run on a GB300 by oracle/ref_harness; the
+ * recorded vectors live in tests/golden/.
+ *
+ * Layout: all particle arrays are stride-4 (x, y, z, w) in the oracle's real
+ * type; iid is uint32.  The step permutes pos/vel/iid in place exactly like
+ * the reference's thrust::sort_by_key over zip(pos, vel, npos, nvel, iid).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../include/pbf.h"
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#ifdef ORACLE_F64
+typedef double real;
+#define SFX(name) name##_f64
+#define RSQRT(x) sqrt(x)
+#define RFMA(a, b, c) fma((a), (b), (c))
+#define RMIN(a, b) fmin((a), (b))
+#define RMAX(a, b) fmax((a), (b))
+#define RPOW(a, b) pow((a), (b))
+#else
+typedef float real;
+#define SFX(name) name##_f32
+#define RSQRT(x) sqrtf(x)
+#define RFMA(a, b, c) fmaf((a), (b), (c))
+#define RMIN(a, b) fminf((a), (b))
+#define RMAX(a, b) fmaxf((a), (b))
+#define RPOW(a, b) powf((a), (b))
+#endif
+
+/* fluids/helper.h:4 — the reference's truncated pi. */
+#define REF_PI 3.14159265359
+
+typedef struct {
+  int dims[3];
+  int cells;
+} grid_dims;
+
+/* Solver constants, restating the host-side set-up of the reference. */
+typedef struct {
+  real h, h2;
+  real poly6_coef;  /* getPoly6 ctor, fluids/Simulator.cu:77-83 */
+  real spiky_coef;  /* getSpikyGrad ctor, fluids/Simulator.cu:94-98 */
+  real coef_corr;   /* fluids/Simulator.cu:235 */
+  real inv_dt;      /* h_updateVelocity ctor, fluids/Simulator.cu:129 */
+  real g[3];
+  real lo[3], hi[3]; /* wall clamp bounds, fluids/Simulator_kernel.cuh:190-192 */
+  double kernel_eps; /* compared in double, as KERNAL_EPS (fluids/helper.h:7) */
+  real max_dp;
+  float llim[3], ulim[3];
+  grid_dims gd;
+} consts;
+
+/* float -> int conversion with round-toward-zero that saturates and maps NaN
+ * to 0, as the GPU's cvt.rzi.s32 does for the reference's (int) casts. */
+static int f2i_rz(double v) {
+  if (v != v) return 0;
+  if (v >= 2147483647.0) return 2147483647;
+  if (v <= -2147483648.0) return (-2147483647 - 1);
+  return (int)v;
+}
+
+/* A float parameter as the double it was typed as: the shortest decimal that
+ * rounds to it.  The reference's LIM_EPS is the double literal 1e-3
+ * (fluids/helper.h:5); the float field 1e-3f promotes back to exactly 1e-3. */
+static double promote_decimal(float f) {
+  char buf[32];
+  for (int prec = 1; prec <= 9; ++prec) {
+    snprintf(buf, sizeof(buf), "%.*g", prec, (double)f);
+    double d = strtod(buf, NULL);
+    if ((float)d == f) return d;
+  }
+  return (double)f;
+}
+
+/* fluids/Simulator.cu:187-188: dims = ceil((ulim - llim) / h), in float. */
+static grid_dims make_dims(const float ulim[3], const float llim[3], float h) {
+  grid_dims g;
+  for (int a = 0; a < 3; ++a) {
+    float diff = ulim[a] - llim[a];
+    g.dims[a] = f2i_rz((double)ceilf(diff / h));
+    if (g.dims[a] < 1) g.dims[a] = 1;
+  }
+  g.cells = g.dims[0] * g.dims[1] * g.dims[2];
+  return g;
+}
+
+/* getPoly6::operator(), fluids/Simulator.cu:84-89. */
+static inline real poly6(const consts* c, real r2) {
+  if (r2 >= c->h2) return 0;
+  real d = c->h2 - r2;
+  return c->poly6_coef * d * d * d;
+}
+
+/* getSpikyGrad::operator(), fluids/Simulator.cu:100-106: out = grad W(r). */
+static inline void spiky(const consts* c, const real r[3], real out[3]) {
+  real rlen = RSQRT(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
+  if (rlen >= c->h || (double)rlen < c->kernel_eps) {
+    out[0] = out[1] = out[2] = 0;
+    return;
+  }
+  real d = c->h - rlen;
+  real s = c->spiky_coef * d * d / rlen;
+  out[0] = s * r[0];
+  out[1] = s * r[1];
+  out[2] = s * r[2];
+}
+
+/* DensityBoundary::densityAt, fluids/Simulator.cu:144-149 (double constant,
+ * float return). */
+static inline real density_at(real d, real h) {
+  if (d > h) return 0;
+  if (d <= 0) return (real)(2 * REF_PI / 3);
+  return (real)((2 * REF_PI / 3) * (h - d) * (h - d) * (h + d));
+}
+
+/* DensityBoundary::operator(), fluids/Simulator.cu:151-160. */
+static inline real boundary_density(const consts* c, const real p[3]) {
+  real up[3], lo[3];
+  for (int a = 0; a < 3; ++a) {
+    up[a] = (real)c->ulim[a];
+    lo[a] = (real)c->llim[a];
+  }
+  return density_at(up[0] - p[0], c->h) + density_at(p[0] - lo[0], c->h) +
+         density_at(up[1] - p[1], c->h) + density_at(p[1] - lo[1], c->h) +
+         density_at(up[2] - p[2], c->h) + density_at(p[2] - lo[2], c->h);
+}
+
+/* getGridxyz::operator(), fluids/Simulator.cu:30-36 (also getGridId :65-71). */
+static inline void cell_xyz(const consts* c, const real* p, int out[3]) {
+  for (int a = 0; a < 3; ++a) {
+    real diff = p[a] - (real)c->llim[a];
+    int v = f2i_rz((double)(diff / c->h));
+    if (v < 0) v = 0;
+    if (v > c->gd.dims[a] - 1) v = c->gd.dims[a] - 1;
+    out[a] = v;
+  }
+}
+
+/* xyzToId::operator(), fluids/Simulator.cu:44-53. */
+static inline int cell_id(const consts* c, const int xyz[3]) {
+  return xyz[0] * c->gd.dims[1] * c->gd.dims[2] + xyz[1] * c->gd.dims[2] + xyz[2];
+}
+
+static void make_consts(consts* c, const pbf_params* p, const float ulim[3],
+                        const float llim[3]) {
+  memcpy(c->ulim, ulim, sizeof(float) * 3);
+  memcpy(c->llim, llim, sizeof(float) * 3);
+  c->gd = make_dims(ulim, llim, p->h);
+#ifdef ORACLE_F64
+  double h = p->h;
+  c->h = h;
+  c->h2 = h * h;
+  c->poly6_coef = 315.0 / (64.0 * REF_PI * pow(h, 9));
+  c->spiky_coef = -45.0 / (REF_PI * pow(h, 6));
+  {
+    double dq2 = (double)p->delta_q * (double)p->delta_q;
+    double w = dq2 >= c->h2 ? 0.0 : c->poly6_coef * pow(c->h2 - dq2, 3);
+    c->coef_corr = -(double)p->k_corr / pow(w, (double)p->n_corr);
+  }
+  c->inv_dt = 1.0 / (double)p->dt;
+  for (int a = 0; a < 3; ++a) {
+    c->lo[a] = (double)llim[a] + promote_decimal(p->lim_eps);
+    c->hi[a] = (double)ulim[a] - promote_decimal(p->lim_eps);
+  }
+#else
+  float h = p->h;
+  c->h = h;
+  c->h2 = h * h;
+  {
+    float ih = 1.f / h;
+    float ih3 = ih * ih * ih;
+    float ih9 = ih3 * ih3 * ih3;
+    c->poly6_coef = (float)((double)(315.f * ih9) / (64.0 * REF_PI));
+  }
+  {
+    float h6 = h * h;
+    h6 = h6 * h6 * h6;
+    c->spiky_coef = (float)(-45.0 / (REF_PI * (double)h6));
+  }
+  c->coef_corr = -p->k_corr / powf(poly6(c, p->delta_q * p->delta_q), p->n_corr);
+  c->inv_dt = 1.f / p->dt;
+  for (int a = 0; a < 3; ++a) {
+    c->lo[a] = (float)((double)llim[a] + promote_decimal(p->lim_eps));
+    c->hi[a] = (float)((double)ulim[a] - promote_decimal(p->lim_eps));
+  }
+#endif
+  for (int a = 0; a < 3; ++a) c->g[a] = -(real)p->g * (real)p->up[a];
+  c->kernel_eps = promote_decimal(p->kernel_eps);
+  c->max_dp = (real)p->max_dp;
+}
+
+/*
+ * Cell ids, stable order and ranges (fluids/Simulator.cu:178-204 with
+ * computeGridRange, fluids/Simulator_kernel.cuh:21-50).  The stable sort is a
+ * counting sort by cell id; start/end use the reference's 0/0 for empty cells.
+ * keys[n] input order; perm[n] input index of each sorted slot; start/end
+ * hold gd.cells entries and may be NULL.
+ */
+static void build_grid(const consts* c, const real* xstar, int n, uint32_t* keys, uint32_t* perm,
+                       uint32_t* start, uint32_t* end) {
+  int cells = c->gd.cells;
+  uint32_t* cnt = (uint32_t*)calloc((size_t)cells + 1, sizeof(uint32_t));
+  for (int i = 0; i < n; ++i) {
+    int xyz[3];
+    cell_xyz(c, xstar + 4 * (size_t)i, xyz);
+    keys[i] = (uint32_t)cell_id(c, xyz);
+    cnt[keys[i] + 1]++;
+  }
+  for (int k = 0; k < cells; ++k) cnt[k + 1] += cnt[k];
+  if (start && end) {
+    for (int k = 0; k < cells; ++k) {
+      if (cnt[k + 1] > cnt[k]) {
+        start[k] = cnt[k];
+        end[k] = cnt[k + 1];
+      } else {
+        start[k] = end[k] = 0;
+      }
+    }
+  }
+  {
+    uint32_t* fill = (uint32_t*)malloc(sizeof(uint32_t) * ((size_t)cells + 1));
+    memcpy(fill, cnt, sizeof(uint32_t) * ((size_t)cells + 1));
+    for (int i = 0; i < n; ++i) perm[fill[keys[i]]++] = (uint32_t)i;
+    free(fill);
+  }
+  free(cnt);
+}
+
+int SFX(oracle_grid)(const pbf_params* p, const float ulim[3], const float llim[3],
+                     const real* xstar, int n, uint32_t* keys, uint32_t* perm, uint32_t* start,
+                     uint32_t* end, int dims[3]) {
+  consts c;
+  make_consts(&c, p, ulim, llim);
+  if (dims) memcpy(dims, c.gd.dims, sizeof(int) * 3);
+  if (n < 0) return 1;
+  if (n == 0) {
+    if (start && end)
+      for (int k = 0; k < c.gd.cells; ++k) start[k] = end[k] = 0;
+    return 0;
+  }
+  build_grid(&c, xstar, n, keys, perm, start, end);
+  return 0;
+}
+
+/* advect_kernel's predicted positions only (fluids/Simulator_kernel.cuh:14-15). */
+int SFX(oracle_predict)(const pbf_params* p, const real* pos, const real* vel, int n, real* xstar) {
+  if (!p || n < 0) return 1;
+  consts c;
+  float z[3] = {0, 0, 0};
+  make_consts(&c, p, z, z);
+  const real dt = (real)p->dt;
+  for (int i = 0; i < n; ++i) {
+    for (int a = 0; a < 3; ++a) {
+      real v = RFMA(dt, c.g[a], vel[4 * (size_t)i + a]);
+      xstar[4 * (size_t)i + a] = RFMA(dt, v, pos[4 * (size_t)i + a]);
+    }
+    xstar[4 * (size_t)i + 3] = pos[4 * (size_t)i + 3];
+  }
+  return 0;
+}
+
+/* Sorted index range of the three z-consecutive cells (x, y, zlo..zhi): with
+ * the reference's loop order (dz innermost, fluids/Simulator_kernel.cuh:78-88)
+ * these cells are visited in a row, so their particles form one run. */
+static inline void column_run(const consts* c, const uint32_t* cs, int x, int y, int z, int* s,
+                              int* e) {
+  int zlo = z > 0 ? z - 1 : 0;
+  int zhi = z + 1 < c->gd.dims[2] ? z + 1 : c->gd.dims[2] - 1;
+  int base = (x * c->gd.dims[1] + y) * c->gd.dims[2];
+  *s = (int)cs[base + zlo];
+  *e = (int)cs[base + zhi + 1];
+}
+
+/* computeLambda, fluids/Simulator_kernel.cuh:52-129.  cs = exclusive prefix
+ * of cell counts (cells + 1 entries): cell k holds sorted slots [cs[k], cs[k+1]). */
+static void lambda_pass(const consts* c, const pbf_params* p, const real* X, const uint32_t* cs,
+                        int n, real* lambda, real* rho) {
+  const real pho0 = (real)p->pho0;
+  const real eps = (real)p->lambda_eps;
+  const real kb = (real)p->k_boundaryDensity;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) {
+    const real* xi = X + 4 * (size_t)i;
+    int ind[3];
+    cell_xyz(c, xi, ind);
+    real pho = 0, gradj_l2 = 0;
+    real gi[3] = {0, 0, 0};
+    for (int dx = -1; dx <= 1; ++dx) {
+      int x = ind[0] + dx;
+      if (x < 0 || x >= c->gd.dims[0]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int y = ind[1] + dy;
+        if (y < 0 || y >= c->gd.dims[1]) continue;
+        int s, e;
+        column_run(c, cs, x, y, ind[2], &s, &e);
+        for (int j = s; j < e; ++j) {
+          const real* xj = X + 4 * (size_t)j;
+          real d[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+          real r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          pho += poly6(c, r2);
+          real g[3];
+          spiky(c, d, g);
+          g[0] /= pho0;
+          g[1] /= pho0;
+          g[2] /= pho0;
+          gi[0] += g[0];
+          gi[1] += g[1];
+          gi[2] += g[2];
+          if (j != i) gradj_l2 += g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+        }
+      }
+    }
+    pho += kb * boundary_density(c, xi);
+    real grad_l2 = gradj_l2 + gi[0] * gi[0] + gi[1] * gi[1] + gi[2] * gi[2];
+    lambda[i] = -(pho / pho0 - 1) / (grad_l2 + eps);
+    rho[i] = pho;
+  }
+}
+
+/* computetpos, fluids/Simulator_kernel.cuh:131-194 (s_corr with powf). */
+static void dp_pass(const consts* c, const pbf_params* p, const real* X, const uint32_t* cs,
+                    int n, const real* lambda, real* T) {
+  const real pho0 = (real)p->pho0;
+  const real n_corr = (real)p->n_corr;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) {
+    const real* xi = X + 4 * (size_t)i;
+    int ind[3];
+    cell_xyz(c, xi, ind);
+    real li = lambda[i];
+    real d[3] = {0, 0, 0};
+    for (int dx = -1; dx <= 1; ++dx) {
+      int x = ind[0] + dx;
+      if (x < 0 || x >= c->gd.dims[0]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int y = ind[1] + dy;
+        if (y < 0 || y >= c->gd.dims[1]) continue;
+        int s, e;
+        column_run(c, cs, x, y, ind[2], &s, &e);
+        for (int j = s; j < e; ++j) {
+          if (j == i) continue;
+          const real* xj = X + 4 * (size_t)j;
+          real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+          real corr = c->coef_corr * RPOW(poly6(c, r[0] * r[0] + r[1] * r[1] + r[2] * r[2]), n_corr);
+          real g[3];
+          spiky(c, r, g);
+          real f = li + lambda[j] + corr;
+          d[0] += f * g[0];
+          d[1] += f * g[1];
+          d[2] += f * g[2];
+        }
+      }
+    }
+    real* ti = T + 4 * (size_t)i;
+    for (int a = 0; a < 3; ++a) {
+      real v = d[a] / pho0;
+      v = RMAX(RMIN(v, c->max_dp), -c->max_dp);
+      v = xi[a] + v;
+      ti[a] = RMAX(RMIN(v, c->hi[a]), c->lo[a]);
+    }
+    ti[3] = xi[3];
+  }
+}
+
+/* computeXSPH, fluids/Simulator_kernel.cuh:196-239. */
+static void xsph_pass(const consts* c, const pbf_params* p, const real* X, const real* V,
+                      const real* rho, const uint32_t* cs, int n, real* NV) {
+  const real cx = (real)p->c_XSPH;
+#pragma omp parallel for schedule(static)
+  for (int i = 0; i < n; ++i) {
+    const real* xi = X + 4 * (size_t)i;
+    const real* vi = V + 4 * (size_t)i;
+    real ci = rho[i];
+    int ind[3];
+    cell_xyz(c, xi, ind);
+    real av[3] = {0, 0, 0};
+    for (int dx = -1; dx <= 1; ++dx) {
+      int x = ind[0] + dx;
+      if (x < 0 || x >= c->gd.dims[0]) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        int y = ind[1] + dy;
+        if (y < 0 || y >= c->gd.dims[1]) continue;
+        int s, e;
+        column_run(c, cs, x, y, ind[2], &s, &e);
+        for (int j = s; j < e; ++j) {
+          const real* xj = X + 4 * (size_t)j;
+          const real* vj = V + 4 * (size_t)j;
+          real dp[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+          real w = poly6(c, dp[0] * dp[0] + dp[1] * dp[1] + dp[2] * dp[2]);
+          real den = ci + rho[j];
+          for (int a = 0; a < 3; ++a) av[a] += (real)2 * (vj[a] - vi[a]) * w / den;
+        }
+      }
+    }
+    real* o = NV + 4 * (size_t)i;
+    for (int a = 0; a < 3; ++a) o[a] = vi[a] + cx * av[a];
+  }
+}
+
+/*
+ * One Simulator::step (fluids/Simulator.cpp:10-99) on host arrays, with the
+ * same in/out contract as the GPU entry point pbf_step.  rho_out/lambda_out
+ * (optional, n entries, cell order) receive the last lambda pass.
+ * Returns 0 on success, nonzero on bad arguments.
+ */
+int SFX(oracle_step)(const pbf_params* p, const float ulim[3], const float llim[3], real* pos,
+                     real* npos, real* vel, real* nvel, uint32_t* iid, int n, real* rho_out,
+                     real* lambda_out) {
+  if (!p || n < 0 || p->niter < 1) return 1;
+  if (n == 0) return 0;
+  consts c;
+  make_consts(&c, p, ulim, llim);
+  size_t n4 = 4 * (size_t)n;
+  real* X = (real*)malloc(sizeof(real) * n4);    /* x, sorted */
+  real* V = (real*)malloc(sizeof(real) * n4);    /* v after gravity, sorted */
+  real* A = (real*)malloc(sizeof(real) * n4);    /* npos ping */
+  real* B = (real*)malloc(sizeof(real) * n4);    /* tpos pong */
+  real* S = (real*)malloc(sizeof(real) * n4);    /* predicted, input order */
+  real* lam = (real*)malloc(sizeof(real) * (size_t)n);
+  real* rho = (real*)malloc(sizeof(real) * (size_t)n);
+  uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t* ids = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t* cs = (uint32_t*)calloc((size_t)c.gd.cells + 1, sizeof(uint32_t));
+
+  /* advect_kernel, fluids/Simulator_kernel.cuh:7-19: v += dt g; x* = x + dt v. */
+  const real dt = (real)p->dt;
+  for (int i = 0; i < n; ++i) {
+    real* v = vel + 4 * (size_t)i;
+    real* x = pos + 4 * (size_t)i;
+    real* s = S + 4 * (size_t)i;
+    for (int a = 0; a < 3; ++a) {
+      v[a] = RFMA(dt, c.g[a], v[a]);
+      s[a] = RFMA(dt, v[a], x[a]);
+    }
+    s[3] = x[3];
+  }
+  /* buildGridHash: ids, stable sort of zip(pos, vel, npos, nvel, iid), ranges. */
+  build_grid(&c, S, n, keys, perm, NULL, NULL);
+  for (int i = 0; i < n; ++i) cs[keys[i] + 1]++;
+  for (int k = 0; k < c.gd.cells; ++k) cs[k + 1] += cs[k];
+  for (int k = 0; k < n; ++k) {
+    uint32_t q = perm[k];
+    memcpy(X + 4 * (size_t)k, pos + 4 * (size_t)q, sizeof(real) * 4);
+    memcpy(V + 4 * (size_t)k, vel + 4 * (size_t)q, sizeof(real) * 4);
+    memcpy(A + 4 * (size_t)k, S + 4 * (size_t)q, sizeof(real) * 4);
+    ids[k] = iid[q];
+  }
+  /* correctDensity x niter (fluids/Simulator.cu:213-249): Jacobi update. */
+  for (int it = 0; it < p->niter; ++it) {
+    lambda_pass(&c, p, A, cs, n, lam, rho);
+    dp_pass(&c, p, A, cs, n, lam, B);
+    real* t = A;
+    A = B;
+    B = t;
+  }
+  /* updateVelocity (fluids/Simulator.cu:267-273): v = (x* - x) * (1/dt). */
+  for (int k = 0; k < n; ++k) {
+    for (int a = 0; a < 3; ++a) V[4 * (size_t)k + a] = (A[4 * (size_t)k + a] - X[4 * (size_t)k + a]) * c.inv_dt;
+  }
+  /* correctVelocity: XSPH with rho of the last lambda pass. */
+  xsph_pass(&c, p, A, V, rho, cs, n, B);
+
+  for (int k = 0; k < n; ++k) {
+    size_t o = 4 * (size_t)k;
+    pos[o] = X[o];
+    pos[o + 1] = X[o + 1];
+    pos[o + 2] = X[o + 2];
+    pos[o + 3] = X[o + 3];
+    npos[o] = A[o];
+    npos[o + 1] = A[o + 1];
+    npos[o + 2] = A[o + 2];
+    npos[o + 3] = X[o + 3];
+    vel[o] = V[o];
+    vel[o + 1] = V[o + 1];
+    vel[o + 2] = V[o + 2];
+    nvel[o] = B[o];
+    nvel[o + 1] = B[o + 1];
+    nvel[o + 2] = B[o + 2];
+    nvel[o + 3] = 0;
+    vel[o + 3] = 0;
+    iid[k] = ids[k];
+    if (rho_out) rho_out[k] = rho[k];
+    if (lambda_out) lambda_out[k] = lam[k];
+  }
+  free(X);
+  free(V);
+  free(A);
+  free(B);
+  free(S);
+  free(lam);
+  free(rho);
+  free(keys);
+  free(perm);
+  free(ids);
+  free(cs);
+  return 0;
+}
+
+/* Number of OpenMP threads the parallel passes use (1 without OpenMP). */
+int SFX(oracle_threads)(void) {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}

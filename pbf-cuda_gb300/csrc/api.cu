@@ -1,0 +1,481 @@
+// api.cu — the C ABI of include/pbf.h: solver object, parameter handling,
+// argument checks and the phase sequence of one step.
+//
+// Phase sequence of pbf_step, as Simulator::step (fluids/Simulator.cpp:10-99):
+//   advect + buildGridHash  -> grid.cu  (predict, hash, counts, radix sort)
+//   (gather into cell order) -> solver.cu reorder
+//   niter x correctDensity   -> solver.cu lambda / delta_p (Jacobi ping-pong)
+//   updateVelocity           -> fused into the last delta_p pass
+//   correctVelocity (XSPH)   -> solver.cu xsph
+// All of it is enqueued on the caller's stream without host synchronisation.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include "pbf_internal.cuh"
+
+// Phase boundaries recorded by pbf_step when profiling is on.
+enum { kEvStart, kEvGrid, kEvReorder, kEvXsphStart, kEvEnd, kEvFixed };
+constexpr int kMaxProfiledIters = 64;
+
+struct pbf_solver {
+  pbf_params params;
+  float ulim[3], llim[3];
+  int max_particles;
+  int max_cells;
+  int device;
+  int last_n;  // particles of the last completed step (for pbf_get_density)
+  pbf::GridScratch grid;
+  pbf::SolverScratch sol;
+  // profiling (Logger equivalent, fluids/Logger.cpp:27-45): CUDA events
+  bool profile;
+  cudaEvent_t ev[kEvFixed];
+  cudaEvent_t ev_it[3 * kMaxProfiledIters];  // per iteration: lambda start, delta_p start, delta_p end
+  int prof_iters;       // iterations recorded by the last profiled step (0: none)
+  int last_launches;    // kernels launched by the last pbf_step
+  int last_grid_launches;
+};
+
+namespace {
+
+thread_local char g_err[512] = "";
+
+pbf_status fail(pbf_status s, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+pbf_status fail(pbf_status s, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return s;
+}
+
+pbf_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(PBF_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define PBF_CUDA(call, what)                         \
+  do {                                               \
+    cudaError_t e_ = (call);                         \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+bool finite_f(float v) { return std::isfinite(v); }
+
+pbf_status check_params(const pbf_params* p) {
+  if (!p) return fail(PBF_ERR_INVALID_ARG, "params is NULL");
+  if (p->niter < 1) return fail(PBF_ERR_INVALID_ARG, "niter must be >= 1 (got %d)", p->niter);
+  const float vals[] = {p->pho0, p->g, p->h, p->dt, p->lambda_eps, p->delta_q, p->k_corr,
+                        p->n_corr, p->k_boundaryDensity, p->c_XSPH, p->up[0], p->up[1],
+                        p->up[2], p->lim_eps, p->kernel_eps, p->max_dp};
+  for (float v : vals)
+    if (!finite_f(v)) return fail(PBF_ERR_INVALID_ARG, "params hold a non-finite value");
+  if (!(p->h > 0.f)) return fail(PBF_ERR_INVALID_ARG, "h must be > 0");
+  if (!(p->dt > 0.f)) return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
+  if (!(p->pho0 > 0.f)) return fail(PBF_ERR_INVALID_ARG, "pho0 must be > 0");
+  if (p->max_dp < 0.f || p->lim_eps < 0.f || p->kernel_eps < 0.f)
+    return fail(PBF_ERR_INVALID_ARG, "max_dp, lim_eps and kernel_eps must be >= 0");
+  return PBF_OK;
+}
+
+// Cells per axis as the reference computes them: (int)ceilf((ulim - llim) / h)
+// in float (fluids/Simulator.cu:187-188), at least 1.
+pbf_status grid_dims(const float ulim[3], const float llim[3], float h, int dims[3],
+                     long long* cells) {
+  long long c = 1;
+  for (int a = 0; a < 3; ++a) {
+    if (!finite_f(ulim[a]) || !finite_f(llim[a]))
+      return fail(PBF_ERR_INVALID_ARG, "limits must be finite");
+    if (!(ulim[a] > llim[a])) return fail(PBF_ERR_INVALID_ARG, "ulim must exceed llim on every axis");
+    const float d = ceilf((ulim[a] - llim[a]) / h);
+    if (!(d < 1e9f)) return fail(PBF_ERR_CAPACITY, "grid too large");
+    dims[a] = d < 1.f ? 1 : (int)d;
+    c *= dims[a];
+  }
+  *cells = c;
+  return PBF_OK;
+}
+
+// A float parameter as the double it was typed as: the shortest decimal that
+// rounds to it.  The reference's LIM_EPS is the double literal 1e-3
+// (fluids/helper.h:5), and the float field 1e-3f promotes back to exactly 1e-3.
+double promote_decimal(float f) {
+  char buf[32];
+  for (int prec = 1; prec <= 9; ++prec) {
+    snprintf(buf, sizeof(buf), "%.*g", prec, (double)f);
+    const double d = strtod(buf, nullptr);
+    if ((float)d == f) return d;
+  }
+  return (double)f;
+}
+
+// The reference's host-side coefficients, bit for bit (see pbf_internal.cuh).
+pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const float llim[3],
+                            const int dims[3]) {
+  pbf::StepConsts c;
+  std::memset(&c, 0, sizeof(c));
+  const float h = p.h;
+  c.h = h;
+  c.h2 = h * h;
+  // Host code is compiled with -ffp-contract=off, so these float expressions
+  // round after every operation, as the reference's host code does.
+  {
+    const float ih = 1.f / h;
+    const float ih3 = ih * ih * ih;
+    const float ih9 = ih3 * ih3 * ih3;
+    c.poly6_coef = (float)((double)(315.f * ih9) / (64.0 * pbf::kRefPi));
+  }
+  {
+    float h6 = h * h;
+    h6 = h6 * h6 * h6;
+    c.spiky_coef = (float)(-45.0 / (pbf::kRefPi * (double)h6));
+  }
+  c.pho0 = p.pho0;
+  c.inv_pho0 = 1.f / p.pho0;
+  c.spiky_coef_rho0 = c.spiky_coef / p.pho0;
+  c.lambda_eps = p.lambda_eps;
+  {
+    const float dq2 = p.delta_q * p.delta_q;
+    float wdq = 0.f;
+    if (dq2 < c.h2) {
+      const float d = c.h2 - dq2;
+      wdq = c.poly6_coef * d * d * d;
+    }
+    c.coef_corr = -p.k_corr / powf(wdq, p.n_corr);
+  }
+  c.n_corr = p.n_corr;
+  c.npow = -1;
+  for (int k = 1; k <= 4; ++k)
+    if (p.n_corr == (float)k) c.npow = k;
+  c.keps2 = p.kernel_eps * p.kernel_eps;
+  c.max_dp = p.max_dp;
+  c.k_b = p.k_boundaryDensity;
+  c.c_xsph = p.c_XSPH;
+  c.dt = p.dt;
+  c.inv_dt = 1.f / p.dt;
+  for (int a = 0; a < 3; ++a) {
+    c.g[a] = -p.g * p.up[a];
+    c.lo[a] = (float)((double)llim[a] + promote_decimal(p.lim_eps));
+    c.hi[a] = (float)((double)ulim[a] - promote_decimal(p.lim_eps));
+    c.llim[a] = llim[a];
+    c.ulim[a] = ulim[a];
+    c.dims[a] = dims[a];
+  }
+  c.cells = dims[0] * dims[1] * dims[2];
+  return c;
+}
+
+template <typename T>
+cudaError_t alloc(T** p, size_t count) {
+  return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
+}
+
+void free_all(pbf_solver* s) {
+  void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
+                  s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
+                  s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
+                  s->sol.lambda, s->sol.rho};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (cudaEvent_t& e : s->ev)
+    if (e) cudaEventDestroy(e);
+  for (cudaEvent_t& e : s->ev_it)
+    if (e) cudaEventDestroy(e);
+}
+
+bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+}  // namespace
+
+extern "C" {
+
+void pbf_params_default(pbf_params* out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  out->niter = 4;
+  out->pho0 = 8000.f;
+  out->g = 9.8f;
+  out->h = .1f;
+  out->dt = 0.0083f;
+  out->lambda_eps = 1000.f;
+  out->delta_q = (float)(0.3 * out->h);
+  out->k_corr = 0.001f;
+  out->n_corr = 4.f;
+  out->k_boundaryDensity = 0.f;
+  out->c_XSPH = 0.5f;
+  out->up[0] = 0.f;
+  out->up[1] = 0.f;
+  out->up[2] = 1.f;
+  out->lim_eps = 1e-3f;
+  out->kernel_eps = 1e-4f;
+  out->max_dp = 0.1f;
+}
+
+const char* pbf_status_string(pbf_status s) {
+  switch (s) {
+    case PBF_OK: return "ok";
+    case PBF_ERR_INVALID_ARG: return "invalid argument";
+    case PBF_ERR_CAPACITY: return "capacity exceeded";
+    case PBF_ERR_CUDA: return "CUDA error";
+    case PBF_ERR_TIMEOUT: return "device wait timed out";
+    case PBF_ERR_NOT_READY: return "no step results yet";
+  }
+  return "unknown status";
+}
+
+const char* pbf_last_error(void) { return g_err; }
+
+int pbf_abi_version(void) { return PBF_ABI_VERSION; }
+
+pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float llim[3],
+                      int max_particles, pbf_solver** out) {
+  g_err[0] = 0;
+  if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!ulim || !llim) return fail(PBF_ERR_INVALID_ARG, "limits are NULL");
+  if (max_particles < 0) return fail(PBF_ERR_INVALID_ARG, "max_particles < 0");
+  pbf_status st = check_params(params);
+  if (st != PBF_OK) return st;
+  int dims[3];
+  long long cells;
+  if ((st = grid_dims(ulim, llim, params->h, dims, &cells)) != PBF_OK) return st;
+  // 4x the initial box's cells, like the reference's ngrid (fluids/Simulator.h:13-14),
+  // so a moving wall can widen the box.
+  long long max_cells = 4 * cells;
+  const long long scan_cap = (long long)pbf::kScanTile * pbf::kMaxScanPartials - 1;
+  if (max_cells > scan_cap) max_cells = cells;
+  if (max_cells > scan_cap) return fail(PBF_ERR_CAPACITY, "box needs %lld cells, limit %lld", cells, scan_cap);
+
+  pbf_solver* s = new (std::nothrow) pbf_solver;
+  if (!s) return fail(PBF_ERR_CAPACITY, "host allocation failed");
+  std::memset(s, 0, sizeof(*s));
+  s->params = *params;
+  std::memcpy(s->ulim, ulim, sizeof(s->ulim));
+  std::memcpy(s->llim, llim, sizeof(s->llim));
+  s->max_particles = max_particles;
+  s->max_cells = (int)max_cells;
+  cudaError_t e = cudaGetDevice(&s->device);
+  const size_t np = (size_t)max_particles;
+  const size_t nc = (size_t)max_cells + 1;
+  if (e == cudaSuccess) e = alloc(&s->grid.keys_a, np);
+  if (e == cudaSuccess) e = alloc(&s->grid.keys_b, np);
+  if (e == cudaSuccess) e = alloc(&s->grid.vals_a, np);
+  if (e == cudaSuccess) e = alloc(&s->grid.vals_b, np);
+  if (e == cudaSuccess) e = alloc(&s->grid.cell_count, nc);
+  if (e == cudaSuccess) e = alloc(&s->grid.cell_start, nc);
+  if (e == cudaSuccess) e = alloc(&s->grid.radix_counts, pbf::radix_counts_len(max_particles));
+  if (e == cudaSuccess) e = alloc(&s->grid.scan_partials, (size_t)pbf::kMaxScanPartials);
+  if (e == cudaSuccess) e = alloc(&s->sol.xs, np);
+  if (e == cudaSuccess) e = alloc(&s->sol.xa, np);
+  if (e == cudaSuccess) e = alloc(&s->sol.xb, np);
+  if (e == cudaSuccess) e = alloc(&s->sol.iid_s, np);
+  if (e == cudaSuccess) e = alloc(&s->sol.lambda, np);
+  if (e == cudaSuccess) e = alloc(&s->sol.rho, np);
+  if (e != cudaSuccess) {
+    free_all(s);
+    delete s;
+    cudaGetLastError();
+    return cuda_fail(e, "pbf_create: cudaMalloc");
+  }
+  *out = s;
+  return PBF_OK;
+}
+
+pbf_status pbf_destroy(pbf_solver* s) {
+  if (!s) return PBF_OK;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != s->device) cudaSetDevice(s->device);
+  free_all(s);
+  if (prev >= 0 && prev != s->device) cudaSetDevice(prev);
+  delete s;
+  return PBF_OK;
+}
+
+pbf_status pbf_set_params(pbf_solver* s, const pbf_params* params) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  pbf_status st = check_params(params);
+  if (st != PBF_OK) return st;
+  int dims[3];
+  long long cells;
+  if ((st = grid_dims(s->ulim, s->llim, params->h, dims, &cells)) != PBF_OK) return st;
+  if (cells > s->max_cells)
+    return fail(PBF_ERR_CAPACITY, "h = %g needs %lld cells, %d allocated", params->h, cells, s->max_cells);
+  s->params = *params;
+  return PBF_OK;
+}
+
+pbf_status pbf_get_params(const pbf_solver* s, pbf_params* out) {
+  if (!s || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  *out = s->params;
+  return PBF_OK;
+}
+
+pbf_status pbf_set_limits(pbf_solver* s, const float ulim[3], const float llim[3]) {
+  if (!s || !ulim || !llim) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  int dims[3];
+  long long cells;
+  pbf_status st = grid_dims(ulim, llim, s->params.h, dims, &cells);
+  if (st != PBF_OK) return st;
+  if (cells > s->max_cells)
+    return fail(PBF_ERR_CAPACITY, "box needs %lld cells, %d allocated", cells, s->max_cells);
+  std::memcpy(s->ulim, ulim, sizeof(s->ulim));
+  std::memcpy(s->llim, llim, sizeof(s->llim));
+  return PBF_OK;
+}
+
+pbf_status pbf_get_limits(const pbf_solver* s, float ulim[3], float llim[3]) {
+  if (!s || !ulim || !llim) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  std::memcpy(ulim, s->ulim, sizeof(s->ulim));
+  std::memcpy(llim, s->llim, sizeof(s->llim));
+  return PBF_OK;
+}
+
+pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
+                    int n, void* stream) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n < 0");
+  if (n > s->max_particles)
+    return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
+  if (n == 0) return PBF_OK;
+  const void* bufs[5] = {pos, npos, vel, nvel, iid};
+  for (int a = 0; a < 5; ++a) {
+    if (!bufs[a]) return fail(PBF_ERR_INVALID_ARG, "buffer %d is NULL", a);
+    if (!aligned16(bufs[a]) && a < 4) return fail(PBF_ERR_INVALID_ARG, "buffer %d not 16-byte aligned", a);
+    for (int b = 0; b < a; ++b)
+      if (bufs[a] == bufs[b]) return fail(PBF_ERR_INVALID_ARG, "buffers %d and %d alias", b, a);
+  }
+  int dims[3];
+  long long cells;
+  pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
+  if (st != PBF_OK) return st;
+  if (cells > s->max_cells) return fail(PBF_ERR_CAPACITY, "box needs %lld cells", cells);
+  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims);
+  cudaStream_t st_ = (cudaStream_t)stream;
+  const bool prof = s->profile;
+  const int niter = s->params.niter;
+  const int piters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
+  s->prof_iters = 0;
+#define PBF_EV(e) \
+  if (prof) PBF_CUDA(cudaEventRecord((e), st_), "pbf_step: event")
+  PBF_EV(s->ev[kEvStart]);
+  // advect + buildGridHash (fluids/Simulator.cpp:46-53)
+  const uint32_t* perm = nullptr;
+  PBF_CUDA(pbf::build_grid(c, (const float4*)pos, (const float4*)vel, nullptr, n, s->grid, &perm,
+                           nullptr, st_),
+           "pbf_step: grid");
+  PBF_EV(s->ev[kEvGrid]);
+  PBF_CUDA(pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, s->sol, st_),
+           "pbf_step: reorder");
+  PBF_EV(s->ev[kEvReorder]);
+  // niter x correctDensity (fluids/Simulator.cpp:55-60), Jacobi ping-pong;
+  // updateVelocity fused into the last position update (fluids/Simulator.cpp:62-66)
+  const uint32_t* cs = s->grid.cell_start;
+  float4* X = s->sol.xa;
+  float4* T = s->sol.xb;
+  for (int it = 0; it < niter; ++it) {
+    if (it < piters) PBF_EV(s->ev_it[3 * it]);
+    PBF_CUDA(pbf::launch_lambda(c, X, cs, n, s->sol.lambda, s->sol.rho, st_), "pbf_step: lambda");
+    if (it < piters) PBF_EV(s->ev_it[3 * it + 1]);
+    if (it + 1 < niter) {
+      PBF_CUDA(pbf::launch_delta_p(c, X, s->sol.lambda, cs, n, T, st_), "pbf_step: delta_p");
+      float4* t = X;
+      X = T;
+      T = t;
+    } else {
+      PBF_CUDA(pbf::launch_delta_p_final(c, X, s->sol.lambda, cs, n, s->sol, (float4*)pos,
+                                         (float4*)npos, (float4*)vel, iid, st_),
+               "pbf_step: delta_p");
+    }
+    if (it < piters) PBF_EV(s->ev_it[3 * it + 2]);
+  }
+  // correctVelocity: XSPH (fluids/Simulator.cpp:68-71)
+  PBF_EV(s->ev[kEvXsphStart]);
+  PBF_CUDA(pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, s->sol.rho, cs, n,
+                            (float4*)nvel, st_),
+           "pbf_step: xsph");
+  PBF_EV(s->ev[kEvEnd]);
+#undef PBF_EV
+  s->last_grid_launches = pbf::grid_launches(c, n);
+  s->last_launches = s->last_grid_launches + 1 + 2 * niter + 1;
+  if (prof) s->prof_iters = piters;
+  s->last_n = n;
+  return PBF_OK;
+}
+
+pbf_status pbf_profile_enable(pbf_solver* s, int on) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (on && !s->ev[0]) {
+    for (cudaEvent_t& e : s->ev) PBF_CUDA(cudaEventCreate(&e), "pbf_profile_enable");
+    for (cudaEvent_t& e : s->ev_it) PBF_CUDA(cudaEventCreate(&e), "pbf_profile_enable");
+  }
+  s->profile = on != 0;
+  return PBF_OK;
+}
+
+pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out) {
+  if (!s || !out) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  std::memset(out, 0, sizeof(*out));
+  out->launches = s->last_launches;
+  out->grid_launches = s->last_grid_launches;
+  if (s->prof_iters == 0) return fail(PBF_ERR_NOT_READY, "no profiled step recorded");
+  PBF_CUDA(cudaEventSynchronize(s->ev[kEvEnd]), "pbf_profile_read");
+  float ms = 0.f;
+  PBF_CUDA(cudaEventElapsedTime(&ms, s->ev[kEvStart], s->ev[kEvGrid]), "pbf_profile_read");
+  out->grid_ms = ms;
+  PBF_CUDA(cudaEventElapsedTime(&ms, s->ev[kEvGrid], s->ev[kEvReorder]), "pbf_profile_read");
+  out->reorder_ms = ms;
+  for (int it = 0; it < s->prof_iters; ++it) {
+    PBF_CUDA(cudaEventElapsedTime(&ms, s->ev_it[3 * it], s->ev_it[3 * it + 1]), "pbf_profile_read");
+    out->lambda_ms += ms;
+    PBF_CUDA(cudaEventElapsedTime(&ms, s->ev_it[3 * it + 1], s->ev_it[3 * it + 2]), "pbf_profile_read");
+    out->delta_p_ms += ms;
+  }
+  PBF_CUDA(cudaEventElapsedTime(&ms, s->ev[kEvXsphStart], s->ev[kEvEnd]), "pbf_profile_read");
+  out->xsph_ms = ms;
+  PBF_CUDA(cudaEventElapsedTime(&ms, s->ev[kEvStart], s->ev[kEvEnd]), "pbf_profile_read");
+  out->total_ms = ms;
+  out->iterations = s->prof_iters;
+  return PBF_OK;
+}
+
+pbf_status pbf_get_density(const pbf_solver* s, float* rho, int n, void* stream) {
+  if (!s || !rho) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  if (s->last_n == 0) return fail(PBF_ERR_NOT_READY, "no step has run");
+  if (n < 0 || n > s->last_n) return fail(PBF_ERR_INVALID_ARG, "n outside [0, %d]", s->last_n);
+  PBF_CUDA(cudaMemcpyAsync(rho, s->sol.rho, sizeof(float) * n, cudaMemcpyDeviceToDevice,
+                           (cudaStream_t)stream),
+           "pbf_get_density");
+  return PBF_OK;
+}
+
+pbf_status pbf_build_grid(pbf_solver* s, const void* xstar, int n, uint32_t* keys, uint32_t* perm,
+                          uint32_t* start, uint32_t* end, int dims[3], void* stream) {
+  if (!s || !dims) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  long long cells;
+  pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
+  if (st != PBF_OK) return st;
+  if (!start && !end && !keys && !perm) return PBF_OK;  // dims query
+  if (cells > s->max_cells) return fail(PBF_ERR_CAPACITY, "box needs %lld cells", cells);
+  if (n < 0 || n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n outside [0, max_particles]");
+  if (!start || !end) return fail(PBF_ERR_INVALID_ARG, "start/end are NULL");
+  if (n > 0 && (!xstar || !keys || !perm)) return fail(PBF_ERR_INVALID_ARG, "NULL buffer");
+  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims);
+  cudaStream_t st_ = (cudaStream_t)stream;
+  if (n == 0) {
+    PBF_CUDA(cudaMemsetAsync(start, 0, sizeof(uint32_t) * cells, st_), "pbf_build_grid");
+    PBF_CUDA(cudaMemsetAsync(end, 0, sizeof(uint32_t) * cells, st_), "pbf_build_grid");
+    return PBF_OK;
+  }
+  const uint32_t* p = nullptr;
+  PBF_CUDA(pbf::build_grid(c, nullptr, nullptr, (const float4*)xstar, n, s->grid, &p, keys, st_),
+           "pbf_build_grid");
+  PBF_CUDA(cudaMemcpyAsync(perm, p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st_),
+           "pbf_build_grid: perm");
+  PBF_CUDA(pbf::export_ranges(c, s->grid.cell_start, start, end, st_), "pbf_build_grid: ranges");
+  return PBF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,166 @@
+// pbf_internal.cuh — constants, device math and launch wrappers shared by the
+// translation units of libpbf.  Internal: the public boundary is include/pbf.h.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pbf.h"
+
+namespace pbf {
+
+// fluids/helper.h:4 — the reference's truncated pi, used by its host-side
+// kernel coefficients (getPoly6 / getSpikyGrad constructors).
+constexpr double kRefPi = 3.14159265359;
+
+// Everything a pass needs, computed once per step on the host and passed by
+// value.  Coefficients follow the reference's host-side set-up bit for bit
+// (fluids/Simulator.cu:77-98, :129, :187-188, :235).
+struct StepConsts {
+  float h, h2;
+  float poly6_coef;        // 315 / (64 pi h^9), getPoly6 ctor
+  float spiky_coef;        // -45 / (pi h^6), getSpikyGrad ctor
+  float spiky_coef_rho0;   // spiky_coef / pho0 (lambda pass gradients are grad W / pho0)
+  float pho0, inv_pho0;
+  float lambda_eps;
+  float coef_corr;         // -k_corr / W(delta_q)^n_corr
+  float n_corr;
+  int npow;                // n_corr as a small positive integer, or -1
+  float keps2;             // kernel_eps^2: spiky gradient is zero for |r| < kernel_eps
+  float max_dp;
+  float k_b;               // k_boundaryDensity
+  float c_xsph;
+  float dt, inv_dt;
+  float g[3];              // gravity vector = -g * up
+  float lo[3], hi[3];      // wall clamp bounds: llim + lim_eps, ulim - lim_eps (rounded once from double)
+  float llim[3], ulim[3];
+  int dims[3];             // cells per axis
+  int cells;
+};
+
+// Cell coordinate along one axis: getGridxyz / getGridId (fluids/Simulator.cu:30-36,
+// :65-71): IEEE (p - llim) / h, truncating conversion (saturating, NaN -> 0),
+// clamped into [0, dim - 1].
+__device__ __forceinline__ int cell_coord(float p, float llim, float h, int dim) {
+  int v = __float2int_rz(__fdiv_rn(__fsub_rn(p, llim), h));
+  return min(max(v, 0), dim - 1);
+}
+
+__device__ __forceinline__ int3 cell_of(const StepConsts& c, float4 p) {
+  return make_int3(cell_coord(p.x, c.llim[0], c.h, c.dims[0]),
+                   cell_coord(p.y, c.llim[1], c.h, c.dims[1]),
+                   cell_coord(p.z, c.llim[2], c.h, c.dims[2]));
+}
+
+// xyzToId (fluids/Simulator.cu:44-53): x-major, z fastest.
+__device__ __forceinline__ int cell_index(const StepConsts& c, int x, int y, int z) {
+  return (x * c.dims[1] + y) * c.dims[2] + z;
+}
+
+// |a - b|^2 with the fused multiply-adds nvcc forms for the reference's
+// d.x*d.x + d.y*d.y + d.z*d.z.
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+  return fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+}
+
+// W(r^2) for r^2 < h^2 (getPoly6::operator(), fluids/Simulator.cu:84-89).
+__device__ __forceinline__ float poly6_inside(const StepConsts& c, float r2) {
+  float d = c.h2 - r2;
+  return c.poly6_coef * d * d * d;
+}
+
+// w^n for the s_corr term (the reference calls powf, fluids/Simulator_kernel.cuh:165).
+__device__ __forceinline__ float pow_corr(const StepConsts& c, float w) {
+  switch (c.npow) {
+    case 1: return w;
+    case 2: return w * w;
+    case 3: return w * w * w;
+    case 4: { float w2 = w * w; return w2 * w2; }
+    default: return powf(w, c.n_corr);
+  }
+}
+
+// DensityBoundary (fluids/Simulator.cu:139-161), evaluated only when
+// k_boundaryDensity != 0.
+__device__ __forceinline__ float density_at(float d, float h) {
+  const float k = (float)(2.0 * kRefPi / 3.0);
+  if (d > h) return 0.f;
+  if (d <= 0.f) return k;
+  return k * (h - d) * (h - d) * (h + d);
+}
+
+__device__ __forceinline__ float boundary_density(const StepConsts& c, float4 p) {
+  return density_at(c.ulim[0] - p.x, c.h) + density_at(p.x - c.llim[0], c.h) +
+         density_at(c.ulim[1] - p.y, c.h) + density_at(p.y - c.llim[1], c.h) +
+         density_at(c.ulim[2] - p.z, c.h) + density_at(p.z - c.llim[2], c.h);
+}
+
+// ---- launch wrappers (grid.cu) ------------------------------------------------
+
+// Scratch of the neighbour grid build, all device pointers owned by the solver.
+struct GridScratch {
+  uint32_t* keys_a;     // [max_particles]
+  uint32_t* keys_b;     // [max_particles]
+  uint32_t* vals_a;     // [max_particles]
+  uint32_t* vals_b;     // [max_particles]
+  uint32_t* cell_count; // [max_cells + 1]
+  uint32_t* cell_start; // [max_cells + 1]  exclusive prefix of cell counts
+  uint32_t* radix_counts;   // [256 * max_sort_tiles]
+  uint32_t* scan_partials;  // [kMaxScanPartials]
+};
+
+constexpr int kScanTile = 2048;
+constexpr int kMaxScanPartials = 8192;
+constexpr int kSortTile = 2048;
+
+int sort_tiles(int n);
+size_t radix_counts_len(int max_particles);
+
+// Hash (optionally predicting x* = x + dt (v + dt g) first), count cells,
+// stable radix sort by cell id, exclusive prefix of counts.
+//   pos/vel != null: predict from them;  xstar != null: hash xstar directly.
+// On return (stream order): *perm_out points at the sorted-slot -> input index
+// array (inside scratch), scratch.cell_start holds cells + 1 prefix entries.
+// keys_copy (optional, n entries) receives the unsorted cell ids.
+cudaError_t build_grid(const StepConsts& c, const float4* pos, const float4* vel,
+                       const float4* xstar, int n, GridScratch& s, const uint32_t** perm_out,
+                       uint32_t* keys_copy, cudaStream_t stream);
+
+// start/end per cell in the reference's format (0/0 for empty cells).
+cudaError_t export_ranges(const StepConsts& c, const uint32_t* cell_start, uint32_t* start,
+                          uint32_t* end, cudaStream_t stream);
+
+// ---- launch wrappers (solver.cu) ----------------------------------------------
+
+struct SolverScratch {
+  float4* xs;       // sorted x (positions at t)
+  float4* xa;       // predicted / iterated positions, ping
+  float4* xb;       // pong
+  uint32_t* iid_s;  // sorted iid
+  float* lambda;
+  float* rho;
+};
+
+// Gather pos/vel/iid into cell order and recompute x* (bit-identical to the hash).
+cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
+                    const uint32_t* iid, int n, SolverScratch& s, cudaStream_t stream);
+
+// lambda_i and rho_i of every particle at positions X.
+cudaError_t launch_lambda(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+                          float* lambda, float* rho, cudaStream_t stream);
+// One Jacobi position update X -> T.
+cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const float* lambda,
+                           const uint32_t* cs, int n, float4* T, cudaStream_t stream);
+// Last position update: x_final -> npos, (x_final - x) / dt -> vel, and the
+// permuted inputs -> pos, iid.
+cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const float* lambda,
+                                 const uint32_t* cs, int n, const SolverScratch& s, float4* pos,
+                                 float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream);
+// XSPH: nvel = vel + c sum_j 2 (v_j - v_i) W / (rho_i + rho_j).
+cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const float* rho,
+                        const uint32_t* cs, int n, float4* NV, cudaStream_t stream);
+
+// Kernel launches of one build_grid call with n particles and c.cells cells.
+int grid_launches(const StepConsts& c, int n);
+
+}  // namespace pbf

@@ -1,0 +1,168 @@
+"""Headless scene sources: the particle lattices the solver is tested and
+measured on, and their solver parameters.
+
+The reference fills its buffers from ParticleSource subclasses
+(fluids/ParticleSource.h:4-17; FixedCubeSource / DoubleDamSource generate
+jittered lattices with srand(27), fluids/DoubleDamSource.cpp:5-21).  These
+sources keep that interface idea (a source produces positions, velocities and
+iids for a box) with seeded numpy jitter and y up:
+
+  dam_break     8,000 particles: 20x20x20 lattice in a 2.0 x 1.0 x 1.0 box
+  double_dam    32,768 particles: two 16x32x32 lattices at opposite x walls of
+                a 3.2 x 1.6 x 1.6 box
+  large_sweep   1,048,576 particles: 128x64x128 lattice in a 12.8 x 6.4 x 6.4
+                box whose x-max wall moves as x_w(t) = 12.8 - 1.6 (1 - cos(2 pi t / 4 s))
+  ensemble      256 independent a x b x c lattices, a, b, c uniform in [12, 40],
+                each in its own (2a d, 2b d, 2c d) box
+  inverse       15,625 particles: 25x25x25 lattice in a 2.0 x 1.0 x 1.0 box
+
+Lattice spacing d = 0.05, jitter uniform +-0.005 per coordinate, velocities 0.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Callable, List, Optional, Tuple
+
+import numpy as np
+
+from ._abi import PbfParams, default_params
+
+SPACING = 0.05
+JITTER = 0.005
+H = 0.1
+FRAME_DT = 1.0 / 60.0
+SUBSTEPS = 2
+
+
+def rest_density(h: float = H, spacing: float = SPACING) -> float:
+    """Poly6 density (mass 1) of a particle in an unjittered cubic lattice,
+    summed in float64 over every lattice site with r < h, self included."""
+    m = int(math.ceil(h / spacing)) + 1
+    coef = 315.0 / (64.0 * math.pi * h ** 9)
+    rho = 0.0
+    for a in range(-m, m + 1):
+        for b in range(-m, m + 1):
+            for c in range(-m, m + 1):
+                r2 = (a * a + b * b + c * c) * spacing * spacing
+                if r2 < h * h * (1 - 1e-12):
+                    rho += coef * (h * h - r2) ** 3
+    return float(np.float32(rho))
+
+
+def scene_params(niter: int = 4) -> PbfParams:
+    """Solver parameters of the dam-break scenes: h = 0.1, pho0 = lattice
+    density, epsilon = 100, s_corr k = 0.1 n = 4 dq = 0.2 h, XSPH c = 0.01,
+    gravity 9.8 along -y, dt = 1/120 s (a 1/60 s frame in 2 steps)."""
+    p = default_params()
+    p.niter = niter
+    p.h = H
+    p.pho0 = rest_density()
+    p.lambda_eps = 100.0
+    p.delta_q = 0.2 * H
+    p.k_corr = 0.1
+    p.n_corr = 4.0
+    p.k_boundaryDensity = 0.0
+    p.c_XSPH = 0.01
+    p.g = 9.8
+    p.up[0], p.up[1], p.up[2] = 0.0, 1.0, 0.0
+    p.dt = FRAME_DT / SUBSTEPS
+    return p
+
+
+def lattice(counts: Tuple[int, int, int], origin, rng: np.random.Generator,
+            spacing: float = SPACING, jitter: float = JITTER) -> np.ndarray:
+    """(a*b*c, 4) float32 positions: origin + d/2 + index * d + U(-jitter, jitter),
+    x slowest, z fastest (the reference's loop order, fluids/FixedCubeSource.cpp:12-20)."""
+    a, b, c = counts
+    ii, jj, kk = np.meshgrid(np.arange(a), np.arange(b), np.arange(c), indexing="ij")
+    base = np.stack([ii.ravel(), jj.ravel(), kk.ravel()], 1).astype(np.float64)
+    p = np.asarray(origin, np.float64) + spacing / 2 + base * spacing
+    p += rng.uniform(-jitter, jitter, size=p.shape)
+    out = np.zeros((p.shape[0], 4), np.float32)
+    out[:, :3] = p
+    return out
+
+
+@dataclass
+class Scene:
+    name: str
+    pos: np.ndarray                      # (n, 4) float32
+    vel: np.ndarray                      # (n, 4) float32
+    ulim: Tuple[float, float, float]
+    llim: Tuple[float, float, float]
+    wall: Optional[Callable[[float], Tuple[Tuple[float, ...], Tuple[float, ...]]]] = None
+    params: PbfParams = field(default_factory=scene_params)
+
+    @property
+    def n(self) -> int:
+        return self.pos.shape[0]
+
+    def limits_at(self, t: float):
+        """(ulim, llim) at time t (the moving wall; static boxes ignore t)."""
+        if self.wall is None:
+            return self.ulim, self.llim
+        return self.wall(t)
+
+
+def _zeros_like(p):
+    return np.zeros_like(p)
+
+
+def dam_break(seed: int = 0, niter: int = 4) -> Scene:
+    rng = np.random.default_rng(seed)
+    pos = lattice((20, 20, 20), (0.0, 0.0, 0.0), rng)
+    return Scene("dam_break_8k", pos, _zeros_like(pos), (2.0, 1.0, 1.0), (0.0, 0.0, 0.0),
+                 params=scene_params(niter))
+
+
+def double_dam(seed: int = 0, niter: int = 4) -> Scene:
+    rng = np.random.default_rng(seed)
+    a = lattice((16, 32, 32), (0.0, 0.0, 0.0), rng)
+    b = lattice((16, 32, 32), (3.2 - 16 * SPACING, 0.0, 0.0), rng)
+    pos = np.concatenate([a, b])
+    return Scene("double_dam_32k", pos, _zeros_like(pos), (3.2, 1.6, 1.6), (0.0, 0.0, 0.0),
+                 params=scene_params(niter))
+
+
+def sweep_wall_x(t: float) -> float:
+    """x-max wall of the large sweep: 12.8 - 1.6 (1 - cos(2 pi t / 4 s))."""
+    return 12.8 - 1.6 * (1.0 - math.cos(2.0 * math.pi * t / 4.0))
+
+
+def large_sweep(seed: int = 0, niter: int = 4) -> Scene:
+    rng = np.random.default_rng(seed)
+    pos = lattice((128, 64, 128), (0.0, 0.0, 0.0), rng)
+
+    def wall(t: float):
+        return (sweep_wall_x(t), 6.4, 6.4), (0.0, 0.0, 0.0)
+
+    return Scene("large_sweep_1m", pos, _zeros_like(pos), (12.8, 6.4, 6.4), (0.0, 0.0, 0.0), wall=wall,
+                 params=scene_params(niter))
+
+
+def inverse_scene(seed: int = 0, niter: int = 4) -> Scene:
+    rng = np.random.default_rng(seed)
+    pos = lattice((25, 25, 25), (0.0, 0.0, 0.0), rng)
+    return Scene("inverse_15k", pos, _zeros_like(pos), (2.0, 1.0, 1.0), (0.0, 0.0, 0.0),
+                 params=scene_params(niter))
+
+
+def ensemble(seed: int = 0, count: int = 256, niter: int = 4) -> List[Scene]:
+    rng = np.random.default_rng(seed)
+    dims = rng.integers(12, 41, size=(count, 3))
+    out = []
+    for s, (a, b, c) in enumerate(dims):
+        pos = lattice((int(a), int(b), int(c)), (0.0, 0.0, 0.0), rng)
+        ext = (2 * a * SPACING, 2 * b * SPACING, 2 * c * SPACING)
+        out.append(Scene(f"ensemble_{s}", pos, _zeros_like(pos), tuple(float(e) for e in ext),
+                         (0.0, 0.0, 0.0), params=scene_params(niter)))
+    return out
+
+
+SCENES = {
+    "dam_break": dam_break,
+    "double_dam": double_dam,
+    "large_sweep": large_sweep,
+    "inverse": inverse_scene,
+}

@@ -1,0 +1,127 @@
+"""CPU tests of the boundary: libpbf.so builds, exports every symbol declared
+in include/pbf.h, mirrors pbf_params' layout, and validates arguments before
+touching the GPU."""
+from __future__ import annotations
+
+import ctypes
+import re
+import subprocess
+import textwrap
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "pbf.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"^\s*(?:[A-Za-z_][\w\s\*]*?[\s\*])(pbf_\w+)\s*\(", text, flags=re.M)
+
+
+def test_header_declares_exported_list(pbf):
+    assert declared_functions() == list(pbf.EXPORTED)
+
+
+def test_library_exports_every_declared_symbol(pbf):
+    L = pbf.lib()
+    for name in declared_functions():
+        assert hasattr(L, name), name
+    out = subprocess.run(["nm", "-D", "--defined-only", str(pbf.lib_path())], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert set(declared_functions()) <= exported
+
+
+def test_params_layout_matches_c(pbf, tmp_path):
+    """ctypes mirror == C struct (size and every field offset), checked by gcc."""
+    fields = [f for f, _ in pbf.PbfParams._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text(textwrap.dedent(f"""
+        #include <stdio.h>
+        #include <stddef.h>
+        #include "{HEADER}"
+        int main(void) {{
+          printf("%zu\\n", sizeof(pbf_params));
+          {''.join(f'printf("%zu\\n", offsetof(pbf_params, {f}));' for f in fields)}
+          return 0;
+        }}
+    """))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
+    vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    assert vals[0] == ctypes.sizeof(pbf.PbfParams)
+    for f, off in zip(fields, vals[1:]):
+        assert getattr(pbf.PbfParams, f).offset == off, f
+
+
+def test_default_params_are_the_reference_defaults(pbf):
+    """fluids/FluidSystem.cpp:15-25, fluids/helper.h:4-9, fluids/Simulator.cu:174."""
+    p = pbf.default_params()
+    f = ctypes.c_float
+    assert p.niter == 4
+    assert p.g == f(9.8).value and p.h == f(0.1).value and p.dt == f(0.0083).value
+    assert p.pho0 == 8000.0 and p.lambda_eps == 1000.0
+    assert p.delta_q == f(0.3 * f(0.1).value).value  # 0.3 * params.h in double
+    assert p.k_corr == f(0.001).value and p.n_corr == 4.0
+    assert p.k_boundaryDensity == 0.0 and p.c_XSPH == 0.5
+    assert list(p.up) == [0.0, 0.0, 1.0]
+    assert p.lim_eps == f(1e-3).value and p.kernel_eps == f(1e-4).value and p.max_dp == f(0.1).value
+
+
+def test_argument_errors_need_no_gpu(pbf):
+    L = pbf.lib()
+    h = ctypes.c_void_p()
+    u = (ctypes.c_float * 3)(1, 1, 1)
+    l = (ctypes.c_float * 3)(0, 0, 0)
+    assert L.pbf_create(None, u, l, 10, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
+    p = pbf.default_params()
+    p.niter = 0
+    assert L.pbf_create(ctypes.byref(p), u, l, 10, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
+    assert b"niter" in L.pbf_last_error()
+    p = pbf.default_params()
+    p.h = float("nan")
+    assert L.pbf_create(ctypes.byref(p), u, l, 10, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
+    p = pbf.default_params()
+    bad = (ctypes.c_float * 3)(0, 1, 1)  # ulim.x == llim.x
+    assert L.pbf_create(ctypes.byref(p), bad, l, 10, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_create(ctypes.byref(p), u, l, -1, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_step(None, None, None, None, None, None, 1, None) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_set_params(None, ctypes.byref(p)) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_destroy(None) == pbf.PBF_OK
+    assert L.pbf_abi_version() == 1
+    assert L.pbf_status_string(pbf.PBF_ERR_CAPACITY) == b"capacity exceeded"
+    with pytest.raises(pbf.PbfError) as e:
+        pbf.check(pbf.PBF_ERR_TIMEOUT, "x")
+    assert e.value.status == pbf.PBF_ERR_TIMEOUT
+
+
+def test_create_without_gpu_reports_cuda_error(pbf):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    p = pbf.default_params()
+    u = (ctypes.c_float * 3)(1, 1, 1)
+    l = (ctypes.c_float * 3)(0, 0, 0)
+    assert pbf.lib().pbf_create(ctypes.byref(p), u, l, 10, ctypes.byref(h)) == pbf.PBF_ERR_CUDA
+    assert h.value is None
+
+
+def test_cpp_facade_compiles(tmp_path):
+    """The C++ Simulator facade compiles against the C ABI (no GPU call made)."""
+    src = tmp_path / "facade.cpp"
+    src.write_text(textwrap.dedent(f"""
+        #include "{ROOT / 'pbf-cuda_gb300' / 'csrc' / 'Simulator.hpp'}"
+        int use(pbf::Simulator& s, void* p, void* np, void* v, void* nv, uint32_t* iid) {{
+          s.step(p, np, v, nv, iid, 10);
+          pbf_params q = s.saveParams();
+          s.loadParams(q);
+          s.setLim({{1, 1, 1}}, {{0, 0, 0}});
+          return q.niter;
+        }}
+    """))
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", str(src)], check=True)

@@ -1,0 +1,269 @@
+"""GPU parity tests: the CUDA path through the C ABI against the CPU oracle.
+
+Bars (stated per test):
+  * cell ids, stable order, cell ranges, permuted pos/iid: bit-exact;
+  * one step from an identical state: max |x - x_fp64| <= 1e-5 h (= 1e-6)
+    with the reference's own parameters (fluids/FluidSystem.cpp:15-25), and
+    with the dam-break scene parameters at one solver iteration;
+  * determinism: two runs are bitwise identical.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL_X = 1e-5 * 0.1  # 1e-5 h
+
+
+def ref_params(pbf, niter=4):
+    p = pbf.default_params()
+    p.up[0], p.up[1], p.up[2] = 0.0, 1.0, 0.0
+    p.niter = niter
+    return p
+
+
+def gpu_step(pbf, params, ulim, llim, pos, vel, iid=None, capacity=None):
+    import torch
+
+    n = pos.shape[0]
+    cap = max(n, 1) if capacity is None else capacity
+    if iid is None:
+        iid = np.arange(n, dtype=np.uint32)
+    d = {}
+    d["pos"] = torch.zeros(cap, 4, device="cuda")
+    d["vel"] = torch.zeros(cap, 4, device="cuda")
+    d["npos"] = torch.zeros(cap, 4, device="cuda")
+    d["nvel"] = torch.zeros(cap, 4, device="cuda")
+    d["iid"] = torch.zeros(cap, dtype=torch.int32, device="cuda")
+    d["pos"][:n] = torch.from_numpy(np.ascontiguousarray(pos, np.float32))
+    d["vel"][:n] = torch.from_numpy(np.ascontiguousarray(vel, np.float32))
+    d["iid"][:n] = torch.from_numpy(iid.astype(np.int32))
+    with pbf.Simulator(params, ulim, llim, cap) as sim:
+        sim.step(d["pos"], d["npos"], d["vel"], d["nvel"], d["iid"], n)
+        rho = sim.density(n) if n else torch.zeros(0, device="cuda")
+        torch.cuda.synchronize()
+    out = {k: v[:n].cpu().numpy() for k, v in d.items()}
+    out["iid"] = out["iid"].astype(np.uint32)
+    out["rho"] = rho.cpu().numpy()
+    return out
+
+
+def compare_grid(pbf, oracle, params, ulim, llim, xs):
+    import torch
+
+    n = xs.shape[0]
+    with pbf.Simulator(params, ulim, llim, max(n, 1)) as sim:
+        g = sim.build_grid(torch.from_numpy(np.ascontiguousarray(xs, np.float32)).cuda())
+        torch.cuda.synchronize()
+        got = {k: (v.cpu().numpy().astype(np.uint32) if hasattr(v, "cpu") else v) for k, v in g.items()}
+    ref = oracle.grid(params, ulim, llim, xs)
+    assert got["dims"] == ref["dims"]
+    np.testing.assert_array_equal(got["keys"], ref["keys"])
+    np.testing.assert_array_equal(got["perm"], ref["perm"])
+    np.testing.assert_array_equal(got["start"], ref["start"])
+    np.testing.assert_array_equal(got["end"], ref["end"])
+
+
+@pytest.mark.parametrize("scene", ["dam_break", "double_dam"])
+def test_grid_bit_exact(pbf, oracle, cuda, scene):
+    sc = getattr(pbf.scenes, scene)(seed=3)
+    xs = oracle.predict(sc.params, sc.pos, sc.vel)
+    compare_grid(pbf, oracle, sc.params, sc.ulim, sc.llim, xs)
+    # a shuffled input order: ties must keep input order
+    perm = np.random.default_rng(0).permutation(sc.n)
+    compare_grid(pbf, oracle, sc.params, sc.ulim, sc.llim, xs[perm])
+
+
+def test_grid_edge_cases(pbf, oracle, cuda):
+    p = ref_params(pbf)
+    rng = np.random.default_rng(11)
+    # out-of-box and NaN positions clamp into edge cells / cell 0
+    xs = np.zeros((5000, 4), np.float32)
+    xs[:, :3] = rng.uniform(-0.5, 2.5, size=(5000, 3))
+    xs[7, 1] = np.nan
+    xs[8, :3] = np.inf
+    compare_grid(pbf, oracle, p, (2.0, 1.0, 1.0), (0.0, 0.0, 0.0), xs)
+    # everything in one cell (every key equal: ranks = input order)
+    xs = np.zeros((4099, 4), np.float32)
+    xs[:, :3] = 0.31 + rng.uniform(0, 0.05, size=(4099, 3))
+    compare_grid(pbf, oracle, p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), xs)
+    # one particle; a one-cell box
+    compare_grid(pbf, oracle, p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), xs[:1])
+    compare_grid(pbf, oracle, p, (0.05, 0.05, 0.05), (0.0, 0.0, 0.0), xs[:100])
+    # ragged sizes around the sort tile (2048) and a key range needing 3 radix passes
+    big_u = (12.8, 6.4, 6.4)
+    for n in (2047, 2048, 2049, 70001):
+        xs = np.zeros((n, 4), np.float32)
+        xs[:, :3] = rng.uniform(0, 1, size=(n, 3)) * np.array(big_u, np.float32)
+        compare_grid(pbf, oracle, p, big_u, (0.0, 0.0, 0.0), xs)
+
+
+def test_step_reference_params_matches_fp64(pbf, oracle, cuda):
+    """Dam break (8,000 particles), reference parameters, 4 iterations."""
+    sc = pbf.scenes.dam_break(seed=0)
+    p = ref_params(pbf, 4)
+    got = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
+    ref = oracle.step(p, sc.ulim, sc.llim, sc.pos, sc.vel, np.arange(sc.n, dtype=np.uint32), prec="f64")
+    np.testing.assert_array_equal(got["iid"], ref["iid"])
+    np.testing.assert_array_equal(got["pos"], sc.pos[ref["iid"]])
+    err = np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max()
+    assert err <= TOL_X, err
+    # v = dx / dt: the position bar scaled by 1/dt
+    assert np.abs(got["vel"][:, :3] - ref["vel"][:, :3]).max() <= TOL_X / p.dt
+    assert np.abs(got["nvel"][:, :3] - ref["nvel"][:, :3]).max() <= TOL_X / p.dt
+    assert np.abs(got["rho"] - ref["rho"]).max() <= 1e-5 * ref["rho"].max()
+    np.testing.assert_array_equal(got["npos"][:, 3], got["pos"][:, 3])
+
+
+def test_step_double_dam_reference_params(pbf, oracle, cuda):
+    sc = pbf.scenes.double_dam(seed=0)
+    p = ref_params(pbf, 4)
+    got = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
+    ref = oracle.step(p, sc.ulim, sc.llim, sc.pos, sc.vel, np.arange(sc.n, dtype=np.uint32), prec="f64")
+    np.testing.assert_array_equal(got["iid"], ref["iid"])
+    assert np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max() <= TOL_X
+
+
+def test_step_scene_params_one_iteration(pbf, oracle, cuda):
+    """Dam-break scene parameters (eps 100, s_corr k 0.1), one iteration."""
+    sc = pbf.scenes.dam_break(seed=1)
+    p = sc.params
+    p.niter = 1
+    got = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
+    ref = oracle.step(p, sc.ulim, sc.llim, sc.pos, sc.vel, np.arange(sc.n, dtype=np.uint32), prec="f64")
+    np.testing.assert_array_equal(got["iid"], ref["iid"])
+    assert np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max() <= TOL_X
+
+
+def test_step_moving_particles_and_walls(pbf, oracle, cuda):
+    """Non-zero velocities, a shuffled input order, a narrowed box and a
+    boundary-density term: every branch of the step, vs FP64."""
+    sc = pbf.scenes.dam_break(seed=4)
+    p = ref_params(pbf, 2)
+    p.k_boundaryDensity = 0.05
+    rng = np.random.default_rng(2)
+    order = rng.permutation(sc.n)
+    pos = sc.pos[order]
+    vel = np.zeros_like(pos)
+    vel[:, :3] = rng.normal(0, 0.3, size=(sc.n, 3))
+    iid = order.astype(np.uint32)
+    ulim, llim = (1.5, 1.0, 1.0), (0.0, 0.0, 0.0)
+    got = gpu_step(pbf, p, ulim, llim, pos, vel, iid)
+    ref = oracle.step(p, ulim, llim, pos, vel, iid, prec="f64")
+    np.testing.assert_array_equal(got["iid"], ref["iid"])
+    assert np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max() <= TOL_X
+    assert got["npos"][:, 0].max() <= np.float32(1.5 - 1e-3)
+
+
+def test_step_is_deterministic(pbf, cuda):
+    sc = pbf.scenes.double_dam(seed=5)
+    a = gpu_step(pbf, sc.params, sc.ulim, sc.llim, sc.pos, sc.vel)
+    b = gpu_step(pbf, sc.params, sc.ulim, sc.llim, sc.pos, sc.vel)
+    for k in ("pos", "vel", "npos", "nvel", "iid", "rho"):
+        np.testing.assert_array_equal(a[k], b[k])
+
+
+def test_step_small_and_clustered(pbf, oracle, cuda):
+    p = ref_params(pbf, 3)
+    one = np.array([[0.5, 0.5, 0.5, 1.0]], np.float32)
+    got = gpu_step(pbf, p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), one, np.zeros_like(one), capacity=17)
+    ref = oracle.step(p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), one, np.zeros_like(one), np.zeros(1, np.uint32),
+                      prec="f64")
+    assert np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max() <= TOL_X
+    assert got["npos"][0, 3] == 1.0
+    # 600 particles packed into ~one cell: every candidate list is the whole cluster
+    rng = np.random.default_rng(9)
+    pos = np.zeros((600, 4), np.float32)
+    pos[:, :3] = 0.5 + rng.uniform(0, 0.1, size=(600, 3))
+    got = gpu_step(pbf, p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), pos, np.zeros_like(pos))
+    ref = oracle.step(p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), pos, np.zeros_like(pos), np.arange(600, dtype=np.uint32),
+                      prec="f32")
+    np.testing.assert_array_equal(got["iid"], ref["iid"])
+    assert np.all(np.isfinite(got["npos"]))
+
+
+def test_errors_on_gpu(pbf, cuda):
+    import torch
+
+    p = ref_params(pbf)
+    sim = pbf.Simulator(p, (1.0, 1.0, 1.0), (0.0, 0.0, 0.0), 64)
+    t = [torch.zeros(128, 4, device="cuda") for _ in range(4)]
+    iid = torch.zeros(128, dtype=torch.int32, device="cuda")
+    with pytest.raises(pbf.PbfError) as e:
+        sim.step(t[0], t[1], t[2], t[3], iid, 100)
+    assert e.value.status == pbf.PBF_ERR_CAPACITY
+    with pytest.raises(pbf.PbfError) as e:
+        sim.step(t[0], t[0], t[2], t[3], iid, 10)
+    assert e.value.status == pbf.PBF_ERR_INVALID_ARG
+    with pytest.raises(pbf.PbfError) as e:
+        sim.density(10)
+    assert e.value.status == pbf.PBF_ERR_NOT_READY
+    with pytest.raises(pbf.PbfError) as e:
+        sim.setLim((10.0, 10.0, 10.0), (0.0, 0.0, 0.0))
+    assert e.value.status == pbf.PBF_ERR_CAPACITY
+    sim.setLim((1.5, 1.0, 1.0), (0.0, 0.0, 0.0))  # within the 4x cell reserve
+    assert sim.getLim()[0] == [1.5, 1.0, 1.0]
+    q = sim.saveParams()
+    q.niter = 2
+    sim.loadParams(q)
+    assert sim.saveParams().niter == 2
+    sim.step(t[0], t[1], t[2], t[3], iid, 0)  # n == 0 is a no-op
+    sim.close()
+
+
+def test_moving_wall_sequence(pbf, oracle, cuda):
+    """A wall that moves every step (setLim before each step, as the
+    reference's FluidSystem::stepSimulate does): 6 steps, each compared with
+    the FP64 oracle from the GPU's own previous state."""
+    import torch
+
+    sc = pbf.scenes.dam_break(seed=6)
+    p = ref_params(pbf, 4)
+    st = pbf.ParticleState(sc.pos, sc.vel)
+    with pbf.Simulator(p, (2.0, 1.0, 1.0), (0.0, 0.0, 0.0), sc.n) as sim:
+        for k in range(6):
+            ulim = (2.0 - 0.08 * k, 1.0, 1.0)
+            pos0 = st.pos.cpu().numpy()
+            vel0 = st.vel.cpu().numpy()
+            iid0 = st.iid[: st.n].cpu().numpy().astype(np.uint32)
+            sim.setLim(ulim, (0.0, 0.0, 0.0))
+            st.step(sim)
+            torch.cuda.synchronize()
+            ref = oracle.step(p, ulim, (0.0, 0.0, 0.0), pos0, vel0, iid0, prec="f64")
+            np.testing.assert_array_equal(st.iid[: st.n].cpu().numpy().astype(np.uint32), ref["iid"])
+            assert np.abs(st.pos.cpu().numpy()[:, :3] - ref["npos"][:, :3]).max() <= TOL_X
+
+
+def test_large_sweep_one_step(pbf, oracle, cuda):
+    """1,048,576 particles (the large-sweep lattice), scene parameters, one
+    step of 4 iterations: order bit-exact vs the float port, outputs finite and
+    inside the box, keys of the output order non-decreasing, deterministic."""
+    sc = pbf.scenes.large_sweep(seed=0)
+    p = sc.params
+    got = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
+    xs = oracle.predict(p, sc.pos, sc.vel)
+    g = oracle.grid(p, sc.ulim, sc.llim, xs)
+    np.testing.assert_array_equal(got["iid"], g["perm"])
+    np.testing.assert_array_equal(got["pos"], sc.pos[g["perm"]])
+    assert np.all(np.diff(g["keys"][g["perm"]].astype(np.int64)) >= 0)
+    assert np.all(np.isfinite(got["npos"])) and np.all(np.isfinite(got["nvel"]))
+    lo = np.float32(1e-3)
+    assert got["npos"][:, :3].min() >= lo - 1e-7
+    assert np.all(got["npos"][:, :3] <= np.array(sc.ulim, np.float32) - lo + 1e-6)
+    again = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
+    np.testing.assert_array_equal(again["npos"], got["npos"])
+
+
+def test_large_sweep_one_iteration_vs_port(pbf, oracle, cuda):
+    """1M particles, one iteration: positions vs the float port within 4 float
+    ulps of the largest coordinate (12.8: ulp 9.5e-7)."""
+    sc = pbf.scenes.large_sweep(seed=0)
+    p = sc.params
+    p.niter = 1
+    got = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
+    ref = oracle.step(p, sc.ulim, sc.llim, sc.pos, sc.vel, np.arange(sc.n, dtype=np.uint32), prec="f32")
+    np.testing.assert_array_equal(got["iid"], ref["iid"])
+    err = np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max()
+    assert err <= 4 * 9.5367e-7, err

@@ -1,0 +1,75 @@
+"""CPU tests of the headless scene sources and their parameters."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def test_rest_density_is_the_lattice_poly6_sum(pbf):
+    rho = pbf.scenes.rest_density()
+    h, d = 0.1, 0.05
+    coef = 315.0 / (64.0 * math.pi * h ** 9)
+    # 27 sites with r < h in a cubic lattice of spacing h/2: 1 + 6 + 12 + 8
+    want = coef * (h * h) ** 3 + 6 * coef * (h * h - d * d) ** 3 + 12 * coef * (h * h - 2 * d * d) ** 3 \
+        + 8 * coef * (h * h - 3 * d * d) ** 3
+    assert abs(rho - want) < 1e-3
+    assert abs(rho - 8078.20) < 0.01
+
+
+def test_scene_sizes_and_boxes(pbf):
+    s = pbf.scenes
+    assert s.inverse_scene().n == 15625
+    for scene, n in ((s.dam_break(), 8000), (s.double_dam(), 32768)):
+        assert scene.n == n
+        assert scene.pos.dtype == np.float32 and scene.pos.shape == (n, 4)
+        assert np.all(scene.pos[:, :3] > np.array(scene.llim)) and np.all(scene.pos[:, :3] < np.array(scene.ulim))
+        assert np.all(scene.vel == 0)
+    big = s.large_sweep()
+    assert big.n == 1 << 20
+    assert big.ulim == (12.8, 6.4, 6.4)
+
+
+def test_lattice_jitter_is_seeded_and_bounded(pbf):
+    s = pbf.scenes
+    a, b = s.dam_break(seed=7), s.dam_break(seed=7)
+    np.testing.assert_array_equal(a.pos, b.pos)
+    assert not np.array_equal(a.pos, s.dam_break(seed=8).pos)
+    ii = np.arange(20)
+    grid = 0.025 + 0.05 * ii
+    dev = a.pos[:, 0].reshape(20, 400) - grid[:, None]
+    assert np.abs(dev).max() <= 0.005 + 1e-6
+
+
+def test_double_dam_against_opposite_walls(pbf):
+    sc = pbf.scenes.double_dam()
+    left, right = sc.pos[:16384], sc.pos[16384:]
+    assert left[:, 0].max() < 0.81 and right[:, 0].min() > 3.2 - 0.81
+
+
+def test_sweep_wall(pbf):
+    s = pbf.scenes
+    assert s.sweep_wall_x(0.0) == 12.8
+    assert abs(s.sweep_wall_x(2.0) - 9.6) < 1e-12
+    assert abs(s.sweep_wall_x(4.0) - 12.8) < 1e-12
+    u, l = s.large_sweep().limits_at(1.0)
+    assert abs(u[0] - 11.2) < 1e-12 and l == (0.0, 0.0, 0.0)
+
+
+def test_ensemble(pbf):
+    scenes = pbf.scenes.ensemble(seed=0)
+    assert len(scenes) == 256
+    ns = np.array([sc.n for sc in scenes])
+    assert ns.min() >= 12 ** 3 and ns.max() <= 40 ** 3
+    assert 3.5e6 < ns.sum() < 5.5e6
+    for sc in scenes[:8]:
+        assert np.all(sc.pos[:, :3] < np.array(sc.ulim))
+
+
+def test_scene_params(pbf):
+    p = pbf.scenes.scene_params()
+    assert p.niter == 4 and abs(p.pho0 - 8078.2) < 0.01
+    assert p.lambda_eps == 100.0 and abs(p.delta_q - 0.02) < 1e-7 and abs(p.k_corr - 0.1) < 1e-7
+    assert p.n_corr == 4.0 and abs(p.c_XSPH - 0.01) < 1e-9
+    assert list(p.up) == [0.0, 1.0, 0.0]
+    assert abs(p.dt - 1.0 / 120.0) < 1e-9
