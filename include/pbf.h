@@ -9,8 +9,9 @@
  *
  * Differences from the reference interface, all deliberate:
  *  - buffers are device pointers to float4 (x, y, z, w) instead of OpenGL
- *    buffer names of float3 (fluids/Simulator.cpp:20-36); w is carried through
- *    the permutation untouched on pos and written as 0 on outputs;
+ *    buffer names of float3 (fluids/Simulator.cpp:20-36); pos.w is a
+ *    per-particle payload carried with the particle (to npos.w), velocity w
+ *    components are written as 0;
  *  - every call returns a pbf_status instead of exit()ing inside
  *    checkCudaErrors (common/cuda_inc/helper_cuda.h:1000-1014);
  *  - pbf_step is asynchronous on the given stream (the reference synchronises

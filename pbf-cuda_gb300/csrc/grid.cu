@@ -203,7 +203,7 @@ k_radix_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restri
     const uint32_t d = valid ? (key[k] >> shift) & (kRadix - 1) : (uint32_t)kRadix;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const uint32_t r = __popc(peers & lt);
-    const uint32_t b = valid ? whist[warp][d] : 0u;
+    const uint32_t b = whist[warp][valid ? d : 0u];  // index stays inside the table
     __syncwarp();
     if (valid && r == 0) whist[warp][d] = b + __popc(peers);
     __syncwarp();
@@ -227,8 +227,10 @@ k_radix_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restri
     if (idx < n) {
       const uint32_t d = (key[k] >> shift) & (kRadix - 1);
       const uint32_t dst = whist[warp][d] + rank[k];
-      if (keys_out) keys_out[dst] = key[k];
-      vals_out[dst] = val[k];
+      if (dst < (uint32_t)n) {  // always true for consistent counts; never write out of range
+        if (keys_out) keys_out[dst] = key[k];
+        vals_out[dst] = val[k];
+      }
     }
   }
 }

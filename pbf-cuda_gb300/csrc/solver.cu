@@ -23,12 +23,13 @@ namespace {
 constexpr int kThreads = 256;
 
 // Sorted-slot range [s, e) of cells (x, y, z-1 .. z+1) clipped to the grid.
+// cs[cells] == n, so e <= n; the clamp keeps even an inconsistent table in range.
 __device__ __forceinline__ void column_run(const StepConsts& c, const uint32_t* __restrict__ cs,
-                                           int x, int y, int z, int& s, int& e) {
+                                           int n, int x, int y, int z, int& s, int& e) {
   const int zlo = max(z - 1, 0), zhi = min(z + 1, c.dims[2] - 1);
   const int base = (x * c.dims[1] + y) * c.dims[2];
   s = (int)__ldg(cs + base + zlo);
-  e = (int)__ldg(cs + base + zhi + 1);
+  e = min((int)__ldg(cs + base + zhi + 1), n);
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -37,7 +38,7 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
           float4* __restrict__ xs, float4* __restrict__ xa, uint32_t* __restrict__ iid_s) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  const uint32_t p = perm[k];
+  const uint32_t p = min(perm[k], (uint32_t)(n - 1));  // a permutation of [0, n): the min never binds
   const float4 x = pos[p];
   const float4 v = vel[p];
   const float vx = fmaf(c.dt, c.g[0], v.x), vy = fmaf(c.dt, c.g[1], v.y),
@@ -62,7 +63,7 @@ k_lambda(const float4* __restrict__ X, const uint32_t* __restrict__ cs, int n, S
       const int y = q.y + dy;
       if (y < 0 || y >= c.dims[1]) continue;
       int s, e;
-      column_run(c, cs, x, y, q.z, s, e);
+      column_run(c, cs, n, x, y, q.z, s, e);
       for (int j = s; j < e; ++j) {
         const float4 xj = __ldg(X + j);
         const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
@@ -93,7 +94,8 @@ k_lambda(const float4* __restrict__ X, const uint32_t* __restrict__ cs, int n, S
 // then / pho0, per-component clamp to +-max_dp, wall clamp.
 __device__ __forceinline__ float4 delta_p(const StepConsts& c, const float4* __restrict__ X,
                                           const float* __restrict__ lambda,
-                                          const uint32_t* __restrict__ cs, int i, float4 xi) {
+                                          const uint32_t* __restrict__ cs, int n, int i,
+                                          float4 xi) {
   const int3 q = cell_of(c, xi);
   const float li = lambda[i];
   float ax = 0.f, ay = 0.f, az = 0.f;
@@ -104,7 +106,7 @@ __device__ __forceinline__ float4 delta_p(const StepConsts& c, const float4* __r
       const int y = q.y + dy;
       if (y < 0 || y >= c.dims[1]) continue;
       int s, e;
-      column_run(c, cs, x, y, q.z, s, e);
+      column_run(c, cs, n, x, y, q.z, s, e);
       for (int j = s; j < e; ++j) {
         const float4 xj = __ldg(X + j);
         const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
@@ -135,7 +137,7 @@ k_delta_p(const float4* __restrict__ X, const float* __restrict__ lambda,
           const uint32_t* __restrict__ cs, int n, StepConsts c, float4* __restrict__ T) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  T[i] = delta_p(c, X, lambda, cs, i, X[i]);
+  T[i] = delta_p(c, X, lambda, cs, n, i, X[i]);
 }
 
 // Last iteration: x_final -> npos, v = (x_final - x) * (1/dt) -> vel, and the
@@ -148,7 +150,7 @@ k_delta_p_final(const float4* __restrict__ X, const float* __restrict__ lambda,
                 uint32_t* __restrict__ iid) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const float4 xf = delta_p(c, X, lambda, cs, i, X[i]);
+  const float4 xf = delta_p(c, X, lambda, cs, n, i, X[i]);
   const float4 x0 = xs[i];
   npos[i] = make_float4(xf.x, xf.y, xf.z, x0.w);
   vel[i] = make_float4((xf.x - x0.x) * c.inv_dt, (xf.y - x0.y) * c.inv_dt,
@@ -174,7 +176,7 @@ k_xsph(const float4* __restrict__ X, const float4* __restrict__ V, const float* 
       const int y = q.y + dy;
       if (y < 0 || y >= c.dims[1]) continue;
       int s, e;
-      column_run(c, cs, x, y, q.z, s, e);
+      column_run(c, cs, n, x, y, q.z, s, e);
       for (int j = s; j < e; ++j) {
         const float4 xj = __ldg(X + j);
         const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
