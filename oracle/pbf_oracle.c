@@ -18,11 +18,11 @@
  * multiply-adds nvcc emits for the reference's advect_kernel, which makes the
  * predicted positions, and so the cell ids, bit-identical to the GPU's.
  *
- * Parity pinning: the integer outputs (cell ids, stable order, cell ranges)
- * and the float outputs of this restatement are checked against outputs of the
- * reference's own kernels (fluids/Simulator_kernel.cuh, fluids/Simulator.cu),
- * built unmodified for sm_103a and run on a GB300 by oracle/ref_harness; the
- * recorded vectors live in tests/golden/.
+ * Parity: unpinned.  The reference ships no tests, golden vectors or
+ * known-answer fixtures, and has no CPU path to run here.  This restatement is
+ * checked against closed-form known answers derived from the reference's
+ * formulas (tests/test_oracle.py), not yet against outputs of the reference's
+ * own kernels.
  *
  * Layout: all particle arrays are stride-4 (x, y, z, w) in the oracle's real
  * type; iid is uint32.  The step permutes pos/vel/iid in place exactly like
