@@ -158,6 +158,22 @@ typedef struct pbf_step_profile {
 pbf_status pbf_profile_enable(pbf_solver* s, int on);
 pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out);
 
+/*
+ * One step, same contract and results as pbf_step, for callers that cannot
+ * allocate device memory (no pbf_solver, so no pbf_create).  It has no
+ * counterpart in the reference.  It calls no cudaMalloc or cudaFree: its
+ * scratch is a fixed array of about 3.6 MB inside this library's device image,
+ * held by every GPU that loads the library until the process exits.
+ * Limits: n <= 32768 particles and a box of at most 131072 cells at cell size
+ * h; larger calls return PBF_ERR_CAPACITY.  The first call on each device
+ * looks up the array's device address (set-up), so make it before any stream
+ * capture.  Every call shares the array: calls that overlap on the GPU race,
+ * so serialise them.
+ */
+pbf_status pbf_step_noalloc(const pbf_params* params, const float ulim[3], const float llim[3],
+                            void* pos, void* npos, void* vel, void* nvel, uint32_t* iid, int n,
+                            void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -34,6 +34,7 @@ EXPORTED = (
     "pbf_build_grid",
     "pbf_profile_enable",
     "pbf_profile_read",
+    "pbf_step_noalloc",
 )
 
 
@@ -127,6 +128,7 @@ def _declare(L) -> None:
         "pbf_build_grid": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, vp, vp, vp, P(ctypes.c_int), vp]),
         "pbf_profile_enable": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_profile_read": (ctypes.c_int, [vp, P(PbfStepProfile)]),
+        "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

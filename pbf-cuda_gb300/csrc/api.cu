@@ -479,3 +479,39 @@ pbf_status pbf_build_grid(pbf_solver* s, const void* xstar, int n, uint32_t* key
 }
 
 }  // extern "C"
+
+// ---- helpers for other translation units of the library ---------------------------
+
+namespace pbf {
+
+pbf_status set_error(pbf_status s, const char* msg) { return fail(s, "%s", msg); }
+
+pbf_status set_cuda_error(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+
+pbf_status validate_step_setup(const pbf_params* params, const float ulim[3], const float llim[3],
+                               long long max_cells, StepConsts* out) {
+  pbf_status st = check_params(params);
+  if (st != PBF_OK) return st;
+  if (!ulim || !llim) return fail(PBF_ERR_INVALID_ARG, "limits are NULL");
+  int dims[3];
+  long long cells;
+  if ((st = grid_dims(ulim, llim, params->h, dims, &cells)) != PBF_OK) return st;
+  if (cells > max_cells)
+    return fail(PBF_ERR_CAPACITY, "box needs %lld cells, the limit is %lld", cells, max_cells);
+  *out = make_consts(*params, ulim, llim, dims);
+  return PBF_OK;
+}
+
+pbf_status validate_step_buffers(const void* pos, const void* npos, const void* vel, const void* nvel,
+                                 const void* iid) {
+  const void* bufs[5] = {pos, npos, vel, nvel, iid};
+  for (int a = 0; a < 5; ++a) {
+    if (!bufs[a]) return fail(PBF_ERR_INVALID_ARG, "buffer %d is NULL", a);
+    if (!aligned16(bufs[a]) && a < 4) return fail(PBF_ERR_INVALID_ARG, "buffer %d not 16-byte aligned", a);
+    for (int b = 0; b < a; ++b)
+      if (bufs[a] == bufs[b]) return fail(PBF_ERR_INVALID_ARG, "buffers %d and %d alias", b, a);
+  }
+  return PBF_OK;
+}
+
+}  // namespace pbf

@@ -1,0 +1,159 @@
+// noalloc.cu — pbf_step_noalloc: one PBF step that allocates nothing.
+//
+// Who needs it: callers that cannot call cudaMalloc.  Typical cases are a host
+// application whose device memory is owned by its own memory manager (a fixed
+// arena or budget that a plug-in must not grow, e.g. a renderer's frame loop
+// that lends the solver only its particle buffers), and real-time loops that
+// cannot afford the implicit device-wide synchronisation a cudaMalloc or
+// cudaFree may cause.  Such callers cannot create a pbf_solver, because
+// pbf_create allocates the solver's scratch.
+//
+// How: the scratch lives in one file-scope __device__ array of fixed size,
+// kNoAllocScratchBytes (about 3.6 MB), which is part of this library's device
+// image: every GPU that loads the library holds it until the process exits.
+// It bounds the problem to kNoAllocMaxParticles particles and
+// kNoAllocMaxCells grid cells; larger calls are rejected with
+// PBF_ERR_CAPACITY.  The caller still passes every input and output buffer.
+//
+// Host code cannot use the array's name as a device address (on the host it
+// names a stand-in object).  The device address is looked up once per device
+// with cudaGetSymbolAddress, on the first call made while that device is
+// current, and cached.  That first call therefore does set-up work and should
+// be made before any stream capture.
+//
+// The array is shared by every call and keeps the last call's contents; the
+// step clears what must start at zero (the per-cell counters) itself.  Calls
+// whose work overlaps on the GPU (different streams, different host threads)
+// race on the array: serialise them.
+//
+// The kernels and their sequence are exactly those of pbf_step; only where the
+// scratch comes from differs.
+#include <mutex>
+
+#include "pbf_internal.cuh"
+
+namespace pbf {
+pbf_status set_error(pbf_status s, const char* msg);
+pbf_status set_cuda_error(cudaError_t e, const char* what);
+pbf_status validate_step_setup(const pbf_params* params, const float ulim[3], const float llim[3],
+                               long long max_cells, StepConsts* out);
+pbf_status validate_step_buffers(const void* pos, const void* npos, const void* vel, const void* nvel,
+                                 const void* iid);
+}  // namespace pbf
+
+namespace {
+
+constexpr int kNoAllocMaxParticles = 32768;
+constexpr int kNoAllocMaxCells = 131072;
+constexpr size_t kAlign = 256;
+
+constexpr size_t align_up(size_t v) { return (v + kAlign - 1) / kAlign * kAlign; }
+
+// Byte offsets of every scratch buffer inside the static array.
+constexpr size_t kNp = (size_t)kNoAllocMaxParticles;
+constexpr size_t kNc = (size_t)kNoAllocMaxCells + 1;
+constexpr size_t kSortTiles = (kNp + pbf::kSortTile - 1) / pbf::kSortTile;
+constexpr size_t kOffKeysA = 0;
+constexpr size_t kOffKeysB = kOffKeysA + align_up(4 * kNp);
+constexpr size_t kOffValsA = kOffKeysB + align_up(4 * kNp);
+constexpr size_t kOffValsB = kOffValsA + align_up(4 * kNp);
+constexpr size_t kOffCount = kOffValsB + align_up(4 * kNp);
+constexpr size_t kOffStart = kOffCount + align_up(4 * kNc);
+constexpr size_t kOffRadix = kOffStart + align_up(4 * kNc);
+constexpr size_t kOffPartials = kOffRadix + align_up(4 * 256 * kSortTiles);
+constexpr size_t kOffXs = kOffPartials + align_up(4 * (size_t)pbf::kMaxScanPartials);
+constexpr size_t kOffXa = kOffXs + align_up(16 * kNp);
+constexpr size_t kOffXb = kOffXa + align_up(16 * kNp);
+constexpr size_t kOffIid = kOffXb + align_up(16 * kNp);
+constexpr size_t kOffLambda = kOffIid + align_up(4 * kNp);
+constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
+constexpr size_t kNoAllocScratchBytes = kOffRho + align_up(4 * kNp);
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+void* g_base[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on the current device (set-up on first use).
+pbf_status scratch_base(unsigned char** out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return pbf::set_cuda_error(e, "pbf_step_noalloc: cudaGetDevice");
+  if (dev < 0 || dev >= kMaxDevices) return pbf::set_error(PBF_ERR_INVALID_ARG, "pbf_step_noalloc: device index out of range");
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_base[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return pbf::set_cuda_error(e, "pbf_step_noalloc: cudaGetSymbolAddress");
+    g_base[dev] = p;
+  }
+  *out = (unsigned char*)g_base[dev];
+  return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float ulim[3],
+                                       const float llim[3], void* pos, void* npos, void* vel,
+                                       void* nvel, uint32_t* iid, int n, void* stream) {
+  if (n < 0) return pbf::set_error(PBF_ERR_INVALID_ARG, "pbf_step_noalloc: n < 0");
+  if (n > kNoAllocMaxParticles)
+    return pbf::set_error(PBF_ERR_CAPACITY,
+                          "pbf_step_noalloc: n exceeds the fixed scratch limit of 32768 particles");
+  pbf::StepConsts c;
+  pbf_status st = pbf::validate_step_setup(params, ulim, llim, kNoAllocMaxCells, &c);
+  if (st != PBF_OK) return st;
+  if (n == 0) return PBF_OK;
+  if ((st = pbf::validate_step_buffers(pos, npos, vel, nvel, iid)) != PBF_OK) return st;
+  unsigned char* base = nullptr;
+  if ((st = scratch_base(&base)) != PBF_OK) return st;
+
+  pbf::GridScratch g;
+  g.keys_a = (uint32_t*)(base + kOffKeysA);
+  g.keys_b = (uint32_t*)(base + kOffKeysB);
+  g.vals_a = (uint32_t*)(base + kOffValsA);
+  g.vals_b = (uint32_t*)(base + kOffValsB);
+  g.cell_count = (uint32_t*)(base + kOffCount);
+  g.cell_start = (uint32_t*)(base + kOffStart);
+  g.radix_counts = (uint32_t*)(base + kOffRadix);
+  g.scan_partials = (uint32_t*)(base + kOffPartials);
+  pbf::SolverScratch s;
+  s.xs = (float4*)(base + kOffXs);
+  s.xa = (float4*)(base + kOffXa);
+  s.xb = (float4*)(base + kOffXb);
+  s.iid_s = (uint32_t*)(base + kOffIid);
+  s.lambda = (float*)(base + kOffLambda);
+  s.rho = (float*)(base + kOffRho);
+
+  cudaStream_t strm = (cudaStream_t)stream;
+  cudaError_t e;
+  const uint32_t* perm = nullptr;
+  // build_grid clears the per-cell counters itself (cudaMemsetAsync, no allocation)
+  if ((e = pbf::build_grid(c, (const float4*)pos, (const float4*)vel, nullptr, n, g, &perm, nullptr,
+                           strm)) != cudaSuccess)
+    return pbf::set_cuda_error(e, "pbf_step_noalloc: grid");
+  if ((e = pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, s, strm)) != cudaSuccess)
+    return pbf::set_cuda_error(e, "pbf_step_noalloc: reorder");
+  const int niter = params->niter;
+  float4* X = s.xa;
+  float4* T = s.xb;
+  for (int it = 0; it < niter; ++it) {
+    if ((e = pbf::launch_lambda(c, X, g.cell_start, n, s.lambda, s.rho, strm)) != cudaSuccess)
+      return pbf::set_cuda_error(e, "pbf_step_noalloc: lambda");
+    if (it + 1 < niter) {
+      if ((e = pbf::launch_delta_p(c, X, s.lambda, g.cell_start, n, T, strm)) != cudaSuccess)
+        return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
+      float4* t = X;
+      X = T;
+      T = t;
+    } else if ((e = pbf::launch_delta_p_final(c, X, s.lambda, g.cell_start, n, s, (float4*)pos,
+                                              (float4*)npos, (float4*)vel, iid, strm)) != cudaSuccess) {
+      return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
+    }
+  }
+  if ((e = pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, s.rho, g.cell_start, n,
+                            (float4*)nvel, strm)) != cudaSuccess)
+    return pbf::set_cuda_error(e, "pbf_step_noalloc: xsph");
+  return PBF_OK;
+}
