@@ -18,11 +18,12 @@
  * multiply-adds nvcc emits for the reference's advect_kernel, which makes the
  * predicted positions, and so the cell ids, bit-identical to the GPU's.
  *
- * Parity: unpinned.  The reference ships no tests, golden vectors or
- * known-answer fixtures, and has no CPU path to run here.  This restatement is
- * checked against closed-form known answers derived from the reference's
- * formulas (tests/test_oracle.py), not yet against outputs of the reference's
- * own kernels.
+ * Parity pinning: the reference ships no tests or fixtures and has no CPU
+ * path, so this restatement is pinned against outputs of the reference's own
+ * kernels (fluids/Simulator.cu, fluids/Simulator_kernel.cuh compiled
+ * unmodified for sm_103a and run on a GB300 by oracle/ref_harness), recorded
+ * in tests/golden/ by tests/golden/make_golden.py: cell ids, order and ranges
+ * bit-exact, positions within 1e-7 (tests/test_golden.py).
  *
  * Layout: all particle arrays are stride-4 (x, y, z, w) in the oracle's real
  * type; iid is uint32.  The step permutes pos/vel/iid in place exactly like

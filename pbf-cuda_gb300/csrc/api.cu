@@ -176,7 +176,7 @@ void free_all(pbf_solver* s) {
   void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
                   s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
                   s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
-                  s->sol.lambda, s->sol.rho};
+                  s->sol.lambda, s->sol.rho, s->sol.flags};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -273,6 +273,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.iid_s, np);
   if (e == cudaSuccess) e = alloc(&s->sol.lambda, np);
   if (e == cudaSuccess) e = alloc(&s->sol.rho, np);
+  if (e == cudaSuccess) e = alloc(&s->sol.flags, (size_t)pbf::kNumFlags);
   if (e != cudaSuccess) {
     free_all(s);
     delete s;
@@ -377,10 +378,12 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   float4* T = s->sol.xb;
   for (int it = 0; it < niter; ++it) {
     if (it < piters) PBF_EV(s->ev_it[3 * it]);
-    PBF_CUDA(pbf::launch_lambda(c, X, cs, n, s->sol.lambda, s->sol.rho, st_), "pbf_step: lambda");
+    PBF_CUDA(pbf::launch_lambda(c, X, cs, n, s->sol.lambda, s->sol.rho, s->sol.flags, st_),
+             "pbf_step: lambda");
     if (it < piters) PBF_EV(s->ev_it[3 * it + 1]);
     if (it + 1 < niter) {
-      PBF_CUDA(pbf::launch_delta_p(c, X, s->sol.lambda, cs, n, T, st_), "pbf_step: delta_p");
+      PBF_CUDA(pbf::launch_delta_p(c, X, s->sol.lambda, cs, n, s->sol.flags, T, st_),
+               "pbf_step: delta_p");
       float4* t = X;
       X = T;
       T = t;
@@ -394,7 +397,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   // correctVelocity: XSPH (fluids/Simulator.cpp:68-71)
   PBF_EV(s->ev[kEvXsphStart]);
   PBF_CUDA(pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, s->sol.rho, cs, n,
-                            (float4*)nvel, st_),
+                            s->sol.flags, (float4*)nvel, st_),
            "pbf_step: xsph");
   PBF_EV(s->ev[kEvEnd]);
 #undef PBF_EV

@@ -67,7 +67,8 @@ constexpr size_t kOffXb = kOffXa + align_up(16 * kNp);
 constexpr size_t kOffIid = kOffXb + align_up(16 * kNp);
 constexpr size_t kOffLambda = kOffIid + align_up(4 * kNp);
 constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
-constexpr size_t kNoAllocScratchBytes = kOffRho + align_up(4 * kNp);
+constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
+constexpr size_t kNoAllocScratchBytes = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -125,6 +126,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.iid_s = (uint32_t*)(base + kOffIid);
   s.lambda = (float*)(base + kOffLambda);
   s.rho = (float*)(base + kOffRho);
+  s.flags = (uint32_t*)(base + kOffFlags);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;
@@ -139,10 +141,10 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   float4* X = s.xa;
   float4* T = s.xb;
   for (int it = 0; it < niter; ++it) {
-    if ((e = pbf::launch_lambda(c, X, g.cell_start, n, s.lambda, s.rho, strm)) != cudaSuccess)
+    if ((e = pbf::launch_lambda(c, X, g.cell_start, n, s.lambda, s.rho, s.flags, strm)) != cudaSuccess)
       return pbf::set_cuda_error(e, "pbf_step_noalloc: lambda");
     if (it + 1 < niter) {
-      if ((e = pbf::launch_delta_p(c, X, s.lambda, g.cell_start, n, T, strm)) != cudaSuccess)
+      if ((e = pbf::launch_delta_p(c, X, s.lambda, g.cell_start, n, s.flags, T, strm)) != cudaSuccess)
         return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
       float4* t = X;
       X = T;
@@ -153,7 +155,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
     }
   }
   if ((e = pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, s.rho, g.cell_start, n,
-                            (float4*)nvel, strm)) != cudaSuccess)
+                            s.flags, (float4*)nvel, strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: xsph");
   return PBF_OK;
 }

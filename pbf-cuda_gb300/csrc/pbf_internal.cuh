@@ -139,6 +139,15 @@ struct SolverScratch {
   uint32_t* iid_s;  // sorted iid
   float* lambda;
   float* rho;
+  uint32_t* flags;  // [kNumFlags] per-step exceptional-value flags, zeroed by reorder
+};
+
+// Flags raised by a pass when a later pass must take its exact (slow) path to
+// reproduce the reference's IEEE results; almost always all zero.
+enum StepFlag {
+  kFlagLambdaNonFinite = 0,  // some lambda_i is NaN/inf: delta_p must see it through zero gradients
+  kFlagXsphExact = 1,        // some rho_i <= 0 or non-finite, or some velocity non-finite
+  kNumFlags = 4
 };
 
 // Gather pos/vel/iid into cell order and recompute x* (bit-identical to the hash).
@@ -147,10 +156,11 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
 
 // lambda_i and rho_i of every particle at positions X.
 cudaError_t launch_lambda(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
-                          float* lambda, float* rho, cudaStream_t stream);
+                          float* lambda, float* rho, uint32_t* flags, cudaStream_t stream);
 // One Jacobi position update X -> T.
 cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const float* lambda,
-                           const uint32_t* cs, int n, float4* T, cudaStream_t stream);
+                           const uint32_t* cs, int n, const uint32_t* flags, float4* T,
+                           cudaStream_t stream);
 // Last position update: x_final -> npos, (x_final - x) / dt -> vel, and the
 // permuted inputs -> pos, iid.
 cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const float* lambda,
@@ -158,7 +168,8 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const flo
                                  float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream);
 // XSPH: nvel = vel + c sum_j 2 (v_j - v_i) W / (rho_i + rho_j).
 cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const float* rho,
-                        const uint32_t* cs, int n, float4* NV, cudaStream_t stream);
+                        const uint32_t* cs, int n, const uint32_t* flags, float4* NV,
+                        cudaStream_t stream);
 
 // Kernel launches of one build_grid call with n particles and c.cells cells.
 int grid_launches(const StepConsts& c, int n);
