@@ -6,7 +6,9 @@ is built with nvcc (build.py); if that fails, import of the binding raises.
 from __future__ import annotations
 
 import ctypes
+import os
 import threading
+from pathlib import Path
 
 from . import build as _build
 
@@ -137,15 +139,15 @@ def _declare(L) -> None:
 
 
 def lib_path():
-    return _build.LIB
+    return Path(os.environ["PBF_LIB"]) if os.environ.get("PBF_LIB") else _build.LIB
 
 
 def lib():
-    """Load (building first if needed) libpbf.so."""
+    """Load (building first if needed) libpbf.so; PBF_LIB names another build of it."""
     global _lib
     with _lock:
         if _lib is None:
-            path = _build.build()
+            path = lib_path() if os.environ.get("PBF_LIB") else _build.build()
             L = ctypes.CDLL(str(path))
             _declare(L)
             _lib = L

@@ -48,9 +48,9 @@ def _deps() -> list[Path]:
                                                                      Path(__file__)]
 
 
-def _compile(src: str, ptxas_v: bool) -> tuple[str, str]:
-    obj = BUILD_DIR / (Path(src).stem + ".o")
-    cmd = [nvcc(), *NVCC_FLAGS, "-c", str(CSRC / src), "-o", str(obj)]
+def _compile(src: str, ptxas_v: bool, defines=(), build_dir=None) -> tuple[str, str]:
+    obj = (build_dir or BUILD_DIR) / (Path(src).stem + ".o")
+    cmd = [nvcc(), *NVCC_FLAGS, *[f"-D{d}" for d in defines], "-c", str(CSRC / src), "-o", str(obj)]
     if ptxas_v:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -59,27 +59,30 @@ def _compile(src: str, ptxas_v: bool) -> tuple[str, str]:
     return str(obj), r.stderr
 
 
-def build(force: bool = False, ptxas_v: bool = False, verbose: bool = False) -> Path:
-    """Compile libpbf.so if it is missing or older than any source."""
-    if LIB.exists() and not force and not ptxas_v:
-        t = LIB.stat().st_mtime
+def build(force: bool = False, ptxas_v: bool = False, verbose: bool = False, defines=(), out=None) -> Path:
+    """Compile libpbf.so if it is missing or older than any source.  ``defines``
+    (tuning macros) and ``out`` build a variant of the library elsewhere."""
+    lib = Path(out) if out else LIB
+    if lib.exists() and not force and not ptxas_v:
+        t = lib.stat().st_mtime
         if all(t >= d.stat().st_mtime for d in _deps()):
-            return LIB
-    BUILD_DIR.mkdir(parents=True, exist_ok=True)
-    LIB_DIR.mkdir(parents=True, exist_ok=True)
+            return lib
+    build_dir = lib.parent / f"_build_{lib.stem}" if out else BUILD_DIR
+    build_dir.mkdir(parents=True, exist_ok=True)
+    lib.parent.mkdir(parents=True, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda s: _compile(s, ptxas_v), SOURCES))
+        results = list(ex.map(lambda s: _compile(s, ptxas_v, defines, build_dir), SOURCES))
     if verbose or ptxas_v:
         for _, log in results:
             if log.strip():
                 print(log)
-    tmp = LIB.with_name(f"libpbf.so.tmp{os.getpid()}")
+    tmp = lib.with_name(f"{lib.name}.tmp{os.getpid()}")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *[o for o, _ in results]]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

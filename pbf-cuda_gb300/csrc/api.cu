@@ -27,6 +27,7 @@ struct pbf_solver {
   int max_particles;
   int max_cells;
   int device;
+  int num_sms;
   int last_n;  // particles of the last completed step (for pbf_get_density)
   pbf::GridScratch grid;
   pbf::SolverScratch sol;
@@ -113,7 +114,7 @@ double promote_decimal(float f) {
 
 // The reference's host-side coefficients, bit for bit (see pbf_internal.cuh).
 pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const float llim[3],
-                            const int dims[3]) {
+                            const int dims[3], int num_sms) {
   pbf::StepConsts c;
   std::memset(&c, 0, sizeof(c));
   const float h = p.h;
@@ -164,7 +165,19 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
     c.dims[a] = dims[a];
   }
   c.cells = dims[0] * dims[1] * dims[2];
+  c.dense_grid = 4 * (num_sms > 0 ? num_sms : 1);
   return c;
+}
+
+// Streaming multiprocessors of the current device (1 if it cannot be queried).
+int current_sms() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return sms;
 }
 
 template <typename T>
@@ -176,7 +189,7 @@ void free_all(pbf_solver* s) {
   void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
                   s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
                   s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
-                  s->sol.lambda, s->sol.rho, s->sol.flags};
+                  s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -274,6 +287,8 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.lambda, np);
   if (e == cudaSuccess) e = alloc(&s->sol.rho, np);
   if (e == cudaSuccess) e = alloc(&s->sol.flags, (size_t)pbf::kNumFlags);
+  if (e == cudaSuccess) e = alloc(&s->sol.dense, pbf::dense_list_len(max_particles));
+  if (e == cudaSuccess) s->num_sms = current_sms();
   if (e != cudaSuccess) {
     free_all(s);
     delete s;
@@ -353,7 +368,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
   if (st != PBF_OK) return st;
   if (cells > s->max_cells) return fail(PBF_ERR_CAPACITY, "box needs %lld cells", cells);
-  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims);
+  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
   cudaStream_t st_ = (cudaStream_t)stream;
   const bool prof = s->profile;
   const int niter = s->params.niter;
@@ -378,17 +393,15 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   float4* T = s->sol.xb;
   for (int it = 0; it < niter; ++it) {
     if (it < piters) PBF_EV(s->ev_it[3 * it]);
-    PBF_CUDA(pbf::launch_lambda(c, X, cs, n, s->sol.lambda, s->sol.rho, s->sol.flags, st_),
-             "pbf_step: lambda");
+    PBF_CUDA(pbf::launch_lambda(c, X, cs, n, s->sol, 2 * it, st_), "pbf_step: lambda");
     if (it < piters) PBF_EV(s->ev_it[3 * it + 1]);
     if (it + 1 < niter) {
-      PBF_CUDA(pbf::launch_delta_p(c, X, s->sol.lambda, cs, n, s->sol.flags, T, st_),
-               "pbf_step: delta_p");
+      PBF_CUDA(pbf::launch_delta_p(c, X, cs, n, s->sol, 2 * it + 1, T, st_), "pbf_step: delta_p");
       float4* t = X;
       X = T;
       T = t;
     } else {
-      PBF_CUDA(pbf::launch_delta_p_final(c, X, s->sol.lambda, cs, n, s->sol, (float4*)pos,
+      PBF_CUDA(pbf::launch_delta_p_final(c, X, cs, n, s->sol, 2 * it + 1, (float4*)pos,
                                          (float4*)npos, (float4*)vel, iid, st_),
                "pbf_step: delta_p");
     }
@@ -396,13 +409,13 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   }
   // correctVelocity: XSPH (fluids/Simulator.cpp:68-71)
   PBF_EV(s->ev[kEvXsphStart]);
-  PBF_CUDA(pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, s->sol.rho, cs, n,
-                            s->sol.flags, (float4*)nvel, st_),
+  PBF_CUDA(pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, cs, n, s->sol, 2 * niter,
+                            (float4*)nvel, st_),
            "pbf_step: xsph");
   PBF_EV(s->ev[kEvEnd]);
 #undef PBF_EV
   s->last_grid_launches = pbf::grid_launches(c, n);
-  s->last_launches = s->last_grid_launches + 1 + 2 * niter + 1;
+  s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1);
   if (prof) s->prof_iters = piters;
   s->last_n = n;
   return PBF_OK;
@@ -465,7 +478,7 @@ pbf_status pbf_build_grid(pbf_solver* s, const void* xstar, int n, uint32_t* key
   if (n < 0 || n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n outside [0, max_particles]");
   if (!start || !end) return fail(PBF_ERR_INVALID_ARG, "start/end are NULL");
   if (n > 0 && (!xstar || !keys || !perm)) return fail(PBF_ERR_INVALID_ARG, "NULL buffer");
-  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims);
+  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
   cudaStream_t st_ = (cudaStream_t)stream;
   if (n == 0) {
     PBF_CUDA(cudaMemsetAsync(start, 0, sizeof(uint32_t) * cells, st_), "pbf_build_grid");
@@ -501,7 +514,7 @@ pbf_status validate_step_setup(const pbf_params* params, const float ulim[3], co
   if ((st = grid_dims(ulim, llim, params->h, dims, &cells)) != PBF_OK) return st;
   if (cells > max_cells)
     return fail(PBF_ERR_CAPACITY, "box needs %lld cells, the limit is %lld", cells, max_cells);
-  *out = make_consts(*params, ulim, llim, dims);
+  *out = make_consts(*params, ulim, llim, dims, current_sms());
   return PBF_OK;
 }
 

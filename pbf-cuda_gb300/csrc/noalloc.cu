@@ -68,7 +68,8 @@ constexpr size_t kOffIid = kOffXb + align_up(16 * kNp);
 constexpr size_t kOffLambda = kOffIid + align_up(4 * kNp);
 constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
 constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
-constexpr size_t kNoAllocScratchBytes = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
+constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
+constexpr size_t kNoAllocScratchBytes = kOffDense + align_up(4 * (kNp / 32 + 1));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -127,6 +128,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.lambda = (float*)(base + kOffLambda);
   s.rho = (float*)(base + kOffRho);
   s.flags = (uint32_t*)(base + kOffFlags);
+  s.dense = (uint32_t*)(base + kOffDense);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;
@@ -141,21 +143,21 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   float4* X = s.xa;
   float4* T = s.xb;
   for (int it = 0; it < niter; ++it) {
-    if ((e = pbf::launch_lambda(c, X, g.cell_start, n, s.lambda, s.rho, s.flags, strm)) != cudaSuccess)
+    if ((e = pbf::launch_lambda(c, X, g.cell_start, n, s, 2 * it, strm)) != cudaSuccess)
       return pbf::set_cuda_error(e, "pbf_step_noalloc: lambda");
     if (it + 1 < niter) {
-      if ((e = pbf::launch_delta_p(c, X, s.lambda, g.cell_start, n, s.flags, T, strm)) != cudaSuccess)
+      if ((e = pbf::launch_delta_p(c, X, g.cell_start, n, s, 2 * it + 1, T, strm)) != cudaSuccess)
         return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
       float4* t = X;
       X = T;
       T = t;
-    } else if ((e = pbf::launch_delta_p_final(c, X, s.lambda, g.cell_start, n, s, (float4*)pos,
+    } else if ((e = pbf::launch_delta_p_final(c, X, g.cell_start, n, s, 2 * it + 1, (float4*)pos,
                                               (float4*)npos, (float4*)vel, iid, strm)) != cudaSuccess) {
       return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
     }
   }
-  if ((e = pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, s.rho, g.cell_start, n,
-                            s.flags, (float4*)nvel, strm)) != cudaSuccess)
+  if ((e = pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, g.cell_start, n, s, 2 * niter,
+                            (float4*)nvel, strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: xsph");
   return PBF_OK;
 }

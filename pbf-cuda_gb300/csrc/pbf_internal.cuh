@@ -36,6 +36,7 @@ struct StepConsts {
   float llim[3], ulim[3];
   int dims[3];             // cells per axis
   int cells;
+  int dense_grid;          // blocks of the dense neighbour kernels (a multiple of the SM count)
 };
 
 // Cell coordinate along one axis: getGridxyz / getGridId (fluids/Simulator.cu:30-36,
@@ -133,43 +134,56 @@ cudaError_t export_ranges(const StepConsts& c, const uint32_t* cell_start, uint3
 // ---- launch wrappers (solver.cu) ----------------------------------------------
 
 struct SolverScratch {
-  float4* xs;       // sorted x (positions at t)
-  float4* xa;       // predicted / iterated positions, ping
-  float4* xb;       // pong
-  uint32_t* iid_s;  // sorted iid
+  float4* xs;          // sorted x (positions at t)
+  float4* xa;          // predicted / iterated positions, ping
+  float4* xb;          // pong
+  uint32_t* iid_s;     // sorted iid
   float* lambda;
   float* rho;
-  uint32_t* flags;  // [kNumFlags] per-step exceptional-value flags, zeroed by reorder
+  uint32_t* flags;     // [kNumFlags] per-step flags and dense-list counters, zeroed by reorder
+  uint32_t* dense;     // [dense_list_len(max_particles)] warps handed to the dense kernels
 };
 
-// Flags raised by a pass when a later pass must take its exact (slow) path to
-// reproduce the reference's IEEE results; almost always all zero.
+// Words of SolverScratch::flags.  The two step flags are raised by a pass
+// when a later pass must take its exact (slow) path to reproduce the
+// reference's IEEE results (almost always zero).  The two counters are the
+// lengths of the dense lists, used alternately by consecutive passes.
 enum StepFlag {
   kFlagLambdaNonFinite = 0,  // some lambda_i is NaN/inf: delta_p must see it through zero gradients
   kFlagXsphExact = 1,        // some rho_i <= 0 or non-finite, or some velocity non-finite
+  kDenseCount0 = 2,
+  kDenseCount1 = 3,
   kNumFlags = 4
 };
+
+// Entries of the dense list: one per warp of 32 consecutive particles.
+inline size_t dense_list_len(int max_particles) { return (size_t)max_particles / 32 + 1; }
 
 // Gather pos/vel/iid into cell order and recompute x* (bit-identical to the hash).
 cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
                     const uint32_t* iid, int n, SolverScratch& s, cudaStream_t stream);
 
+// Each neighbour pass is two launches: the sparse kernel over all particles,
+// then the dense kernel over the warps the sparse kernel handed on.  `pass`
+// numbers the passes of a step (0, 1, 2, ...) and picks the dense counter.
+
 // lambda_i and rho_i of every particle at positions X.
 cudaError_t launch_lambda(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
-                          float* lambda, float* rho, uint32_t* flags, cudaStream_t stream);
+                          const SolverScratch& s, int pass, cudaStream_t stream);
 // One Jacobi position update X -> T.
-cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const float* lambda,
-                           const uint32_t* cs, int n, const uint32_t* flags, float4* T,
-                           cudaStream_t stream);
+cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+                           const SolverScratch& s, int pass, float4* T, cudaStream_t stream);
 // Last position update: x_final -> npos, (x_final - x) / dt -> vel, and the
 // permuted inputs -> pos, iid.
-cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const float* lambda,
-                                 const uint32_t* cs, int n, const SolverScratch& s, float4* pos,
-                                 float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream);
+cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+                                 const SolverScratch& s, int pass, float4* pos, float4* npos,
+                                 float4* vel, uint32_t* iid, cudaStream_t stream);
 // XSPH: nvel = vel + c sum_j 2 (v_j - v_i) W / (rho_i + rho_j).
-cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const float* rho,
-                        const uint32_t* cs, int n, const uint32_t* flags, float4* NV,
-                        cudaStream_t stream);
+cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const uint32_t* cs,
+                        int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream);
+
+// Kernel launches of one neighbour pass.
+constexpr int kLaunchesPerPass = 2;
 
 // Kernel launches of one build_grid call with n particles and c.cells cells.
 int grid_launches(const StepConsts& c, int n);

@@ -6,19 +6,30 @@
 //             caller's permuted pos / iid       h_updateVelocity (fluids/Simulator.cu:127-137)
 //   xsph      XSPH viscosity                    computeXSPH    (fluids/Simulator_kernel.cuh:196-239)
 //
-// Every pass is gather-only (no atomics, no cross-thread writes), so results
-// are deterministic.  Neighbour semantics follow the reference exactly: the
-// grid is built once per step from x*, every pass looks up the 3x3x3 cells
-// around cell(current x_i) in that (stale) grid, and candidates are visited in
-// the reference's order (dx, dy outer; the three z-consecutive cells of a
-// column form one contiguous run of sorted slots, visited in slot order).
+// Every pass is gather-only (no atomics on results, no cross-thread writes),
+// so results are deterministic.  Neighbour semantics follow the reference
+// exactly: the grid is built once per step from x*, every pass looks up the
+// 3x3x3 cells around cell(current x_i) in that (stale) grid.  For each
+// (dx, dy) column the three z-consecutive cells are adjacent in cell order,
+// so the window is 9 runs of sorted slots, visited in the reference's order
+// (dx outer, dy inner, slots ascending; fluids/Simulator_kernel.cuh:78-88).
 // Jacobi iterations ping-pong between two position buffers instead of the
 // reference's tpos -> npos copy (fluids/Simulator.cu:247-248).
 //
-// IEEE semantics follow the reference's: its kernels evaluate every candidate
-// of the window, so a NaN distance (from a NaN position) poisons the sums, a
-// non-finite lambda_j poisons delta_p through a zero gradient, and
-// 0 * v / (rho_i + rho_j) is NaN when both densities are zero.  Here the
+// Each pass is two kernels.  The sparse kernel gives every particle one
+// thread and walks its window in a compact loop (fluid at rest: ~200
+// candidates).  A warp in which some window exceeds kDenseWindow candidates
+// (particles piled into a few cells) instead appends itself to a dense list
+// and returns; the dense kernel then gives each listed warp a block of
+// kDenseWarps warps, each walking one contiguous chunk of every lane's
+// window, and adds the chunks' partial sums in chunk order in shared memory.
+// Both orders are fixed, so results stay deterministic; they differ from the
+// reference's sequential sums only by rounding.
+//
+// IEEE semantics follow the reference's: its kernels evaluate every
+// candidate of the window, so a NaN distance (from a NaN position) poisons
+// the sums, a non-finite lambda_j poisons delta_p through a zero gradient,
+// and 0 * v / (rho_i + rho_j) is NaN when both densities are zero.  Here the
 // candidate test is written NaN-inclusively (!(r2 >= h2), as the reference's
 // `if (r2 >= h2) return 0`), and the two poisoning rules that need every
 // candidate's lambda / density / velocity run only when a per-step flag says
@@ -30,25 +41,355 @@ namespace pbf {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kSparseThreads = 128;
+constexpr int kDenseWarps = 8;                  // chunks of a dense warp's windows
+constexpr int kDenseThreads = 32 * kDenseWarps;
+constexpr int kDenseWindow = 512;               // candidates above which a warp goes dense
+constexpr int kMaxFields = 6;                   // partial-sum fields of the largest pass
+constexpr unsigned kFull = 0xffffffffu;
+
+enum PassKind { kLambda = 0, kDeltaP = 1, kDeltaPFinal = 2, kXsph = 3 };
+
+// Everything any pass kernel needs (passed by value).
+struct PassArgs {
+  StepConsts c;
+  const float4* X;        // positions the pass reads (sorted)
+  const uint32_t* cs;     // cell prefix, cells + 1 entries
+  int n;
+  int counter;            // flags word holding this pass's dense-list length
+  int next_counter;       // the other one, cleared for the next pass
+  uint32_t* flags;
+  uint32_t* dense;
+  float* lambda;          // lambda: out;  delta_p: in
+  float* rho;             // lambda: out;  xsph: in
+  float4* T;              // delta_p: out
+  const float4* xs;       // delta_p_final: sorted x at t
+  const uint32_t* iid_s;  // delta_p_final: sorted iid
+  float4* npos;           // delta_p_final: out
+  float4* vel;            // delta_p_final: out
+  float4* pos;            // delta_p_final: out (permuted inputs)
+  uint32_t* iid;          // delta_p_final: out (permuted inputs)
+  const float4* V;        // xsph: velocities
+  float4* NV;             // xsph: out
+};
+
+// ---- windows ------------------------------------------------------------------------
 
 // Sorted-slot range [s, e) of cells (x, y, z-1 .. z+1) clipped to the grid.
-// cs[cells] == n, so e <= n; the clamp keeps even an inconsistent table in range.
+// cs[cells] == n, so e <= n; the clamps keep even an inconsistent table in range.
 __device__ __forceinline__ void column_run(const StepConsts& c, const uint32_t* __restrict__ cs,
                                            int n, int x, int y, int z, int& s, int& e) {
   const int zlo = max(z - 1, 0), zhi = min(z + 1, c.dims[2] - 1);
   const int base = (x * c.dims[1] + y) * c.dims[2];
   s = (int)__ldg(cs + base + zlo);
-  e = min((int)__ldg(cs + base + zhi + 1), n);
+  e = max(min((int)__ldg(cs + base + zhi + 1), n), s);
 }
 
-__global__ void __launch_bounds__(kThreads)
+__device__ __forceinline__ int window_total(const StepConsts& c, const uint32_t* __restrict__ cs,
+                                            int n, int3 q) {
+  int total = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= c.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= c.dims[1]) continue;
+      int s, e;
+      column_run(c, cs, n, x, y, q.z, s, e);
+      total += e - s;
+    }
+  }
+  return total;
+}
+
+// Every candidate of the window, in order.
+template <class P>
+__device__ __forceinline__ void visit_window(const StepConsts& c, const uint32_t* __restrict__ cs,
+                                             int n, int3 q, const float4* __restrict__ X, P& p) {
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= c.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= c.dims[1]) continue;
+      int s, e;
+      column_run(c, cs, n, x, y, q.z, s, e);
+      for (int j = s; j < e; ++j) p.visit(__ldg(X + j), j);
+    }
+  }
+}
+
+// Candidates [v_lo, v_hi) of the window (numbered in visiting order), four
+// loads in flight at a time.
+template <class P>
+__device__ __forceinline__ void visit_window_chunk(const StepConsts& c,
+                                                   const uint32_t* __restrict__ cs, int n, int3 q,
+                                                   const float4* __restrict__ X, P& p, int v_lo,
+                                                   int v_hi) {
+  int v0 = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= c.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= c.dims[1]) continue;
+      int s, e;
+      column_run(c, cs, n, x, y, q.z, s, e);
+      const int len = e - s;
+      const int a = max(v_lo, v0), b = min(v_hi, v0 + len);
+      v0 += len;
+      if (a >= b) continue;
+      int j = s + (a - (v0 - len));
+      const int jend = s + (b - (v0 - len));
+      for (; j + 3 < jend; j += 4) {
+        const float4 q0 = __ldg(X + j), q1 = __ldg(X + j + 1), q2 = __ldg(X + j + 2),
+                     q3 = __ldg(X + j + 3);
+        p.visit(q0, j);
+        p.visit(q1, j + 1);
+        p.visit(q2, j + 2);
+        p.visit(q3, j + 3);
+      }
+      for (; j < jend; ++j) p.visit(__ldg(X + j), j);
+    }
+  }
+}
+
+// ---- the passes: per-candidate visit, partial-sum fields, finish ----------------------
+
+struct LambdaPass {
+  static constexpr int kFields = 5;
+  const StepConsts& c;
+  float4 xi;
+  int i;
+  float pho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, gl2 = 0.f;
+
+  __device__ LambdaPass(const PassArgs& a, float4 xi_, int i_, bool) : c(a.c), xi(xi_), i(i_) {}
+  __device__ __forceinline__ void visit(float4 xj, int j) {
+    const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
+    const float r2 = dist2(ex, ey, ez);
+    if (!(r2 >= c.h2)) {  // NaN-inclusive, as getPoly6
+      pho += poly6_inside(c, r2);
+      if (!(r2 < c.keps2)) {  // as getSpikyGrad's |r| < KERNAL_EPS test
+        const float ir = rsqrtf(r2);
+        const float t = c.h - r2 * ir;
+        const float sc = c.spiky_coef_rho0 * t * t * ir;
+        const float ax = sc * ex, ay = sc * ey, az = sc * ez;
+        gx += ax;
+        gy += ay;
+        gz += az;
+        if (j != i) gl2 += dist2(ax, ay, az);
+      }
+    }
+  }
+  __device__ void store(float* f, int stride) const {
+    f[0] = pho, f[stride] = gx, f[2 * stride] = gy, f[3 * stride] = gz, f[4 * stride] = gl2;
+  }
+  __device__ void add(const float* f, int stride) {
+    pho += f[0], gx += f[stride], gy += f[2 * stride], gz += f[3 * stride], gl2 += f[4 * stride];
+  }
+  __device__ void finish(const PassArgs& a) const {
+    float rho = pho;
+    if (c.k_b != 0.f) rho += c.k_b * boundary_density(c, xi);
+    const float grad_l2 = gl2 + dist2(gx, gy, gz);
+    const float lam = -(rho / c.pho0 - 1.f) / (grad_l2 + c.lambda_eps);
+    a.lambda[i] = lam;
+    a.rho[i] = rho;
+    if (!isfinite(lam)) atomicOr(&a.flags[kFlagLambdaNonFinite], 1u);
+    if (!(rho > 0.f) || !isfinite(rho)) atomicOr(&a.flags[kFlagXsphExact], 1u);
+  }
+};
+
+// sum over neighbours j != i of (lambda_i + lambda_j + s_corr) grad W.  exact
+// adds the reference's poisoning of the sum by a non-finite lambda through a
+// zero gradient (candidates j != i outside the cutoff).
+template <bool kFinal>
+struct DeltaPPass {
+  static constexpr int kFields = 4;
+  const StepConsts& c;
+  const float* __restrict__ lambda;
+  float4 xi;
+  int i;
+  float li;
+  bool exact;
+  float ax = 0.f, ay = 0.f, az = 0.f;
+  bool poison = false;
+
+  __device__ DeltaPPass(const PassArgs& a, float4 xi_, int i_, bool exact_)
+      : c(a.c), lambda(a.lambda), xi(xi_), i(i_), li(a.lambda[i_]), exact(exact_) {}
+  __device__ __forceinline__ void visit(float4 xj, int j) {
+    const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
+    const float r2 = dist2(ex, ey, ez);
+    if (!(r2 >= c.h2) && !(r2 < c.keps2) && j != i) {  // NaN-inclusive, as the reference
+      const float wgt = poly6_inside(c, r2);
+      const float corr = c.coef_corr * pow_corr(c, wgt);
+      const float ir = rsqrtf(r2);
+      const float t = c.h - r2 * ir;
+      const float f = (li + __ldg(lambda + j) + corr) * (c.spiky_coef * t * t * ir);
+      ax = fmaf(f, ex, ax);
+      ay = fmaf(f, ey, ay);
+      az = fmaf(f, ez, az);
+    } else if (exact && j != i) {
+      // zero gradient: (lambda_i + lambda_j + s_corr) * 0 is NaN iff a lambda is not finite
+      poison |= !isfinite(li) || !isfinite(__ldg(lambda + j));
+    }
+  }
+  __device__ void store(float* f, int stride) const {
+    f[0] = ax, f[stride] = ay, f[2 * stride] = az, f[3 * stride] = poison ? 1.f : 0.f;
+  }
+  __device__ void add(const float* f, int stride) {
+    ax += f[0], ay += f[stride], az += f[2 * stride];
+    poison |= f[3 * stride] != 0.f;
+  }
+  // d / pho0, per-component clamp to +-max_dp, wall clamp
+  // (fluids/Simulator_kernel.cuh:184-193); fminf/fmaxf map a NaN to the bound.
+  __device__ void finish(const PassArgs& a) const {
+    float sx = ax, sy = ay, sz = az;
+    if (poison) sx = sy = sz = __int_as_float(0x7fffffff);
+    const float dx = fmaxf(fminf(sx / c.pho0, c.max_dp), -c.max_dp);
+    const float dy = fmaxf(fminf(sy / c.pho0, c.max_dp), -c.max_dp);
+    const float dz = fmaxf(fminf(sz / c.pho0, c.max_dp), -c.max_dp);
+    const float4 xf = make_float4(fmaxf(fminf(xi.x + dx, c.hi[0]), c.lo[0]),
+                                  fmaxf(fminf(xi.y + dy, c.hi[1]), c.lo[1]),
+                                  fmaxf(fminf(xi.z + dz, c.hi[2]), c.lo[2]), xi.w);
+    if (!kFinal) {
+      a.T[i] = xf;
+      return;
+    }
+    // last iteration: x_final -> npos, v = (x_final - x) * (1/dt) -> vel, and the
+    // caller's pos / iid receive the permuted inputs (the reference's in-place sort)
+    const float4 x0 = a.xs[i];
+    a.npos[i] = make_float4(xf.x, xf.y, xf.z, x0.w);
+    const float4 v = make_float4((xf.x - x0.x) * c.inv_dt, (xf.y - x0.y) * c.inv_dt,
+                                 (xf.z - x0.z) * c.inv_dt, 0.f);
+    a.vel[i] = v;
+    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z))
+      atomicOr(&a.flags[kFlagXsphExact], 1u);
+    a.pos[i] = x0;
+    a.iid[i] = a.iid_s[i];
+  }
+};
+
+// sum over the window of 2 (v_j - v_i) W / (rho_i + rho_j).  exact adds the
+// reference's NaN from 0 * v / (rho_i + rho_j) outside the cutoff.
+struct XsphPass {
+  static constexpr int kFields = 6;
+  const StepConsts& c;
+  const float4* __restrict__ V;
+  const float* __restrict__ rho;
+  float4 xi, vi;
+  float ri;
+  int i;
+  bool exact;
+  float ax = 0.f, ay = 0.f, az = 0.f;
+  bool px = false, py = false, pz = false;
+
+  __device__ XsphPass(const PassArgs& a, float4 xi_, int i_, bool exact_)
+      : c(a.c), V(a.V), rho(a.rho), xi(xi_), vi(a.V[i_]), ri(a.rho[i_]), i(i_), exact(exact_) {}
+  __device__ __forceinline__ void visit(float4 xj, int j) {
+    const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+    if (!(r2 >= c.h2)) {  // NaN-inclusive, as getPoly6
+      const float4 vj = __ldg(V + j);
+      const float w2 = 2.f * poly6_inside(c, r2) / (ri + __ldg(rho + j));
+      ax = fmaf(vj.x - vi.x, w2, ax);
+      ay = fmaf(vj.y - vi.y, w2, ay);
+      az = fmaf(vj.z - vi.z, w2, az);
+    } else if (exact) {
+      // W = 0: 2 (v_j - v_i) * 0 / (rho_i + rho_j) is NaN iff the velocity
+      // difference is not finite or the denominator is 0 or NaN
+      const float4 vj = __ldg(V + j);
+      const float den = ri + __ldg(rho + j);
+      const bool bad_den = !(den != 0.f) || isnan(den);
+      px |= bad_den || !isfinite(vj.x - vi.x);
+      py |= bad_den || !isfinite(vj.y - vi.y);
+      pz |= bad_den || !isfinite(vj.z - vi.z);
+    }
+  }
+  __device__ void store(float* f, int stride) const {
+    f[0] = ax, f[stride] = ay, f[2 * stride] = az;
+    f[3 * stride] = px ? 1.f : 0.f, f[4 * stride] = py ? 1.f : 0.f, f[5 * stride] = pz ? 1.f : 0.f;
+  }
+  __device__ void add(const float* f, int stride) {
+    ax += f[0], ay += f[stride], az += f[2 * stride];
+    px |= f[3 * stride] != 0.f, py |= f[4 * stride] != 0.f, pz |= f[5 * stride] != 0.f;
+  }
+  __device__ void finish(const PassArgs& a) const {
+    const float qnan = __int_as_float(0x7fffffff);
+    a.NV[i] = make_float4(fmaf(c.c_xsph, px ? qnan : ax, vi.x), fmaf(c.c_xsph, py ? qnan : ay, vi.y),
+                          fmaf(c.c_xsph, pz ? qnan : az, vi.z), 0.f);
+  }
+};
+
+template <int kKind> struct PassOf;
+template <> struct PassOf<kLambda> { using type = LambdaPass; };
+template <> struct PassOf<kDeltaP> { using type = DeltaPPass<false>; };
+template <> struct PassOf<kDeltaPFinal> { using type = DeltaPPass<true>; };
+template <> struct PassOf<kXsph> { using type = XsphPass; };
+
+__device__ __forceinline__ bool exact_path(int kind, const uint32_t* flags) {
+  if (kind == kDeltaP || kind == kDeltaPFinal) return flags[kFlagLambdaNonFinite] != 0u;
+  if (kind == kXsph) return flags[kFlagXsphExact] != 0u;
+  return false;
+}
+
+// ---- kernels ------------------------------------------------------------------------
+
+template <int kKind>
+__global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
+  using P = typename PassOf<kKind>::type;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = i < a.n;
+  const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const int3 q = cell_of(a.c, xi);
+  const int total = valid ? window_total(a.c, a.cs, a.n, q) : 0;
+  if (__any_sync(kFull, total > kDenseWindow)) {
+    if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(i >> 5);
+    return;
+  }
+  if (!valid) return;
+  P p(a, xi, i, exact_path(kKind, a.flags));
+  visit_window(a.c, a.cs, a.n, q, a.X, p);
+  p.finish(a);
+}
+
+template <int kKind>
+__global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
+  using P = typename PassOf<kKind>::type;
+  __shared__ float part[kDenseWarps][kMaxFields][32];
+  static_assert(P::kFields <= kMaxFields, "partial-sum fields");
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
+  const uint32_t count = a.flags[a.counter];  // written by this pass's sparse kernel
+  const bool exact = exact_path(kKind, a.flags);
+  for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+    const int i = (int)a.dense[item] * 32 + lane;
+    const bool valid = i < a.n;
+    const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int3 q = cell_of(a.c, xi);
+    if (valid) {
+      const int total = window_total(a.c, a.cs, a.n, q);
+      const int lo = (int)((long long)total * warp / kDenseWarps);
+      const int hi = (int)((long long)total * (warp + 1) / kDenseWarps);
+      P p(a, xi, i, exact);
+      visit_window_chunk(a.c, a.cs, a.n, q, a.X, p, lo, hi);
+      p.store(&part[warp][0][lane], 32);
+    }
+    __syncthreads();
+    if (warp == 0 && valid) {
+      P p(a, xi, i, exact);
+      for (int k = 0; k < kDenseWarps; ++k) p.add(&part[k][0][lane], 32);
+      p.finish(a);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256)
 k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
           const float4* __restrict__ vel, const uint32_t* __restrict__ iid, int n, StepConsts c,
           float4* __restrict__ xs, float4* __restrict__ xa, uint32_t* __restrict__ iid_s,
           uint32_t* __restrict__ flags) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < kNumFlags) flags[k] = 0u;  // the step's flags start clear
+  if (k < kNumFlags) flags[k] = 0u;  // the step's flags and counters start clear
   if (k >= n) return;
   const uint32_t p = min(perm[k], (uint32_t)(n - 1));  // a permutation of [0, n): the min never binds
   const float4 x = pos[p];
@@ -60,219 +401,69 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
   iid_s[k] = iid[p];
 }
 
-__global__ void __launch_bounds__(kThreads)
-k_lambda(const float4* __restrict__ X, const uint32_t* __restrict__ cs, int n, StepConsts c,
-         float* __restrict__ lambda, float* __restrict__ rho, uint32_t* __restrict__ flags) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 xi = X[i];
-  const int3 q = cell_of(c, xi);
-  float pho = 0.f, gl2 = 0.f, gx = 0.f, gy = 0.f, gz = 0.f;
-  for (int dx = -1; dx <= 1; ++dx) {
-    const int x = q.x + dx;
-    if (x < 0 || x >= c.dims[0]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = q.y + dy;
-      if (y < 0 || y >= c.dims[1]) continue;
-      int s, e;
-      column_run(c, cs, n, x, y, q.z, s, e);
-      for (int j = s; j < e; ++j) {
-        const float4 xj = __ldg(X + j);
-        const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
-        const float r2 = dist2(ex, ey, ez);
-        if (!(r2 >= c.h2)) {  // NaN-inclusive, as getPoly6
-          pho += poly6_inside(c, r2);
-          if (!(r2 < c.keps2)) {  // as getSpikyGrad's |r| < KERNAL_EPS test
-            const float ir = rsqrtf(r2);
-            const float t = c.h - r2 * ir;
-            const float sc = c.spiky_coef_rho0 * t * t * ir;
-            const float ax = sc * ex, ay = sc * ey, az = sc * ez;
-            gx += ax;
-            gy += ay;
-            gz += az;
-            if (j != i) gl2 += dist2(ax, ay, az);
-          }
-        }
-      }
-    }
-  }
-  if (c.k_b != 0.f) pho += c.k_b * boundary_density(c, xi);
-  const float grad_l2 = gl2 + dist2(gx, gy, gz);
-  const float lam = -(pho / c.pho0 - 1.f) / (grad_l2 + c.lambda_eps);
-  lambda[i] = lam;
-  rho[i] = pho;
-  if (!isfinite(lam)) atomicOr(&flags[kFlagLambdaNonFinite], 1u);
-  if (!(pho > 0.f) || !isfinite(pho)) atomicOr(&flags[kFlagXsphExact], 1u);
+PassArgs base_args(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+                   const SolverScratch& s, int pass) {
+  PassArgs a = {};
+  a.c = c;
+  a.X = X;
+  a.cs = cs;
+  a.n = n;
+  a.counter = kDenseCount0 + (pass & 1);
+  a.next_counter = kDenseCount0 + ((pass + 1) & 1);
+  a.flags = s.flags;
+  a.dense = s.dense;
+  a.lambda = s.lambda;
+  a.rho = s.rho;
+  return a;
 }
 
-// delta_p for slot i: sum over neighbours j != i of (lambda_i + lambda_j + s_corr) grad W,
-// then / pho0, per-component clamp to +-max_dp, wall clamp.
-// exact: also apply the reference's poisoning of the sum by a non-finite
-// lambda through a zero gradient (candidates j != i outside the cutoff).
-template <bool kExact>
-__device__ __forceinline__ float4 delta_p(const StepConsts& c, const float4* __restrict__ X,
-                                          const float* __restrict__ lambda,
-                                          const uint32_t* __restrict__ cs, int n, int i,
-                                          float4 xi) {
-  const int3 q = cell_of(c, xi);
-  const float li = lambda[i];
-  float ax = 0.f, ay = 0.f, az = 0.f;
-  bool poison = false;
-  for (int dx = -1; dx <= 1; ++dx) {
-    const int x = q.x + dx;
-    if (x < 0 || x >= c.dims[0]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = q.y + dy;
-      if (y < 0 || y >= c.dims[1]) continue;
-      int s, e;
-      column_run(c, cs, n, x, y, q.z, s, e);
-      for (int j = s; j < e; ++j) {
-        const float4 xj = __ldg(X + j);
-        const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
-        const float r2 = dist2(ex, ey, ez);
-        if (!(r2 >= c.h2) && !(r2 < c.keps2) && j != i) {  // NaN-inclusive, as the reference
-          const float w = poly6_inside(c, r2);
-          const float corr = c.coef_corr * pow_corr(c, w);
-          const float ir = rsqrtf(r2);
-          const float t = c.h - r2 * ir;
-          const float f = (li + __ldg(lambda + j) + corr) * (c.spiky_coef * t * t * ir);
-          ax = fmaf(f, ex, ax);
-          ay = fmaf(f, ey, ay);
-          az = fmaf(f, ez, az);
-        } else if (kExact && j != i) {
-          // zero gradient: (lambda_i + lambda_j + s_corr) * 0 is NaN iff a lambda is not finite
-          poison |= !isfinite(li) || !isfinite(__ldg(lambda + j));
-        }
-      }
-    }
-  }
-  if (kExact && poison) ax = ay = az = __int_as_float(0x7fffffff);
-  const float dx = fmaxf(fminf(ax / c.pho0, c.max_dp), -c.max_dp);
-  const float dy = fmaxf(fminf(ay / c.pho0, c.max_dp), -c.max_dp);
-  const float dz = fmaxf(fminf(az / c.pho0, c.max_dp), -c.max_dp);
-  return make_float4(fmaxf(fminf(xi.x + dx, c.hi[0]), c.lo[0]),
-                     fmaxf(fminf(xi.y + dy, c.hi[1]), c.lo[1]),
-                     fmaxf(fminf(xi.z + dz, c.hi[2]), c.lo[2]), xi.w);
-}
-
-__global__ void __launch_bounds__(kThreads)
-k_delta_p(const float4* __restrict__ X, const float* __restrict__ lambda,
-          const uint32_t* __restrict__ cs, int n, StepConsts c, const uint32_t* __restrict__ flags,
-          float4* __restrict__ T) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  T[i] = flags[kFlagLambdaNonFinite] ? delta_p<true>(c, X, lambda, cs, n, i, X[i])
-                                     : delta_p<false>(c, X, lambda, cs, n, i, X[i]);
-}
-
-// Last iteration: x_final -> npos, v = (x_final - x) * (1/dt) -> vel, and the
-// caller's pos / iid receive the permuted inputs (the reference's in-place sort).
-__global__ void __launch_bounds__(kThreads)
-k_delta_p_final(const float4* __restrict__ X, const float* __restrict__ lambda,
-                const uint32_t* __restrict__ cs, int n, StepConsts c,
-                const float4* __restrict__ xs, const uint32_t* __restrict__ iid_s,
-                float4* __restrict__ npos, float4* __restrict__ vel, float4* __restrict__ pos,
-                uint32_t* __restrict__ iid, uint32_t* __restrict__ flags) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const float4 xf = flags[kFlagLambdaNonFinite] ? delta_p<true>(c, X, lambda, cs, n, i, X[i])
-                                                : delta_p<false>(c, X, lambda, cs, n, i, X[i]);
-  const float4 x0 = xs[i];
-  npos[i] = make_float4(xf.x, xf.y, xf.z, x0.w);
-  const float4 v = make_float4((xf.x - x0.x) * c.inv_dt, (xf.y - x0.y) * c.inv_dt,
-                               (xf.z - x0.z) * c.inv_dt, 0.f);
-  vel[i] = v;
-  if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z)) atomicOr(&flags[kFlagXsphExact], 1u);
-  pos[i] = x0;
-  iid[i] = iid_s[i];
-}
-
-__global__ void __launch_bounds__(kThreads)
-k_xsph(const float4* __restrict__ X, const float4* __restrict__ V, const float* __restrict__ rho,
-       const uint32_t* __restrict__ cs, int n, StepConsts c, const uint32_t* __restrict__ flags,
-       float4* __restrict__ NV) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const bool exact = flags[kFlagXsphExact] != 0u;
-  bool px = false, py = false, pz = false;  // exact path: NaN from 0 * v / (rho_i + rho_j)
-  const float4 xi = X[i];
-  const float4 vi = V[i];
-  const float ri = rho[i];
-  const int3 q = cell_of(c, xi);
-  float ax = 0.f, ay = 0.f, az = 0.f;
-  for (int dx = -1; dx <= 1; ++dx) {
-    const int x = q.x + dx;
-    if (x < 0 || x >= c.dims[0]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = q.y + dy;
-      if (y < 0 || y >= c.dims[1]) continue;
-      int s, e;
-      column_run(c, cs, n, x, y, q.z, s, e);
-      for (int j = s; j < e; ++j) {
-        const float4 xj = __ldg(X + j);
-        const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
-        if (!(r2 >= c.h2)) {  // NaN-inclusive, as getPoly6
-          const float4 vj = __ldg(V + j);
-          const float w2 = 2.f * poly6_inside(c, r2) / (ri + __ldg(rho + j));
-          ax = fmaf(vj.x - vi.x, w2, ax);
-          ay = fmaf(vj.y - vi.y, w2, ay);
-          az = fmaf(vj.z - vi.z, w2, az);
-        } else if (exact) {
-          // W = 0: 2 (v_j - v_i) * 0 / (rho_i + rho_j) is NaN iff the velocity
-          // difference is not finite or the denominator is 0 or NaN
-          const float4 vj = __ldg(V + j);
-          const float den = ri + __ldg(rho + j);
-          const bool bad_den = !(den != 0.f) || isnan(den);
-          px |= bad_den || !isfinite(vj.x - vi.x);
-          py |= bad_den || !isfinite(vj.y - vi.y);
-          pz |= bad_den || !isfinite(vj.z - vi.z);
-        }
-      }
-    }
-  }
-  const float qnan = __int_as_float(0x7fffffff);
-  if (px) ax = qnan;
-  if (py) ay = qnan;
-  if (pz) az = qnan;
-  NV[i] = make_float4(fmaf(c.c_xsph, ax, vi.x), fmaf(c.c_xsph, ay, vi.y),
-                      fmaf(c.c_xsph, az, vi.z), 0.f);
+template <int kKind>
+cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
+  k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, 0, stream>>>(a);
+  k_dense<kKind><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
+  return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
                     const uint32_t* iid, int n, SolverScratch& s, cudaStream_t stream) {
-  k_reorder<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(perm, pos, vel, iid, n, c,
-                                                                     s.xs, s.xa, s.iid_s, s.flags);
+  k_reorder<<<(n + 255) / 256, 256, 0, stream>>>(perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
+                                                  s.flags);
   return cudaGetLastError();
 }
 
 cudaError_t launch_lambda(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
-                          float* lambda, float* rho, uint32_t* flags, cudaStream_t stream) {
-  k_lambda<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(X, cs, n, c, lambda, rho, flags);
-  return cudaGetLastError();
+                          const SolverScratch& s, int pass, cudaStream_t stream) {
+  return run_pass<kLambda>(base_args(c, X, cs, n, s, pass), stream);
 }
 
-cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const float* lambda,
-                           const uint32_t* cs, int n, const uint32_t* flags, float4* T,
-                           cudaStream_t stream) {
-  k_delta_p<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(X, lambda, cs, n, c, flags, T);
-  return cudaGetLastError();
+cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+                           const SolverScratch& s, int pass, float4* T, cudaStream_t stream) {
+  PassArgs a = base_args(c, X, cs, n, s, pass);
+  a.T = T;
+  return run_pass<kDeltaP>(a, stream);
 }
 
-cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const float* lambda,
-                                 const uint32_t* cs, int n, const SolverScratch& s, float4* pos,
-                                 float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream) {
-  k_delta_p_final<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(
-      X, lambda, cs, n, c, s.xs, s.iid_s, npos, vel, pos, iid, s.flags);
-  return cudaGetLastError();
+cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+                                 const SolverScratch& s, int pass, float4* pos, float4* npos,
+                                 float4* vel, uint32_t* iid, cudaStream_t stream) {
+  PassArgs a = base_args(c, X, cs, n, s, pass);
+  a.xs = s.xs;
+  a.iid_s = s.iid_s;
+  a.npos = npos;
+  a.vel = vel;
+  a.pos = pos;
+  a.iid = iid;
+  return run_pass<kDeltaPFinal>(a, stream);
 }
 
-cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const float* rho,
-                        const uint32_t* cs, int n, const uint32_t* flags, float4* NV,
-                        cudaStream_t stream) {
-  k_xsph<<<(n + kThreads - 1) / kThreads, kThreads, 0, stream>>>(X, V, rho, cs, n, c, flags, NV);
-  return cudaGetLastError();
+cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const uint32_t* cs,
+                        int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream) {
+  PassArgs a = base_args(c, X, cs, n, s, pass);
+  a.V = V;
+  a.NV = NV;
+  return run_pass<kXsph>(a, stream);
 }
 
 }  // namespace pbf
