@@ -14,8 +14,10 @@ ours:       W untimed steps, then K steps timed with CUDA events on the
             step, inputs resident in HBM.  Prints one JSON line (rank 0).
 reference:  the reference has no CPU implementation, so its CPU arm is the
             float OpenMP port of its kernels (oracle/), on all host threads,
-            same workload, each step a full 1M-particle step, bounded to a few
-            minutes in total.
+            same workload, each step a full 1M-particle step; a bounded sample:
+            at most 3 warm-up steps, then timed steps for about 20 s, from the
+            initial lattice (later steps of this workload pile particles into
+            a few cells and cost the CPU minutes per step).
 N > 1 runs N independent replicas (one per GPU); the path does not shard.
 """
 from __future__ import annotations
@@ -159,7 +161,7 @@ def run_reference(args):
     t = 0.0
     w_done = 0
     a = time.perf_counter()
-    while w_done < args.warmup and (time.perf_counter() - a < args.cpu_warmup_budget or w_done < 3):
+    while w_done < min(args.warmup, args.cpu_warmup_steps) and (time.perf_counter() - a < args.cpu_warmup_budget):
         ulim, llim = scene.limits_at(t)
         r = oracle.step(scene.params, ulim, llim, pos, vel, iid, prec="f32")
         pos, vel, iid = r["npos"], r["nvel"], r["iid"]
@@ -256,6 +258,7 @@ def run_ours(args):
 
     # -- end to end through the public API with host buffers ------------------------
     e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps, stream)
+    alt = measure_reference_params(pkg, torch, args, stream) if args.params == "scene" else None
 
     value = world * n * args.steps / (total_ms / 1e3)
     if rank != 0:
@@ -279,12 +282,17 @@ def run_ours(args):
     # the kernels time far above HBM: an FP32 figure explains them (pair work)
     launches = profs[-1]["launches"]
 
-    # -- CPU baseline: the float OpenMP port on the same state, bounded ---------------
+    # -- CPU baseline: the float OpenMP port on a bounded sample of the workload ---------
+    # The timed GPU steps (after the warm-up) are far too costly for the CPU once
+    # particles have piled up, so the sample is the workload's first steps from
+    # the initial lattice, and the GPU is timed on exactly those steps beside it.
     from oracle import oracle
 
-    pos0, vel0, iid0, t0 = state0
-    cpu_rate, cpu_steps, cpu_s = cpu_port_rate(oracle, scene, pos0, vel0, iid0, t0, args.cpu_budget,
-                                               max(args.steps, 1))
+    cpu_steps_max = max(1, min(args.cpu_steps, args.steps))
+    cpu_rate, cpu_steps, cpu_s = cpu_port_rate(oracle, scene, scene.pos, scene.vel,
+                                               np.arange(n, dtype=np.uint32), 0.0, args.cpu_budget,
+                                               cpu_steps_max)
+    gpu_same = gpu_rate_first_steps(pkg, torch, scene, cpu_steps, stream)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -296,17 +304,78 @@ def run_ours(args):
                      "traffic": ncu_traffic(kernel)},
         "phases_ms": phases,
         "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
-                         "sample": f"{n} particles from the state at the first timed step, {cpu_steps} steps "
-                                   f"({cpu_s:.1f} s)"},
+                         "sample": f"the workload's first {cpu_steps} steps from the initial lattice, {n} "
+                                   f"particles ({cpu_s:.1f} s of CPU time); the GPU on the same steps: "
+                                   f"{gpu_same:.4g} {UNIT}",
+                         "gpu_same_sample": gpu_same},
         "e2e": e2e,
         "gpu_launches": launches * args.steps,
         "clocks": clk,
         "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
+        "reference_params": alt,
     }
     print(json.dumps(line), flush=True)
     sim.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def gpu_rate_first_steps(pkg, torch, scene, steps, stream):
+    """GPU particle-updates/s over the workload's first `steps` steps from the
+    initial lattice, L2 flushed before each, CUDA events on the stream."""
+    p = scene.params
+    st = pkg.ParticleState(scene.pos, scene.vel)
+    sim = pkg.Simulator(p, scene.ulim, scene.llim, scene.n)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    total, t = 0.0, 0.0
+    for _ in range(steps):
+        ulim, llim = scene.limits_at(t)
+        flush.fill_(1.0)
+        torch.cuda._sleep(2_000_000)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.setLim(ulim, llim)
+        st.step(sim)
+        e1.record(stream)
+        e1.synchronize()
+        total += e0.elapsed_time(e1)
+        t += p.dt
+    sim.close()
+    return scene.n * steps / (total / 1e3)
+
+
+def measure_reference_params(pkg, torch, args, stream):
+    """The same workload (particles, box, moving wall, iterations, dt) with the
+    reference's own solver parameters (fluids/FluidSystem.cpp:15-25), under
+    which the fluid stays a fluid: warm-up and timed steps as the main run,
+    timed the same way (L2 flushed before every step)."""
+    scene = make_scene(pkg, args.scene, "reference")
+    p = scene.params
+    st = pkg.ParticleState(scene.pos, scene.vel)
+    sim = pkg.Simulator(p, scene.ulim, scene.llim, scene.n)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    t = 0.0
+    total = 0.0
+    for k in range(args.warmup + args.steps):
+        ulim, llim = scene.limits_at(t)
+        if k >= args.warmup:
+            flush.fill_(1.0)
+            torch.cuda._sleep(2_000_000)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+        sim.setLim(ulim, llim)
+        st.step(sim)
+        if k >= args.warmup:
+            e1.record(stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1)
+        t += p.dt
+    sim.close()
+    return {"value": scene.n * args.steps / (total / 1e3), "unit": UNIT, "ms_per_step": total / args.steps,
+            "params": {"pho0": float(p.pho0), "lambda_eps": float(p.lambda_eps), "k_corr": round(float(p.k_corr), 6),
+                       "delta_q": round(float(p.delta_q), 6), "c_XSPH": float(p.c_XSPH)}}
 
 
 def measure_e2e(pkg, torch, sim, scene, state0, steps, stream):
@@ -361,6 +430,8 @@ def main(argv=None):
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
+    ap.add_argument("--cpu-steps", type=int, default=3, help="most steps the CPU baseline times")
+    ap.add_argument("--cpu-warmup-steps", type=int, default=3, help="most warm-up steps of the reference arm")
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
     args = ap.parse_args(argv)
     if args.warmup < 3:

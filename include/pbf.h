@@ -159,6 +159,15 @@ pbf_status pbf_profile_enable(pbf_solver* s, int on);
 pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out);
 
 /*
+ * Whether pbf_step runs as a CUDA graph (default: on).  The step's launches
+ * are captured on an internal stream, the solver's executable graph is
+ * updated in place (new wall positions only change kernel arguments) and
+ * launched on the caller's stream; off, the kernels are launched one by one.
+ * No counterpart in the reference, which launches eagerly and synchronises.
+ */
+pbf_status pbf_use_graphs(pbf_solver* s, int on);
+
+/*
  * One step, same contract and results as pbf_step, for callers that cannot
  * allocate device memory (no pbf_solver, so no pbf_create).  It has no
  * counterpart in the reference.  It calls no cudaMalloc or cudaFree: its

@@ -36,6 +36,7 @@ EXPORTED = (
     "pbf_build_grid",
     "pbf_profile_enable",
     "pbf_profile_read",
+    "pbf_use_graphs",
     "pbf_step_noalloc",
 )
 
@@ -130,6 +131,7 @@ def _declare(L) -> None:
         "pbf_build_grid": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, vp, vp, vp, P(ctypes.c_int), vp]),
         "pbf_profile_enable": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_profile_read": (ctypes.c_int, [vp, P(PbfStepProfile)]),
+        "pbf_use_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
     }
     for name, (res, args) in sig.items():

@@ -38,6 +38,10 @@ struct pbf_solver {
   int prof_iters;       // iterations recorded by the last profiled step (0: none)
   int last_launches;    // kernels launched by the last pbf_step
   int last_grid_launches;
+  // CUDA graph of the step: captured on cap_stream, updated in place each step
+  bool use_graph;
+  cudaStream_t cap_stream;
+  cudaGraphExec_t exec;
 };
 
 namespace {
@@ -196,6 +200,8 @@ void free_all(pbf_solver* s) {
     if (e) cudaEventDestroy(e);
   for (cudaEvent_t& e : s->ev_it)
     if (e) cudaEventDestroy(e);
+  if (s->exec) cudaGraphExecDestroy(s->exec);
+  if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
 }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
@@ -289,6 +295,8 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.flags, (size_t)pbf::kNumFlags);
   if (e == cudaSuccess) e = alloc(&s->sol.dense, pbf::dense_list_len(max_particles));
   if (e == cudaSuccess) s->num_sms = current_sms();
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
+  s->use_graph = true;
   if (e != cudaSuccess) {
     free_all(s);
     delete s;
@@ -349,33 +357,19 @@ pbf_status pbf_get_limits(const pbf_solver* s, float ulim[3], float llim[3]) {
   return PBF_OK;
 }
 
-pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
-                    int n, void* stream) {
-  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
-  if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n < 0");
-  if (n > s->max_particles)
-    return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
-  if (n == 0) return PBF_OK;
-  const void* bufs[5] = {pos, npos, vel, nvel, iid};
-  for (int a = 0; a < 5; ++a) {
-    if (!bufs[a]) return fail(PBF_ERR_INVALID_ARG, "buffer %d is NULL", a);
-    if (!aligned16(bufs[a]) && a < 4) return fail(PBF_ERR_INVALID_ARG, "buffer %d not 16-byte aligned", a);
-    for (int b = 0; b < a; ++b)
-      if (bufs[a] == bufs[b]) return fail(PBF_ERR_INVALID_ARG, "buffers %d and %d alias", b, a);
-  }
-  int dims[3];
-  long long cells;
-  pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
-  if (st != PBF_OK) return st;
-  if (cells > s->max_cells) return fail(PBF_ERR_CAPACITY, "box needs %lld cells", cells);
-  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
-  cudaStream_t st_ = (cudaStream_t)stream;
-  const bool prof = s->profile;
+}  // extern "C"
+
+namespace {
+
+// Enqueues one step on stream st_ (a capturing stream when building the graph).
+pbf_status enqueue_step(pbf_solver* s, const pbf::StepConsts& c, void* pos, void* npos, void* vel,
+                        void* nvel, uint32_t* iid, int n, cudaStream_t st_, bool prof) {
   const int niter = s->params.niter;
   const int piters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
-  s->prof_iters = 0;
+  // External: under stream capture the record becomes an event-record node of
+  // the graph (a plain record would only order the capture).
 #define PBF_EV(e) \
-  if (prof) PBF_CUDA(cudaEventRecord((e), st_), "pbf_step: event")
+  if (prof) PBF_CUDA(cudaEventRecordWithFlags((e), st_, cudaEventRecordExternal), "pbf_step: event")
   PBF_EV(s->ev[kEvStart]);
   // advect + buildGridHash (fluids/Simulator.cpp:46-53)
   const uint32_t* perm = nullptr;
@@ -414,10 +408,87 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
            "pbf_step: xsph");
   PBF_EV(s->ev[kEvEnd]);
 #undef PBF_EV
+  return PBF_OK;
+}
+
+// Captures the step into a graph, updates the solver's executable graph in
+// place (kernel arguments change every step as the walls move; the topology
+// does not) or re-instantiates it, and launches it on st_.
+pbf_status launch_step_graph(pbf_solver* s, const pbf::StepConsts& c, void* pos, void* npos,
+                             void* vel, void* nvel, uint32_t* iid, int n, cudaStream_t st_,
+                             bool prof) {
+  PBF_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal),
+           "pbf_step: begin capture");
+  const pbf_status est = enqueue_step(s, c, pos, npos, vel, nvel, iid, n, s->cap_stream, prof);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(s->cap_stream, &g);
+  if (est != PBF_OK) {
+    if (g) cudaGraphDestroy(g);
+    return est;
+  }
+  if (ce != cudaSuccess) return cuda_fail(ce, "pbf_step: end capture");
+  if (s->exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(s->exec, g, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(s->exec);
+      s->exec = nullptr;
+    }
+  }
+  if (!s->exec) {
+    const cudaError_t ie = cudaGraphInstantiate(&s->exec, g, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(g);
+      s->exec = nullptr;
+      return cuda_fail(ie, "pbf_step: graph instantiate");
+    }
+  }
+  cudaGraphDestroy(g);
+  PBF_CUDA(cudaGraphLaunch(s->exec, st_), "pbf_step: graph launch");
+  return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
+                    int n, void* stream) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n < 0");
+  if (n > s->max_particles)
+    return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
+  if (n == 0) return PBF_OK;
+  const void* bufs[5] = {pos, npos, vel, nvel, iid};
+  for (int a = 0; a < 5; ++a) {
+    if (!bufs[a]) return fail(PBF_ERR_INVALID_ARG, "buffer %d is NULL", a);
+    if (!aligned16(bufs[a]) && a < 4) return fail(PBF_ERR_INVALID_ARG, "buffer %d not 16-byte aligned", a);
+    for (int b = 0; b < a; ++b)
+      if (bufs[a] == bufs[b]) return fail(PBF_ERR_INVALID_ARG, "buffers %d and %d alias", b, a);
+  }
+  int dims[3];
+  long long cells;
+  pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
+  if (st != PBF_OK) return st;
+  if (cells > s->max_cells) return fail(PBF_ERR_CAPACITY, "box needs %lld cells", cells);
+  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
+  cudaStream_t st_ = (cudaStream_t)stream;
+  const bool prof = s->profile;
+  s->prof_iters = 0;
+  st = s->use_graph ? launch_step_graph(s, c, pos, npos, vel, nvel, iid, n, st_, prof)
+                    : enqueue_step(s, c, pos, npos, vel, nvel, iid, n, st_, prof);
+  if (st != PBF_OK) return st;
+  const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
   s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1);
-  if (prof) s->prof_iters = piters;
+  if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
+  return PBF_OK;
+}
+
+pbf_status pbf_use_graphs(pbf_solver* s, int on) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  s->use_graph = on != 0;
   return PBF_OK;
 }
 

@@ -128,6 +128,10 @@ class Simulator:
               "pbf_build_grid")
         return {"keys": keys[:n], "perm": perm[:n], "start": start, "end": end, "dims": dims}
 
+    def use_graphs(self, on: bool = True) -> None:
+        """Run each step as a CUDA graph (default) or as individual launches."""
+        check(self._L.pbf_use_graphs(self._h, int(bool(on))), "pbf_use_graphs")
+
     def profile(self, on: bool = True) -> None:
         """Record CUDA events between the phases of every following step."""
         check(self._L.pbf_profile_enable(self._h, int(bool(on))), "pbf_profile_enable")
