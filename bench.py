@@ -419,6 +419,71 @@ def measure_e2e(pkg, torch, sim, scene, state0, steps, stream):
             "steps": steps, "ms_per_step": ms / steps}
 
 
+def run_ensemble(args):
+    """Ensemble scenes/s: 256 independent dam-break scenes (a x b x c lattices,
+    a, b, c uniform in [12, 40], each in its own (2a d, 2b d, 2c d) box), one
+    scene-step = one scene advanced one step.  Batched (pbf_batch_step: one
+    launch per pass for all scenes) vs one scene per launch (256 solvers
+    stepped in turn), same steps, same stream, CUDA events."""
+    import torch
+
+    pkg = load_pkg()
+    scenes = pkg.scenes.ensemble(seed=0, count=args.scenes)
+    p = scenes[0].params
+    if args.params == "reference":
+        q = pkg.default_params()
+        q.up[0], q.up[1], q.up[2] = 0.0, 1.0, 0.0
+        q.dt = p.dt
+        p = q
+    stream = torch.cuda.current_stream()
+    counts = [sc.n for sc in scenes]
+    pos = np.concatenate([sc.pos for sc in scenes])
+    # batched
+    st = pkg.ParticleState(pos, np.zeros_like(pos))
+    ens = pkg.Ensemble(p, [sc.ulim for sc in scenes], [sc.llim for sc in scenes], counts)
+    for _ in range(args.warmup):
+        st.step(ens)
+    torch.cuda.synchronize()
+    torch.cuda._sleep(5_000_000)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        st.step(ens)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1)
+    ens.close()
+    # one scene per launch
+    sts = [pkg.ParticleState(sc.pos, sc.vel) for sc in scenes]
+    sims = [pkg.Simulator(p, sc.ulim, sc.llim, sc.n) for sc in scenes]
+    for _ in range(args.warmup):
+        for s_, m in zip(sts, sims):
+            s_.step(m)
+    torch.cuda.synchronize()
+    torch.cuda._sleep(5_000_000)
+    e0.record(stream)
+    for _ in range(args.steps):
+        for s_, m in zip(sts, sims):
+            s_.step(m)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    single_ms = e0.elapsed_time(e1)
+    for m in sims:
+        m.close()
+    k = len(scenes) * args.steps
+    line = {
+        "metric": "ensemble scenes/s", "value": k / (batched_ms / 1e3), "unit": "scene-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{len(scenes)} dam-break scenes, a,b,c ~ U{{12..40}} (seed 0), "
+                               f"{sum(counts)} particles, {p.niter} iterations, dt=1/120 s",
+                   "params": args.params, "particles": sum(counts)},
+        "one_scene_per_launch": {"value": k / (single_ms / 1e3), "ms_per_step": single_ms / args.steps},
+        "batched_over_per_scene": single_ms / batched_ms,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -426,6 +491,9 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=120, help="untimed steps (default: 60 frames x 2 steps)")
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--scene", default="large_sweep", choices=("large_sweep", "double_dam", "dam_break"))
+    ap.add_argument("--workload", choices=("step", "ensemble"), default="step",
+                    help="step: particle-updates/s of one scene; ensemble: scene-steps/s of 256 scenes")
+    ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--params", choices=("scene", "reference"), default="scene",
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
     ap.add_argument("--e2e-steps", type=int, default=20)
@@ -436,7 +504,9 @@ def main(argv=None):
     args = ap.parse_args(argv)
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
-    if args.impl == "reference":
+    if args.workload == "ensemble":
+        run_ensemble(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

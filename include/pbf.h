@@ -168,6 +168,32 @@ pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out);
 pbf_status pbf_use_graphs(pbf_solver* s, int on);
 
 /*
+ * Batched ensemble: many independent scenes of uneven particle counts, each
+ * with its own box, advanced together, one launch per pass for all scenes.
+ * No counterpart in the reference (one Simulator per scene there).
+ * Particle arrays hold the scenes back to back: scene s occupies slots
+ * [offset_s, offset_s + counts[s]), offset_s = counts[0] + ... + counts[s-1].
+ * Every scene follows pbf_step's contract within its own range (stable cell
+ * order, outputs, vel = (npos - pos) / dt); scenes never exchange particles.
+ * All scenes share one parameter set.  At most 65535 scenes.
+ */
+typedef struct pbf_batch pbf_batch;
+
+/* ulim/llim: 3 * nscenes floats; counts: nscenes particle counts.  Reserves
+ * 4x the cells of the initial boxes, like pbf_create. */
+pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* ulim, const float* llim,
+                            const int* counts, pbf_batch** out);
+pbf_status pbf_batch_destroy(pbf_batch* b);
+/* Moves the walls of one scene (Simulator::setLim of that scene). */
+pbf_status pbf_batch_set_limits(pbf_batch* b, int scene, const float ulim[3], const float llim[3]);
+/* One step of every scene; the five buffers hold sum(counts) entries. */
+pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
+                          void* stream);
+/* rho of the last step's final lambda pass for all particles (device, sum(counts) floats). */
+pbf_status pbf_batch_get_density(const pbf_batch* b, float* rho, void* stream);
+pbf_status pbf_batch_use_graphs(pbf_batch* b, int on);
+
+/*
  * One step, same contract and results as pbf_step, for callers that cannot
  * allocate device memory (no pbf_solver, so no pbf_create).  It has no
  * counterpart in the reference.  It calls no cudaMalloc or cudaFree: its

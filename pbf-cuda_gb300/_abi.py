@@ -37,6 +37,12 @@ EXPORTED = (
     "pbf_profile_enable",
     "pbf_profile_read",
     "pbf_use_graphs",
+    "pbf_batch_create",
+    "pbf_batch_destroy",
+    "pbf_batch_set_limits",
+    "pbf_batch_step",
+    "pbf_batch_get_density",
+    "pbf_batch_use_graphs",
     "pbf_step_noalloc",
 )
 
@@ -132,6 +138,12 @@ def _declare(L) -> None:
         "pbf_profile_enable": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_profile_read": (ctypes.c_int, [vp, P(PbfStepProfile)]),
         "pbf_use_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pbf_batch_create": (ctypes.c_int, [P(PbfParams), ctypes.c_int, f3, f3, P(ctypes.c_int), P(vp)]),
+        "pbf_batch_destroy": (ctypes.c_int, [vp]),
+        "pbf_batch_set_limits": (ctypes.c_int, [vp, ctypes.c_int, f3, f3]),
+        "pbf_batch_step": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
+        "pbf_batch_get_density": (ctypes.c_int, [vp, vp, vp]),
+        "pbf_batch_use_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
     }
     for name, (res, args) in sig.items():

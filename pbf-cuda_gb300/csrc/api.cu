@@ -14,6 +14,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "pbf_internal.cuh"
 
@@ -116,6 +117,24 @@ double promote_decimal(float f) {
   return (double)f;
 }
 
+// A scene's box: limits, clamp bounds (double arithmetic with LIM_EPS, as the
+// reference's min/max against ulim.x - LIM_EPS, fluids/Simulator_kernel.cuh:190-192),
+// cells per axis and its first global cell id.
+pbf::SceneGeom make_geom(const pbf_params& p, const float ulim[3], const float llim[3],
+                         const int dims[3], int cell_base) {
+  pbf::SceneGeom g;
+  std::memset(&g, 0, sizeof(g));
+  for (int a = 0; a < 3; ++a) {
+    g.lo[a] = (float)((double)llim[a] + promote_decimal(p.lim_eps));
+    g.hi[a] = (float)((double)ulim[a] - promote_decimal(p.lim_eps));
+    g.llim[a] = llim[a];
+    g.ulim[a] = ulim[a];
+    g.dims[a] = dims[a];
+  }
+  g.cell_base = cell_base;
+  return g;
+}
+
 // The reference's host-side coefficients, bit for bit (see pbf_internal.cuh).
 pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const float llim[3],
                             const int dims[3], int num_sms) {
@@ -160,14 +179,8 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   c.c_xsph = p.c_XSPH;
   c.dt = p.dt;
   c.inv_dt = 1.f / p.dt;
-  for (int a = 0; a < 3; ++a) {
-    c.g[a] = -p.g * p.up[a];
-    c.lo[a] = (float)((double)llim[a] + promote_decimal(p.lim_eps));
-    c.hi[a] = (float)((double)ulim[a] - promote_decimal(p.lim_eps));
-    c.llim[a] = llim[a];
-    c.ulim[a] = ulim[a];
-    c.dims[a] = dims[a];
-  }
+  for (int a = 0; a < 3; ++a) c.g[a] = -p.g * p.up[a];
+  c.geom = make_geom(p, ulim, llim, dims, 0);
   c.cells = dims[0] * dims[1] * dims[2];
   c.dense_grid = 4 * (num_sms > 0 ? num_sms : 1);
   return c;
@@ -361,90 +374,105 @@ pbf_status pbf_get_limits(const pbf_solver* s, float ulim[3], float llim[3]) {
 
 namespace {
 
+// One step's launches: constants, geometry, scratch, and the profiling
+// events (null when the step is not profiled).
+struct StepPlan {
+  pbf::StepConsts c;
+  pbf::Geometry G;
+  pbf::GridScratch* grid;
+  pbf::SolverScratch* sol;
+  int niter;
+  cudaEvent_t* ev;     // [kEvFixed] or null
+  cudaEvent_t* ev_it;  // [3 * kMaxProfiledIters] or null
+};
+
 // Enqueues one step on stream st_ (a capturing stream when building the graph).
-pbf_status enqueue_step(pbf_solver* s, const pbf::StepConsts& c, void* pos, void* npos, void* vel,
-                        void* nvel, uint32_t* iid, int n, cudaStream_t st_, bool prof) {
-  const int niter = s->params.niter;
+pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, void* nvel,
+                        uint32_t* iid, int n, cudaStream_t st_) {
+  const pbf::StepConsts& c = P.c;
+  const pbf::Geometry& G = P.G;
+  const int niter = P.niter;
   const int piters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
+  const bool prof = P.ev != nullptr;
   // External: under stream capture the record becomes an event-record node of
   // the graph (a plain record would only order the capture).
 #define PBF_EV(e) \
   if (prof) PBF_CUDA(cudaEventRecordWithFlags((e), st_, cudaEventRecordExternal), "pbf_step: event")
-  PBF_EV(s->ev[kEvStart]);
+  PBF_EV(P.ev[kEvStart]);
   // advect + buildGridHash (fluids/Simulator.cpp:46-53)
   const uint32_t* perm = nullptr;
-  PBF_CUDA(pbf::build_grid(c, (const float4*)pos, (const float4*)vel, nullptr, n, s->grid, &perm,
+  PBF_CUDA(pbf::build_grid(c, G, (const float4*)pos, (const float4*)vel, nullptr, n, *P.grid, &perm,
                            nullptr, st_),
            "pbf_step: grid");
-  PBF_EV(s->ev[kEvGrid]);
-  PBF_CUDA(pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, s->sol, st_),
+  PBF_EV(P.ev[kEvGrid]);
+  PBF_CUDA(pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, *P.sol, st_),
            "pbf_step: reorder");
-  PBF_EV(s->ev[kEvReorder]);
+  PBF_EV(P.ev[kEvReorder]);
   // niter x correctDensity (fluids/Simulator.cpp:55-60), Jacobi ping-pong;
   // updateVelocity fused into the last position update (fluids/Simulator.cpp:62-66)
-  const uint32_t* cs = s->grid.cell_start;
-  float4* X = s->sol.xa;
-  float4* T = s->sol.xb;
+  const uint32_t* cs = P.grid->cell_start;
+  const pbf::SolverScratch& sol = *P.sol;
+  float4* X = sol.xa;
+  float4* T = sol.xb;
   for (int it = 0; it < niter; ++it) {
-    if (it < piters) PBF_EV(s->ev_it[3 * it]);
-    PBF_CUDA(pbf::launch_lambda(c, X, cs, n, s->sol, 2 * it, st_), "pbf_step: lambda");
-    if (it < piters) PBF_EV(s->ev_it[3 * it + 1]);
+    if (it < piters) PBF_EV(P.ev_it[3 * it]);
+    PBF_CUDA(pbf::launch_lambda(c, G, X, cs, n, sol, 2 * it, st_), "pbf_step: lambda");
+    if (it < piters) PBF_EV(P.ev_it[3 * it + 1]);
     if (it + 1 < niter) {
-      PBF_CUDA(pbf::launch_delta_p(c, X, cs, n, s->sol, 2 * it + 1, T, st_), "pbf_step: delta_p");
+      PBF_CUDA(pbf::launch_delta_p(c, G, X, cs, n, sol, 2 * it + 1, T, st_), "pbf_step: delta_p");
       float4* t = X;
       X = T;
       T = t;
     } else {
-      PBF_CUDA(pbf::launch_delta_p_final(c, X, cs, n, s->sol, 2 * it + 1, (float4*)pos,
+      PBF_CUDA(pbf::launch_delta_p_final(c, G, X, cs, n, sol, 2 * it + 1, (float4*)pos,
                                          (float4*)npos, (float4*)vel, iid, st_),
                "pbf_step: delta_p");
     }
-    if (it < piters) PBF_EV(s->ev_it[3 * it + 2]);
+    if (it < piters) PBF_EV(P.ev_it[3 * it + 2]);
   }
   // correctVelocity: XSPH (fluids/Simulator.cpp:68-71)
-  PBF_EV(s->ev[kEvXsphStart]);
-  PBF_CUDA(pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, cs, n, s->sol, 2 * niter,
+  PBF_EV(P.ev[kEvXsphStart]);
+  PBF_CUDA(pbf::launch_xsph(c, G, (const float4*)npos, (const float4*)vel, cs, n, sol, 2 * niter,
                             (float4*)nvel, st_),
            "pbf_step: xsph");
-  PBF_EV(s->ev[kEvEnd]);
+  PBF_EV(P.ev[kEvEnd]);
 #undef PBF_EV
   return PBF_OK;
 }
 
-// Captures the step into a graph, updates the solver's executable graph in
+// Captures the step into a graph, updates the executable graph `exec` in
 // place (kernel arguments change every step as the walls move; the topology
 // does not) or re-instantiates it, and launches it on st_.
-pbf_status launch_step_graph(pbf_solver* s, const pbf::StepConsts& c, void* pos, void* npos,
-                             void* vel, void* nvel, uint32_t* iid, int n, cudaStream_t st_,
-                             bool prof) {
-  PBF_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal),
-           "pbf_step: begin capture");
-  const pbf_status est = enqueue_step(s, c, pos, npos, vel, nvel, iid, n, s->cap_stream, prof);
+pbf_status launch_step_graph(const StepPlan& P, cudaStream_t cap, cudaGraphExec_t* exec, void* pos,
+                             void* npos, void* vel, void* nvel, uint32_t* iid, int n,
+                             cudaStream_t st_) {
+  PBF_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "pbf_step: begin capture");
+  const pbf_status est = enqueue_step(P, pos, npos, vel, nvel, iid, n, cap);
   cudaGraph_t g = nullptr;
-  const cudaError_t ce = cudaStreamEndCapture(s->cap_stream, &g);
+  const cudaError_t ce = cudaStreamEndCapture(cap, &g);
   if (est != PBF_OK) {
     if (g) cudaGraphDestroy(g);
     return est;
   }
   if (ce != cudaSuccess) return cuda_fail(ce, "pbf_step: end capture");
-  if (s->exec) {
+  if (*exec) {
     cudaGraphExecUpdateResultInfo info;
-    if (cudaGraphExecUpdate(s->exec, g, &info) != cudaSuccess) {
+    if (cudaGraphExecUpdate(*exec, g, &info) != cudaSuccess) {
       cudaGetLastError();
-      cudaGraphExecDestroy(s->exec);
-      s->exec = nullptr;
+      cudaGraphExecDestroy(*exec);
+      *exec = nullptr;
     }
   }
-  if (!s->exec) {
-    const cudaError_t ie = cudaGraphInstantiate(&s->exec, g, 0);
+  if (!*exec) {
+    const cudaError_t ie = cudaGraphInstantiate(exec, g, 0);
     if (ie != cudaSuccess) {
       cudaGraphDestroy(g);
-      s->exec = nullptr;
+      *exec = nullptr;
       return cuda_fail(ie, "pbf_step: graph instantiate");
     }
   }
   cudaGraphDestroy(g);
-  PBF_CUDA(cudaGraphLaunch(s->exec, st_), "pbf_step: graph launch");
+  PBF_CUDA(cudaGraphLaunch(*exec, st_), "pbf_step: graph launch");
   return PBF_OK;
 }
 
@@ -471,12 +499,20 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
   if (st != PBF_OK) return st;
   if (cells > s->max_cells) return fail(PBF_ERR_CAPACITY, "box needs %lld cells", cells);
-  const pbf::StepConsts c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
   cudaStream_t st_ = (cudaStream_t)stream;
   const bool prof = s->profile;
   s->prof_iters = 0;
-  st = s->use_graph ? launch_step_graph(s, c, pos, npos, vel, nvel, iid, n, st_, prof)
-                    : enqueue_step(s, c, pos, npos, vel, nvel, iid, n, st_, prof);
+  StepPlan P;
+  P.c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
+  P.G = pbf::Geometry{nullptr, nullptr};
+  P.grid = &s->grid;
+  P.sol = &s->sol;
+  P.niter = s->params.niter;
+  P.ev = prof ? s->ev : nullptr;
+  P.ev_it = prof ? s->ev_it : nullptr;
+  const pbf::StepConsts& c = P.c;
+  st = s->use_graph ? launch_step_graph(P, s->cap_stream, &s->exec, pos, npos, vel, nvel, iid, n, st_)
+                    : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
   if (st != PBF_OK) return st;
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
@@ -557,7 +593,8 @@ pbf_status pbf_build_grid(pbf_solver* s, const void* xstar, int n, uint32_t* key
     return PBF_OK;
   }
   const uint32_t* p = nullptr;
-  PBF_CUDA(pbf::build_grid(c, nullptr, nullptr, (const float4*)xstar, n, s->grid, &p, keys, st_),
+  PBF_CUDA(pbf::build_grid(c, pbf::Geometry{nullptr, nullptr}, nullptr, nullptr, (const float4*)xstar, n,
+                           s->grid, &p, keys, st_),
            "pbf_build_grid");
   PBF_CUDA(cudaMemcpyAsync(perm, p, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st_),
            "pbf_build_grid: perm");
@@ -602,3 +639,216 @@ pbf_status validate_step_buffers(const void* pos, const void* npos, const void* 
 }
 
 }  // namespace pbf
+
+// ---- batched ensemble ---------------------------------------------------------------
+
+struct pbf_batch {
+  pbf_params params;
+  int nscenes;
+  int n;          // particles of all scenes
+  int max_cells;  // cells reserved for all scenes together
+  int num_sms;
+  int device;
+  int last_n;
+  std::vector<float> ulim, llim;  // 3 * nscenes
+  std::vector<int> counts;
+  std::vector<pbf::SceneGeom> geom;  // host copy of the scene table
+  pbf::SceneGeom* d_geom;
+  uint16_t* d_sid;
+  pbf::GridScratch grid;
+  pbf::SolverScratch sol;
+  bool use_graph;
+  cudaStream_t cap_stream;
+  cudaGraphExec_t exec;
+};
+
+namespace {
+
+void batch_free(pbf_batch* b) {
+  void* ptrs[] = {b->grid.keys_a, b->grid.keys_b, b->grid.vals_a, b->grid.vals_b,
+                  b->grid.cell_count, b->grid.cell_start, b->grid.radix_counts,
+                  b->grid.scan_partials, b->sol.xs, b->sol.xa, b->sol.xb, b->sol.iid_s,
+                  b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->d_geom, b->d_sid};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+}
+
+// Rebuilds the host scene table from the current limits; returns the total cells.
+pbf_status batch_tables(pbf_batch* b, long long* total_cells) {
+  long long base = 0;
+  for (int k = 0; k < b->nscenes; ++k) {
+    int dims[3];
+    long long cells;
+    pbf_status st = grid_dims(&b->ulim[3 * k], &b->llim[3 * k], b->params.h, dims, &cells);
+    if (st != PBF_OK) return st;
+    if (base + cells > 2147483647LL) return fail(PBF_ERR_CAPACITY, "too many cells");
+    b->geom[k] = make_geom(b->params, &b->ulim[3 * k], &b->llim[3 * k], dims, (int)base);
+    base += cells;
+  }
+  *total_cells = base;
+  return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* ulim, const float* llim,
+                            const int* counts, pbf_batch** out) {
+  g_err[0] = 0;
+  if (!out) return fail(PBF_ERR_INVALID_ARG, "out is NULL");
+  *out = nullptr;
+  if (!ulim || !llim || !counts) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  if (nscenes < 1 || nscenes > 65535) return fail(PBF_ERR_INVALID_ARG, "nscenes must be in [1, 65535]");
+  pbf_status st = check_params(params);
+  if (st != PBF_OK) return st;
+  long long n = 0;
+  for (int k = 0; k < nscenes; ++k) {
+    if (counts[k] < 0) return fail(PBF_ERR_INVALID_ARG, "counts[%d] < 0", k);
+    n += counts[k];
+  }
+  if (n > 2147483647LL / 2) return fail(PBF_ERR_CAPACITY, "too many particles");
+  pbf_batch* b = new (std::nothrow) pbf_batch();
+  if (!b) return fail(PBF_ERR_CAPACITY, "host allocation failed");
+  b->params = *params;
+  b->nscenes = nscenes;
+  b->n = (int)n;
+  b->ulim.assign(ulim, ulim + 3 * nscenes);
+  b->llim.assign(llim, llim + 3 * nscenes);
+  b->counts.assign(counts, counts + nscenes);
+  b->geom.resize(nscenes);
+  long long cells;
+  if ((st = batch_tables(b, &cells)) != PBF_OK) {
+    delete b;
+    return st;
+  }
+  long long max_cells = 4 * cells;
+  const long long scan_cap = (long long)pbf::kScanTile * pbf::kMaxScanPartials - 1;
+  if (max_cells > scan_cap) max_cells = cells;
+  if (max_cells > scan_cap) {
+    delete b;
+    return fail(PBF_ERR_CAPACITY, "scenes need %lld cells, limit %lld", cells, scan_cap);
+  }
+  b->max_cells = (int)max_cells;
+  cudaError_t e = cudaGetDevice(&b->device);
+  const size_t np = (size_t)(n > 0 ? n : 1), nc = (size_t)max_cells + 1;
+  if (e == cudaSuccess) e = alloc(&b->grid.keys_a, np);
+  if (e == cudaSuccess) e = alloc(&b->grid.keys_b, np);
+  if (e == cudaSuccess) e = alloc(&b->grid.vals_a, np);
+  if (e == cudaSuccess) e = alloc(&b->grid.vals_b, np);
+  if (e == cudaSuccess) e = alloc(&b->grid.cell_count, nc);
+  if (e == cudaSuccess) e = alloc(&b->grid.cell_start, nc);
+  if (e == cudaSuccess) e = alloc(&b->grid.radix_counts, pbf::radix_counts_len((int)np));
+  if (e == cudaSuccess) e = alloc(&b->grid.scan_partials, (size_t)pbf::kMaxScanPartials);
+  if (e == cudaSuccess) e = alloc(&b->sol.xs, np);
+  if (e == cudaSuccess) e = alloc(&b->sol.xa, np);
+  if (e == cudaSuccess) e = alloc(&b->sol.xb, np);
+  if (e == cudaSuccess) e = alloc(&b->sol.iid_s, np);
+  if (e == cudaSuccess) e = alloc(&b->sol.lambda, np);
+  if (e == cudaSuccess) e = alloc(&b->sol.rho, np);
+  if (e == cudaSuccess) e = alloc(&b->sol.flags, (size_t)pbf::kNumFlags);
+  if (e == cudaSuccess) e = alloc(&b->sol.dense, pbf::dense_list_len((int)np));
+  if (e == cudaSuccess) e = alloc(&b->d_geom, (size_t)nscenes);
+  if (e == cudaSuccess) e = alloc(&b->d_sid, np);
+  if (e == cudaSuccess) {
+    std::vector<uint16_t> sid(np, 0);
+    size_t k = 0;
+    for (int sc = 0; sc < nscenes; ++sc)
+      for (int j = 0; j < counts[sc]; ++j) sid[k++] = (uint16_t)sc;
+    e = cudaMemcpy(b->d_sid, sid.data(), sizeof(uint16_t) * np, cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    batch_free(b);
+    delete b;
+    cudaGetLastError();
+    return cuda_fail(e, "pbf_batch_create");
+  }
+  b->num_sms = current_sms();
+  b->use_graph = true;
+  *out = b;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_destroy(pbf_batch* b) {
+  if (!b) return PBF_OK;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  if (prev != b->device) cudaSetDevice(b->device);
+  batch_free(b);
+  if (prev >= 0 && prev != b->device) cudaSetDevice(prev);
+  delete b;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_set_limits(pbf_batch* b, int scene, const float ulim[3], const float llim[3]) {
+  if (!b || !ulim || !llim) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  if (scene < 0 || scene >= b->nscenes) return fail(PBF_ERR_INVALID_ARG, "scene %d out of range", scene);
+  const std::vector<float> old_u(b->ulim.begin() + 3 * scene, b->ulim.begin() + 3 * scene + 3);
+  const std::vector<float> old_l(b->llim.begin() + 3 * scene, b->llim.begin() + 3 * scene + 3);
+  std::memcpy(&b->ulim[3 * scene], ulim, sizeof(float) * 3);
+  std::memcpy(&b->llim[3 * scene], llim, sizeof(float) * 3);
+  long long cells;
+  pbf_status st = batch_tables(b, &cells);
+  if (st == PBF_OK && cells > b->max_cells)
+    st = fail(PBF_ERR_CAPACITY, "scenes need %lld cells, %d reserved", cells, b->max_cells);
+  if (st != PBF_OK) {
+    std::memcpy(&b->ulim[3 * scene], old_u.data(), sizeof(float) * 3);
+    std::memcpy(&b->llim[3 * scene], old_l.data(), sizeof(float) * 3);
+    long long ignored;
+    batch_tables(b, &ignored);
+  }
+  return st;
+}
+
+pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
+                          void* stream) {
+  if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+  const int n = b->n;
+  if (n == 0) return PBF_OK;
+  if (pbf::validate_step_buffers(pos, npos, vel, nvel, iid) != PBF_OK) return PBF_ERR_INVALID_ARG;
+  long long cells;
+  pbf_status st = batch_tables(b, &cells);
+  if (st != PBF_OK) return st;
+  if (cells > b->max_cells) return fail(PBF_ERR_CAPACITY, "scenes need %lld cells", cells);
+  cudaStream_t st_ = (cudaStream_t)stream;
+  // the scene table goes in stream order ahead of the step (pageable source:
+  // staged before the call returns, so the host copy may change afterwards)
+  PBF_CUDA(cudaMemcpyAsync(b->d_geom, b->geom.data(), sizeof(pbf::SceneGeom) * b->nscenes,
+                           cudaMemcpyHostToDevice, st_),
+           "pbf_batch_step: scene table");
+  StepPlan P;
+  int unit_dims[3] = {1, 1, 1};
+  P.c = make_consts(b->params, &b->ulim[0], &b->llim[0], unit_dims, b->num_sms);
+  P.c.cells = (int)cells;
+  P.G = pbf::Geometry{b->d_geom, b->d_sid};
+  P.grid = &b->grid;
+  P.sol = &b->sol;
+  P.niter = b->params.niter;
+  P.ev = nullptr;
+  P.ev_it = nullptr;
+  st = b->use_graph ? launch_step_graph(P, b->cap_stream, &b->exec, pos, npos, vel, nvel, iid, n, st_)
+                    : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
+  if (st != PBF_OK) return st;
+  b->last_n = n;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_get_density(const pbf_batch* b, float* rho, void* stream) {
+  if (!b || !rho) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
+  if (b->last_n == 0) return fail(PBF_ERR_NOT_READY, "no step has run");
+  PBF_CUDA(cudaMemcpyAsync(rho, b->sol.rho, sizeof(float) * b->n, cudaMemcpyDeviceToDevice,
+                           (cudaStream_t)stream),
+           "pbf_batch_get_density");
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_use_graphs(pbf_batch* b, int on) {
+  if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+  b->use_graph = on != 0;
+  return PBF_OK;
+}
+
+}  // extern "C"

@@ -136,7 +136,7 @@ cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, int len, uint32_t*
 template <bool kPredict>
 __global__ void __launch_bounds__(256)
 k_hash(const float4* __restrict__ pos, const float4* __restrict__ vel, int n, StepConsts c,
-       uint32_t* __restrict__ keys, uint32_t* __restrict__ cell_count) {
+       Geometry G, uint32_t* __restrict__ keys, uint32_t* __restrict__ cell_count) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float4 x = pos[i];
@@ -148,8 +148,9 @@ k_hash(const float4* __restrict__ pos, const float4* __restrict__ vel, int n, St
     x.y = fmaf(c.dt, vy, x.y);
     x.z = fmaf(c.dt, vz, x.z);
   }
-  const int3 q = cell_of(c, x);
-  const uint32_t key = (uint32_t)cell_index(c, q.x, q.y, q.z);
+  const SceneGeom g = geom_of(c, G, i);
+  const int3 q = cell_of(c, g, x);
+  const uint32_t key = (uint32_t)cell_index(g, q.x, q.y, q.z);
   keys[i] = key;
   atomicAdd(&cell_count[key], 1u);
 }
@@ -265,7 +266,7 @@ size_t radix_counts_len(int max_particles) {
   return (size_t)kRadix * (size_t)(sort_tiles(max_particles) > 0 ? sort_tiles(max_particles) : 1);
 }
 
-cudaError_t build_grid(const StepConsts& c, const float4* pos, const float4* vel,
+cudaError_t build_grid(const StepConsts& c, const Geometry& G, const float4* pos, const float4* vel,
                        const float4* xstar, int n, GridScratch& s, const uint32_t** perm_out,
                        uint32_t* keys_copy, cudaStream_t stream) {
   cudaError_t err;
@@ -274,9 +275,9 @@ cudaError_t build_grid(const StepConsts& c, const float4* pos, const float4* vel
     return err;
   const int blocks = (n + 255) / 256;
   if (xstar)
-    k_hash<false><<<blocks, 256, 0, stream>>>(xstar, nullptr, n, c, s.keys_a, s.cell_count);
+    k_hash<false><<<blocks, 256, 0, stream>>>(xstar, nullptr, n, c, G, s.keys_a, s.cell_count);
   else
-    k_hash<true><<<blocks, 256, 0, stream>>>(pos, vel, n, c, s.keys_a, s.cell_count);
+    k_hash<true><<<blocks, 256, 0, stream>>>(pos, vel, n, c, G, s.keys_a, s.cell_count);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   if (keys_copy &&
       (err = cudaMemcpyAsync(keys_copy, s.keys_a, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,

@@ -134,7 +134,8 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   cudaError_t e;
   const uint32_t* perm = nullptr;
   // build_grid clears the per-cell counters itself (cudaMemsetAsync, no allocation)
-  if ((e = pbf::build_grid(c, (const float4*)pos, (const float4*)vel, nullptr, n, g, &perm, nullptr,
+  const pbf::Geometry G{nullptr, nullptr};
+  if ((e = pbf::build_grid(c, G, (const float4*)pos, (const float4*)vel, nullptr, n, g, &perm, nullptr,
                            strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: grid");
   if ((e = pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, s, strm)) != cudaSuccess)
@@ -143,20 +144,20 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   float4* X = s.xa;
   float4* T = s.xb;
   for (int it = 0; it < niter; ++it) {
-    if ((e = pbf::launch_lambda(c, X, g.cell_start, n, s, 2 * it, strm)) != cudaSuccess)
+    if ((e = pbf::launch_lambda(c, G, X, g.cell_start, n, s, 2 * it, strm)) != cudaSuccess)
       return pbf::set_cuda_error(e, "pbf_step_noalloc: lambda");
     if (it + 1 < niter) {
-      if ((e = pbf::launch_delta_p(c, X, g.cell_start, n, s, 2 * it + 1, T, strm)) != cudaSuccess)
+      if ((e = pbf::launch_delta_p(c, G, X, g.cell_start, n, s, 2 * it + 1, T, strm)) != cudaSuccess)
         return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
       float4* t = X;
       X = T;
       T = t;
-    } else if ((e = pbf::launch_delta_p_final(c, X, g.cell_start, n, s, 2 * it + 1, (float4*)pos,
+    } else if ((e = pbf::launch_delta_p_final(c, G, X, g.cell_start, n, s, 2 * it + 1, (float4*)pos,
                                               (float4*)npos, (float4*)vel, iid, strm)) != cudaSuccess) {
       return pbf::set_cuda_error(e, "pbf_step_noalloc: delta_p");
     }
   }
-  if ((e = pbf::launch_xsph(c, (const float4*)npos, (const float4*)vel, g.cell_start, n, s, 2 * niter,
+  if ((e = pbf::launch_xsph(c, G, (const float4*)npos, (const float4*)vel, g.cell_start, n, s, 2 * niter,
                             (float4*)nvel, strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: xsph");
   return PBF_OK;

@@ -13,6 +13,14 @@ namespace pbf {
 // kernel coefficients (getPoly6 / getSpikyGrad constructors).
 constexpr double kRefPi = 3.14159265359;
 
+// The box of one scene and where its cells sit in the global cell numbering.
+struct SceneGeom {
+  float llim[3], ulim[3];
+  float lo[3], hi[3];      // wall clamp bounds: llim + lim_eps, ulim - lim_eps (rounded once from double)
+  int dims[3];             // cells per axis
+  int cell_base;           // global id of the scene's cell 0
+};
+
 // Everything a pass needs, computed once per step on the host and passed by
 // value.  Coefficients follow the reference's host-side set-up bit for bit
 // (fluids/Simulator.cu:77-98, :129, :187-188, :235).
@@ -32,12 +40,23 @@ struct StepConsts {
   float c_xsph;
   float dt, inv_dt;
   float g[3];              // gravity vector = -g * up
-  float lo[3], hi[3];      // wall clamp bounds: llim + lim_eps, ulim - lim_eps (rounded once from double)
-  float llim[3], ulim[3];
-  int dims[3];             // cells per axis
-  int cells;
+  int cells;               // cells of all scenes
   int dense_grid;          // blocks of the dense neighbour kernels (a multiple of the SM count)
+  SceneGeom geom;          // the box of a single-scene step
 };
+
+// Where a particle's box comes from: the single scene in StepConsts, or a
+// table of scenes indexed by a per-particle scene id.  Scenes occupy
+// contiguous particle ranges, before and after the cell sort alike, so one
+// id array serves both orders.
+struct Geometry {
+  const SceneGeom* scenes;  // nullptr: single scene
+  const uint16_t* sid;      // [n] scene of each particle slot
+};
+
+__device__ __forceinline__ SceneGeom geom_of(const StepConsts& c, const Geometry& G, int i) {
+  return G.scenes ? G.scenes[G.sid[i]] : c.geom;
+}
 
 // Cell coordinate along one axis: getGridxyz / getGridId (fluids/Simulator.cu:30-36,
 // :65-71): IEEE (p - llim) / h, truncating conversion (saturating, NaN -> 0),
@@ -47,15 +66,15 @@ __device__ __forceinline__ int cell_coord(float p, float llim, float h, int dim)
   return min(max(v, 0), dim - 1);
 }
 
-__device__ __forceinline__ int3 cell_of(const StepConsts& c, float4 p) {
-  return make_int3(cell_coord(p.x, c.llim[0], c.h, c.dims[0]),
-                   cell_coord(p.y, c.llim[1], c.h, c.dims[1]),
-                   cell_coord(p.z, c.llim[2], c.h, c.dims[2]));
+__device__ __forceinline__ int3 cell_of(const StepConsts& c, const SceneGeom& g, float4 p) {
+  return make_int3(cell_coord(p.x, g.llim[0], c.h, g.dims[0]),
+                   cell_coord(p.y, g.llim[1], c.h, g.dims[1]),
+                   cell_coord(p.z, g.llim[2], c.h, g.dims[2]));
 }
 
-// xyzToId (fluids/Simulator.cu:44-53): x-major, z fastest.
-__device__ __forceinline__ int cell_index(const StepConsts& c, int x, int y, int z) {
-  return (x * c.dims[1] + y) * c.dims[2] + z;
+// xyzToId (fluids/Simulator.cu:44-53): x-major, z fastest; offset to the scene's cells.
+__device__ __forceinline__ int cell_index(const SceneGeom& g, int x, int y, int z) {
+  return g.cell_base + (x * g.dims[1] + y) * g.dims[2] + z;
 }
 
 // |a - b|^2 with the fused multiply-adds nvcc forms for the reference's
@@ -90,10 +109,10 @@ __device__ __forceinline__ float density_at(float d, float h) {
   return k * (h - d) * (h - d) * (h + d);
 }
 
-__device__ __forceinline__ float boundary_density(const StepConsts& c, float4 p) {
-  return density_at(c.ulim[0] - p.x, c.h) + density_at(p.x - c.llim[0], c.h) +
-         density_at(c.ulim[1] - p.y, c.h) + density_at(p.y - c.llim[1], c.h) +
-         density_at(c.ulim[2] - p.z, c.h) + density_at(p.z - c.llim[2], c.h);
+__device__ __forceinline__ float boundary_density(const StepConsts& c, const SceneGeom& g, float4 p) {
+  return density_at(g.ulim[0] - p.x, c.h) + density_at(p.x - g.llim[0], c.h) +
+         density_at(g.ulim[1] - p.y, c.h) + density_at(p.y - g.llim[1], c.h) +
+         density_at(g.ulim[2] - p.z, c.h) + density_at(p.z - g.llim[2], c.h);
 }
 
 // ---- launch wrappers (grid.cu) ------------------------------------------------
@@ -123,7 +142,7 @@ size_t radix_counts_len(int max_particles);
 // On return (stream order): *perm_out points at the sorted-slot -> input index
 // array (inside scratch), scratch.cell_start holds cells + 1 prefix entries.
 // keys_copy (optional, n entries) receives the unsorted cell ids.
-cudaError_t build_grid(const StepConsts& c, const float4* pos, const float4* vel,
+cudaError_t build_grid(const StepConsts& c, const Geometry& G, const float4* pos, const float4* vel,
                        const float4* xstar, int n, GridScratch& s, const uint32_t** perm_out,
                        uint32_t* keys_copy, cudaStream_t stream);
 
@@ -168,18 +187,18 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
 // numbers the passes of a step (0, 1, 2, ...) and picks the dense counter.
 
 // lambda_i and rho_i of every particle at positions X.
-cudaError_t launch_lambda(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+cudaError_t launch_lambda(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                           const SolverScratch& s, int pass, cudaStream_t stream);
 // One Jacobi position update X -> T.
-cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+cudaError_t launch_delta_p(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                            const SolverScratch& s, int pass, float4* T, cudaStream_t stream);
 // Last position update: x_final -> npos, (x_final - x) / dt -> vel, and the
 // permuted inputs -> pos, iid.
-cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                                  const SolverScratch& s, int pass, float4* pos, float4* npos,
                                  float4* vel, uint32_t* iid, cudaStream_t stream);
 // XSPH: nvel = vel + c sum_j 2 (v_j - v_i) W / (rho_i + rho_j).
-cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const uint32_t* cs,
+cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X, const float4* V, const uint32_t* cs,
                         int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream);
 
 // Kernel launches of one neighbour pass.

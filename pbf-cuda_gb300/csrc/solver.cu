@@ -53,6 +53,7 @@ enum PassKind { kLambda = 0, kDeltaP = 1, kDeltaPFinal = 2, kXsph = 3 };
 // Everything any pass kernel needs (passed by value).
 struct PassArgs {
   StepConsts c;
+  Geometry G;
   const float4* X;        // positions the pass reads (sorted)
   const uint32_t* cs;     // cell prefix, cells + 1 entries
   int n;
@@ -77,25 +78,25 @@ struct PassArgs {
 
 // Sorted-slot range [s, e) of cells (x, y, z-1 .. z+1) clipped to the grid.
 // cs[cells] == n, so e <= n; the clamps keep even an inconsistent table in range.
-__device__ __forceinline__ void column_run(const StepConsts& c, const uint32_t* __restrict__ cs,
+__device__ __forceinline__ void column_run(const SceneGeom& g, const uint32_t* __restrict__ cs,
                                            int n, int x, int y, int z, int& s, int& e) {
-  const int zlo = max(z - 1, 0), zhi = min(z + 1, c.dims[2] - 1);
-  const int base = (x * c.dims[1] + y) * c.dims[2];
+  const int zlo = max(z - 1, 0), zhi = min(z + 1, g.dims[2] - 1);
+  const int base = g.cell_base + (x * g.dims[1] + y) * g.dims[2];
   s = (int)__ldg(cs + base + zlo);
   e = max(min((int)__ldg(cs + base + zhi + 1), n), s);
 }
 
-__device__ __forceinline__ int window_total(const StepConsts& c, const uint32_t* __restrict__ cs,
+__device__ __forceinline__ int window_total(const SceneGeom& g, const uint32_t* __restrict__ cs,
                                             int n, int3 q) {
   int total = 0;
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
-    if (x < 0 || x >= c.dims[0]) continue;
+    if (x < 0 || x >= g.dims[0]) continue;
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
-      if (y < 0 || y >= c.dims[1]) continue;
+      if (y < 0 || y >= g.dims[1]) continue;
       int s, e;
-      column_run(c, cs, n, x, y, q.z, s, e);
+      column_run(g, cs, n, x, y, q.z, s, e);
       total += e - s;
     }
   }
@@ -104,16 +105,16 @@ __device__ __forceinline__ int window_total(const StepConsts& c, const uint32_t*
 
 // Every candidate of the window, in order.
 template <class P>
-__device__ __forceinline__ void visit_window(const StepConsts& c, const uint32_t* __restrict__ cs,
+__device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t* __restrict__ cs,
                                              int n, int3 q, const float4* __restrict__ X, P& p) {
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
-    if (x < 0 || x >= c.dims[0]) continue;
+    if (x < 0 || x >= g.dims[0]) continue;
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
-      if (y < 0 || y >= c.dims[1]) continue;
+      if (y < 0 || y >= g.dims[1]) continue;
       int s, e;
-      column_run(c, cs, n, x, y, q.z, s, e);
+      column_run(g, cs, n, x, y, q.z, s, e);
       for (int j = s; j < e; ++j) p.visit(__ldg(X + j), j);
     }
   }
@@ -122,19 +123,19 @@ __device__ __forceinline__ void visit_window(const StepConsts& c, const uint32_t
 // Candidates [v_lo, v_hi) of the window (numbered in visiting order), four
 // loads in flight at a time.
 template <class P>
-__device__ __forceinline__ void visit_window_chunk(const StepConsts& c,
+__device__ __forceinline__ void visit_window_chunk(const SceneGeom& g,
                                                    const uint32_t* __restrict__ cs, int n, int3 q,
                                                    const float4* __restrict__ X, P& p, int v_lo,
                                                    int v_hi) {
   int v0 = 0;
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
-    if (x < 0 || x >= c.dims[0]) continue;
+    if (x < 0 || x >= g.dims[0]) continue;
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
-      if (y < 0 || y >= c.dims[1]) continue;
+      if (y < 0 || y >= g.dims[1]) continue;
       int s, e;
-      column_run(c, cs, n, x, y, q.z, s, e);
+      column_run(g, cs, n, x, y, q.z, s, e);
       const int len = e - s;
       const int a = max(v_lo, v0), b = min(v_hi, v0 + len);
       v0 += len;
@@ -159,11 +160,13 @@ __device__ __forceinline__ void visit_window_chunk(const StepConsts& c,
 struct LambdaPass {
   static constexpr int kFields = 5;
   const StepConsts& c;
+  const SceneGeom& g;
   float4 xi;
   int i;
   float pho = 0.f, gx = 0.f, gy = 0.f, gz = 0.f, gl2 = 0.f;
 
-  __device__ LambdaPass(const PassArgs& a, float4 xi_, int i_, bool) : c(a.c), xi(xi_), i(i_) {}
+  __device__ LambdaPass(const PassArgs& a, const SceneGeom& g_, float4 xi_, int i_, bool)
+      : c(a.c), g(g_), xi(xi_), i(i_) {}
   __device__ __forceinline__ void visit(float4 xj, int j) {
     const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
     const float r2 = dist2(ex, ey, ez);
@@ -189,7 +192,7 @@ struct LambdaPass {
   }
   __device__ void finish(const PassArgs& a) const {
     float rho = pho;
-    if (c.k_b != 0.f) rho += c.k_b * boundary_density(c, xi);
+    if (c.k_b != 0.f) rho += c.k_b * boundary_density(c, g, xi);
     const float grad_l2 = gl2 + dist2(gx, gy, gz);
     const float lam = -(rho / c.pho0 - 1.f) / (grad_l2 + c.lambda_eps);
     a.lambda[i] = lam;
@@ -206,6 +209,7 @@ template <bool kFinal>
 struct DeltaPPass {
   static constexpr int kFields = 4;
   const StepConsts& c;
+  const SceneGeom& g;
   const float* __restrict__ lambda;
   float4 xi;
   int i;
@@ -214,8 +218,8 @@ struct DeltaPPass {
   float ax = 0.f, ay = 0.f, az = 0.f;
   bool poison = false;
 
-  __device__ DeltaPPass(const PassArgs& a, float4 xi_, int i_, bool exact_)
-      : c(a.c), lambda(a.lambda), xi(xi_), i(i_), li(a.lambda[i_]), exact(exact_) {}
+  __device__ DeltaPPass(const PassArgs& a, const SceneGeom& g_, float4 xi_, int i_, bool exact_)
+      : c(a.c), g(g_), lambda(a.lambda), xi(xi_), i(i_), li(a.lambda[i_]), exact(exact_) {}
   __device__ __forceinline__ void visit(float4 xj, int j) {
     const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
     const float r2 = dist2(ex, ey, ez);
@@ -248,9 +252,9 @@ struct DeltaPPass {
     const float dx = fmaxf(fminf(sx / c.pho0, c.max_dp), -c.max_dp);
     const float dy = fmaxf(fminf(sy / c.pho0, c.max_dp), -c.max_dp);
     const float dz = fmaxf(fminf(sz / c.pho0, c.max_dp), -c.max_dp);
-    const float4 xf = make_float4(fmaxf(fminf(xi.x + dx, c.hi[0]), c.lo[0]),
-                                  fmaxf(fminf(xi.y + dy, c.hi[1]), c.lo[1]),
-                                  fmaxf(fminf(xi.z + dz, c.hi[2]), c.lo[2]), xi.w);
+    const float4 xf = make_float4(fmaxf(fminf(xi.x + dx, g.hi[0]), g.lo[0]),
+                                  fmaxf(fminf(xi.y + dy, g.hi[1]), g.lo[1]),
+                                  fmaxf(fminf(xi.z + dz, g.hi[2]), g.lo[2]), xi.w);
     if (!kFinal) {
       a.T[i] = xf;
       return;
@@ -283,7 +287,7 @@ struct XsphPass {
   float ax = 0.f, ay = 0.f, az = 0.f;
   bool px = false, py = false, pz = false;
 
-  __device__ XsphPass(const PassArgs& a, float4 xi_, int i_, bool exact_)
+  __device__ XsphPass(const PassArgs& a, const SceneGeom&, float4 xi_, int i_, bool exact_)
       : c(a.c), V(a.V), rho(a.rho), xi(xi_), vi(a.V[i_]), ri(a.rho[i_]), i(i_), exact(exact_) {}
   __device__ __forceinline__ void visit(float4 xj, int j) {
     const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
@@ -339,15 +343,16 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
   const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const int3 q = cell_of(a.c, xi);
-  const int total = valid ? window_total(a.c, a.cs, a.n, q) : 0;
+  const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
+  const int3 q = cell_of(a.c, g, xi);
+  const int total = valid ? window_total(g, a.cs, a.n, q) : 0;
   if (__any_sync(kFull, total > kDenseWindow)) {
     if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(i >> 5);
     return;
   }
   if (!valid) return;
-  P p(a, xi, i, exact_path(kKind, a.flags));
-  visit_window(a.c, a.cs, a.n, q, a.X, p);
+  P p(a, g, xi, i, exact_path(kKind, a.flags));
+  visit_window(g, a.cs, a.n, q, a.X, p);
   p.finish(a);
 }
 
@@ -364,18 +369,19 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     const int i = (int)a.dense[item] * 32 + lane;
     const bool valid = i < a.n;
     const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const int3 q = cell_of(a.c, xi);
+    const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
+    const int3 q = cell_of(a.c, g, xi);
     if (valid) {
-      const int total = window_total(a.c, a.cs, a.n, q);
+      const int total = window_total(g, a.cs, a.n, q);
       const int lo = (int)((long long)total * warp / kDenseWarps);
       const int hi = (int)((long long)total * (warp + 1) / kDenseWarps);
-      P p(a, xi, i, exact);
-      visit_window_chunk(a.c, a.cs, a.n, q, a.X, p, lo, hi);
+      P p(a, g, xi, i, exact);
+      visit_window_chunk(g, a.cs, a.n, q, a.X, p, lo, hi);
       p.store(&part[warp][0][lane], 32);
     }
     __syncthreads();
     if (warp == 0 && valid) {
-      P p(a, xi, i, exact);
+      P p(a, g, xi, i, exact);
       for (int k = 0; k < kDenseWarps; ++k) p.add(&part[k][0][lane], 32);
       p.finish(a);
     }
@@ -401,10 +407,11 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
   iid_s[k] = iid[p];
 }
 
-PassArgs base_args(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
-                   const SolverScratch& s, int pass) {
+PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs,
+                   int n, const SolverScratch& s, int pass) {
   PassArgs a = {};
   a.c = c;
+  a.G = G;
   a.X = X;
   a.cs = cs;
   a.n = n;
@@ -433,22 +440,22 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
   return cudaGetLastError();
 }
 
-cudaError_t launch_lambda(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+cudaError_t launch_lambda(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                           const SolverScratch& s, int pass, cudaStream_t stream) {
-  return run_pass<kLambda>(base_args(c, X, cs, n, s, pass), stream);
+  return run_pass<kLambda>(base_args(c, G, X, cs, n, s, pass), stream);
 }
 
-cudaError_t launch_delta_p(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+cudaError_t launch_delta_p(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                            const SolverScratch& s, int pass, float4* T, cudaStream_t stream) {
-  PassArgs a = base_args(c, X, cs, n, s, pass);
+  PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.T = T;
   return run_pass<kDeltaP>(a, stream);
 }
 
-cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const uint32_t* cs, int n,
+cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                                  const SolverScratch& s, int pass, float4* pos, float4* npos,
                                  float4* vel, uint32_t* iid, cudaStream_t stream) {
-  PassArgs a = base_args(c, X, cs, n, s, pass);
+  PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.xs = s.xs;
   a.iid_s = s.iid_s;
   a.npos = npos;
@@ -458,9 +465,9 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const float4* X, const uin
   return run_pass<kDeltaPFinal>(a, stream);
 }
 
-cudaError_t launch_xsph(const StepConsts& c, const float4* X, const float4* V, const uint32_t* cs,
+cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X, const float4* V, const uint32_t* cs,
                         int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream) {
-  PassArgs a = base_args(c, X, cs, n, s, pass);
+  PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.V = V;
   a.NV = NV;
   return run_pass<kXsph>(a, stream);

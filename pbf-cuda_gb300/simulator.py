@@ -199,9 +199,71 @@ class ParticleState:
     def vel(self) -> torch.Tensor:
         return (self.b_vel if self.tictoc else self.a_vel)[: self.n]
 
-    def step(self, sim: Simulator, stream=None) -> None:
+    def step(self, sim, stream=None) -> None:
+        """One step with a Simulator, or with an Ensemble over all its scenes."""
         if not self.tictoc:
-            sim.step(self.a_pos, self.b_pos, self.a_vel, self.b_vel, self.iid, self.n, stream)
+            src = (self.a_pos, self.b_pos, self.a_vel, self.b_vel)
         else:
-            sim.step(self.b_pos, self.a_pos, self.b_vel, self.a_vel, self.iid, self.n, stream)
+            src = (self.b_pos, self.a_pos, self.b_vel, self.a_vel)
+        if isinstance(sim, Ensemble):
+            sim.step(src[0], src[1], src[2], src[3], self.iid, stream)
+        else:
+            sim.step(src[0], src[1], src[2], src[3], self.iid, self.n, stream)
         self.tictoc = not self.tictoc
+
+
+class Ensemble:
+    """Many independent scenes advanced together (pbf_batch_* of the C ABI).
+
+    Scene s owns particle slots [offsets[s], offsets[s] + counts[s]) of every
+    buffer; each scene follows Simulator.step's contract inside its range.
+    """
+
+    def __init__(self, params: PbfParams, ulims, llims, counts):
+        self._L = lib()
+        self.nscenes = len(counts)
+        u = (ctypes.c_float * (3 * self.nscenes))(*[float(x) for v in ulims for x in v])
+        l = (ctypes.c_float * (3 * self.nscenes))(*[float(x) for v in llims for x in v])
+        cnt = (ctypes.c_int * self.nscenes)(*[int(c) for c in counts])
+        self._h = ctypes.c_void_p()
+        check(self._L.pbf_batch_create(ctypes.byref(params), self.nscenes, u, l, cnt, ctypes.byref(self._h)),
+              "pbf_batch_create")
+        self.counts = [int(c) for c in counts]
+        self.n = sum(self.counts)
+        self.offsets = [sum(self.counts[:k]) for k in range(self.nscenes)]
+
+    def step(self, pos, npos, vel, nvel, iid, stream=None) -> None:
+        for t, name, cols in ((pos, "pos", 4), (npos, "npos", 4), (vel, "vel", 4), (nvel, "nvel", 4),
+                              (iid, "iid", None)):
+            _check_state(t, name, self.n, cols)
+        check(self._L.pbf_batch_step(self._h, pos.data_ptr(), npos.data_ptr(), vel.data_ptr(), nvel.data_ptr(),
+                                     iid.data_ptr(), _stream_handle(stream)), "pbf_batch_step")
+
+    def setLim(self, scene: int, ulim: Sequence[float], llim: Sequence[float]) -> None:
+        check(self._L.pbf_batch_set_limits(self._h, int(scene), _vec3(ulim), _vec3(llim)), "pbf_batch_set_limits")
+
+    def density(self, stream=None) -> torch.Tensor:
+        out = torch.empty(max(self.n, 1), dtype=torch.float32, device="cuda")
+        check(self._L.pbf_batch_get_density(self._h, out.data_ptr(), _stream_handle(stream)),
+              "pbf_batch_get_density")
+        return out[: self.n]
+
+    def use_graphs(self, on: bool = True) -> None:
+        check(self._L.pbf_batch_use_graphs(self._h, int(bool(on))), "pbf_batch_use_graphs")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            check(self._L.pbf_batch_destroy(self._h), "pbf_batch_destroy")
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
