@@ -206,7 +206,7 @@ void free_all(pbf_solver* s) {
   void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
                   s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
                   s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
-                  s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense};
+                  s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense, s->sol.masks};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -307,6 +307,8 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.rho, np);
   if (e == cudaSuccess) e = alloc(&s->sol.flags, (size_t)pbf::kNumFlags);
   if (e == cudaSuccess) e = alloc(&s->sol.dense, pbf::dense_list_len(max_particles));
+  if (e == cudaSuccess) e = alloc(&s->sol.masks, (size_t)pbf::kMaskWords * np);
+  s->sol.mask_stride = (int)np;
   if (e == cudaSuccess) s->num_sms = current_sms();
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
   s->use_graph = true;
@@ -668,7 +670,8 @@ void batch_free(pbf_batch* b) {
   void* ptrs[] = {b->grid.keys_a, b->grid.keys_b, b->grid.vals_a, b->grid.vals_b,
                   b->grid.cell_count, b->grid.cell_start, b->grid.radix_counts,
                   b->grid.scan_partials, b->sol.xs, b->sol.xa, b->sol.xb, b->sol.iid_s,
-                  b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->d_geom, b->d_sid};
+                  b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->sol.masks,
+                  b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -750,6 +753,8 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
   if (e == cudaSuccess) e = alloc(&b->sol.rho, np);
   if (e == cudaSuccess) e = alloc(&b->sol.flags, (size_t)pbf::kNumFlags);
   if (e == cudaSuccess) e = alloc(&b->sol.dense, pbf::dense_list_len((int)np));
+  if (e == cudaSuccess) e = alloc(&b->sol.masks, (size_t)pbf::kMaskWords * np);
+  b->sol.mask_stride = (int)np;
   if (e == cudaSuccess) e = alloc(&b->d_geom, (size_t)nscenes);
   if (e == cudaSuccess) e = alloc(&b->d_sid, np);
   if (e == cudaSuccess) {

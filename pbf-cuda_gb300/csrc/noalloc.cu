@@ -9,7 +9,7 @@
 // pbf_create allocates the solver's scratch.
 //
 // How: the scratch lives in one file-scope __device__ array of fixed size,
-// kNoAllocScratchBytes (about 3.6 MB), which is part of this library's device
+// kNoAllocScratchBytes (about 5.7 MB), which is part of this library's device
 // image: every GPU that loads the library holds it until the process exits.
 // It bounds the problem to kNoAllocMaxParticles particles and
 // kNoAllocMaxCells grid cells; larger calls are rejected with
@@ -69,7 +69,8 @@ constexpr size_t kOffLambda = kOffIid + align_up(4 * kNp);
 constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
 constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
 constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
-constexpr size_t kNoAllocScratchBytes = kOffDense + align_up(4 * (kNp / 32 + 1));
+constexpr size_t kOffMasks = kOffDense + align_up(4 * (kNp / 32 + 1));
+constexpr size_t kNoAllocScratchBytes = kOffMasks + align_up(4 * (size_t)pbf::kMaskWords * kNp);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -129,6 +130,8 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.rho = (float*)(base + kOffRho);
   s.flags = (uint32_t*)(base + kOffFlags);
   s.dense = (uint32_t*)(base + kOffDense);
+  s.masks = (uint32_t*)(base + kOffMasks);
+  s.mask_stride = kNoAllocMaxParticles;
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;

@@ -161,7 +161,13 @@ struct SolverScratch {
   float* rho;
   uint32_t* flags;     // [kNumFlags] per-step flags and dense-list counters, zeroed by reorder
   uint32_t* dense;     // [dense_list_len(max_particles)] warps handed to the dense kernels
+  uint32_t* masks;     // [kMaskWords][mask_stride] the lambda pass's neighbour masks
+  int mask_stride;     // >= particles
 };
+
+// Neighbour masks a particle keeps between the lambda and delta_p passes of
+// one iteration: one 32-bit mask per chunk of 32 consecutive candidates.
+constexpr int kMaskWords = 16;
 
 // Words of SolverScratch::flags.  The two step flags are raised by a pass
 // when a later pass must take its exact (slow) path to reproduce the

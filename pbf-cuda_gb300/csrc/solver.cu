@@ -61,6 +61,8 @@ struct PassArgs {
   int next_counter;       // the other one, cleared for the next pass
   uint32_t* flags;
   uint32_t* dense;
+  uint32_t* masks;        // neighbour masks: lambda saves them, delta_p reads them
+  int mask_stride;
   float* lambda;          // lambda: out;  delta_p: in
   float* rho;             // lambda: out;  xsph: in
   float4* T;              // delta_p: out
@@ -103,6 +105,24 @@ __device__ __forceinline__ int window_total(const SceneGeom& g, const uint32_t* 
   return total;
 }
 
+// Chunks of 32 consecutive candidates the window splits into (per run).
+__device__ __forceinline__ int window_chunks(const SceneGeom& g, const uint32_t* __restrict__ cs,
+                                             int n, int3 q) {
+  int chunks = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      int s, e;
+      column_run(g, cs, n, x, y, q.z, s, e);
+      chunks += (e - s + 31) >> 5;
+    }
+  }
+  return chunks;
+}
+
 // Every candidate of the window, in order.
 template <class P>
 __device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t* __restrict__ cs,
@@ -116,6 +136,85 @@ __device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t*
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
       for (int j = s; j < e; ++j) p.visit(__ldg(X + j), j);
+    }
+  }
+}
+
+// Every candidate of the window, in order, in two stages per chunk of 32
+// consecutive slots of a run: a cheap test p.hit() of each candidate (four
+// loads in flight) into a bit mask, then p.visit() on the set bits in
+// ascending order.  p.visit() leaves non-hits untouched, so the result is that
+// of visit_window; the neighbour body runs max(hits) times per warp and chunk
+// instead of once per candidate.
+//
+// save_masks: store chunk k's mask at masks[k * stride + i] (k < kMaskWords)
+// for the next pass over the same positions.
+template <class P>
+__device__ __forceinline__ void visit_window_masked(const SceneGeom& g,
+                                                    const uint32_t* __restrict__ cs, int n,
+                                                    int3 q, const float4* __restrict__ X, P& p,
+                                                    uint32_t* __restrict__ masks, int stride,
+                                                    int i) {
+  int chunk = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      int s, e;
+      column_run(g, cs, n, x, y, q.z, s, e);
+      for (int j0 = s; j0 < e; j0 += 32) {
+        const int m = min(32, e - j0);
+        uint32_t mask = 0u;
+        int k = 0;
+        for (; k + 3 < m; k += 4) {
+          const float4 a = __ldg(X + j0 + k), b = __ldg(X + j0 + k + 1),
+                       c2 = __ldg(X + j0 + k + 2), d = __ldg(X + j0 + k + 3);
+          mask |= (uint32_t)p.hit(a, j0 + k) << k;
+          mask |= (uint32_t)p.hit(b, j0 + k + 1) << (k + 1);
+          mask |= (uint32_t)p.hit(c2, j0 + k + 2) << (k + 2);
+          mask |= (uint32_t)p.hit(d, j0 + k + 3) << (k + 3);
+        }
+        for (; k < m; ++k) mask |= (uint32_t)p.hit(__ldg(X + j0 + k), j0 + k) << k;
+        if (masks && chunk < kMaskWords) masks[chunk * stride + i] = mask;
+        ++chunk;
+        while (mask) {
+          const int b = __ffs(mask) - 1;
+          mask &= mask - 1u;
+          p.visit(__ldg(X + j0 + b), j0 + b);
+        }
+      }
+    }
+  }
+}
+
+// The window's neighbours from the masks a previous pass over the same
+// positions saved (visit_window_masked with save): p.visit() on the set bits,
+// in order.  The saved hits are a superset of p's (p.visit re-tests).
+template <class P>
+__device__ __forceinline__ void visit_window_saved(const SceneGeom& g,
+                                                   const uint32_t* __restrict__ cs, int n, int3 q,
+                                                   const float4* __restrict__ X, P& p,
+                                                   const uint32_t* __restrict__ masks, int stride,
+                                                   int i) {
+  int chunk = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      int s, e;
+      column_run(g, cs, n, x, y, q.z, s, e);
+      for (int j0 = s; j0 < e; j0 += 32, ++chunk) {
+        uint32_t mask = __ldg(masks + chunk * stride + i);
+        while (mask) {
+          const int b = __ffs(mask) - 1;
+          mask &= mask - 1u;
+          p.visit(__ldg(X + j0 + b), j0 + b);
+        }
+      }
     }
   }
 }
@@ -167,6 +266,9 @@ struct LambdaPass {
 
   __device__ LambdaPass(const PassArgs& a, const SceneGeom& g_, float4 xi_, int i_, bool)
       : c(a.c), g(g_), xi(xi_), i(i_) {}
+  __device__ __forceinline__ bool hit(float4 xj, int) const {
+    return !(dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) >= c.h2);
+  }
   __device__ __forceinline__ void visit(float4 xj, int j) {
     const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
     const float r2 = dist2(ex, ey, ez);
@@ -220,6 +322,10 @@ struct DeltaPPass {
 
   __device__ DeltaPPass(const PassArgs& a, const SceneGeom& g_, float4 xi_, int i_, bool exact_)
       : c(a.c), g(g_), lambda(a.lambda), xi(xi_), i(i_), li(a.lambda[i_]), exact(exact_) {}
+  __device__ __forceinline__ bool hit(float4 xj, int j) const {
+    const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
+    return !(r2 >= c.h2) && !(r2 < c.keps2) && j != i;
+  }
   __device__ __forceinline__ void visit(float4 xj, int j) {
     const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
     const float r2 = dist2(ex, ey, ez);
@@ -289,6 +395,9 @@ struct XsphPass {
 
   __device__ XsphPass(const PassArgs& a, const SceneGeom&, float4 xi_, int i_, bool exact_)
       : c(a.c), V(a.V), rho(a.rho), xi(xi_), vi(a.V[i_]), ri(a.rho[i_]), i(i_), exact(exact_) {}
+  __device__ __forceinline__ bool hit(float4 xj, int) const {
+    return !(dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) >= c.h2);
+  }
   __device__ __forceinline__ void visit(float4 xj, int j) {
     const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
     if (!(r2 >= c.h2)) {  // NaN-inclusive, as getPoly6
@@ -351,8 +460,18 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
     return;
   }
   if (!valid) return;
-  P p(a, g, xi, i, exact_path(kKind, a.flags));
-  visit_window(g, a.cs, a.n, q, a.X, p);
+  const bool exact = exact_path(kKind, a.flags);
+  P p(a, g, xi, i, exact);
+  if (exact) {
+    visit_window(g, a.cs, a.n, q, a.X, p);  // non-neighbours matter: visit every candidate
+  } else if (kKind == kLambda) {
+    visit_window_masked(g, a.cs, a.n, q, a.X, p, a.masks, a.mask_stride, i);  // saves its masks
+  } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) &&
+             window_chunks(g, a.cs, a.n, q) <= kMaskWords) {
+    visit_window_saved(g, a.cs, a.n, q, a.X, p, a.masks, a.mask_stride, i);  // lambda's masks
+  } else {
+    visit_window_masked(g, a.cs, a.n, q, a.X, p, nullptr, 0, i);
+  }
   p.finish(a);
 }
 
@@ -419,6 +538,8 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.next_counter = kDenseCount0 + ((pass + 1) & 1);
   a.flags = s.flags;
   a.dense = s.dense;
+  a.masks = s.masks;
+  a.mask_stride = s.mask_stride;
   a.lambda = s.lambda;
   a.rho = s.rho;
   return a;
