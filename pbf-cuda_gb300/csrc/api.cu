@@ -206,7 +206,8 @@ void free_all(pbf_solver* s) {
   void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
                   s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
                   s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
-                  s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense, s->sol.masks};
+                  s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense, s->sol.masks,
+                  s->sol.cell_flags};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -309,6 +310,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.dense, pbf::dense_list_len(max_particles));
   if (e == cudaSuccess) e = alloc(&s->sol.masks, (size_t)pbf::kMaskWords * np);
   s->sol.mask_stride = (int)np;
+  if (e == cudaSuccess) e = alloc(&s->sol.cell_flags, nc);
   if (e == cudaSuccess) s->num_sms = current_sms();
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
   s->use_graph = true;
@@ -407,6 +409,7 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
                            nullptr, st_),
            "pbf_step: grid");
   PBF_EV(P.ev[kEvGrid]);
+  P.sol->keys_sorted = P.grid->keys_sorted;
   PBF_CUDA(pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, *P.sol, st_),
            "pbf_step: reorder");
   PBF_EV(P.ev[kEvReorder]);
@@ -671,7 +674,7 @@ void batch_free(pbf_batch* b) {
                   b->grid.cell_count, b->grid.cell_start, b->grid.radix_counts,
                   b->grid.scan_partials, b->sol.xs, b->sol.xa, b->sol.xb, b->sol.iid_s,
                   b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->sol.masks,
-                  b->d_geom, b->d_sid};
+                  b->sol.cell_flags, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -755,6 +758,7 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
   if (e == cudaSuccess) e = alloc(&b->sol.dense, pbf::dense_list_len((int)np));
   if (e == cudaSuccess) e = alloc(&b->sol.masks, (size_t)pbf::kMaskWords * np);
   b->sol.mask_stride = (int)np;
+  if (e == cudaSuccess) e = alloc(&b->sol.cell_flags, nc);
   if (e == cudaSuccess) e = alloc(&b->d_geom, (size_t)nscenes);
   if (e == cudaSuccess) e = alloc(&b->d_sid, np);
   if (e == cudaSuccess) {

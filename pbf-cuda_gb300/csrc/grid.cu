@@ -298,13 +298,14 @@ cudaError_t build_grid(const StepConsts& c, const Geometry& G, const float4* pos
   uint32_t* vout = s.vals_a;
   for (int p = 0; p < passes; ++p) {
     const int shift = p * kRadixBits;
-    const bool last = p == passes - 1;
+    const bool last = p == passes - 1;  // its keys stay: the passes flag cells by them
     k_radix_upsweep<<<ntiles, kSortThreads, 0, stream>>>(kin, n, shift, s.radix_counts, ntiles);
     if ((err = exclusive_scan(s.radix_counts, s.radix_counts, clen, s.scan_partials, stream)) !=
         cudaSuccess)
       return err;
-    k_radix_downsweep<<<ntiles, kSortThreads, 0, stream>>>(
-        kin, vin, last ? nullptr : kout, vout, n, shift, s.radix_counts, ntiles);
+    k_radix_downsweep<<<ntiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n, shift,
+                                                           s.radix_counts, ntiles);
+    if (last) s.keys_sorted = kout;
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
     uint32_t* t = kin;
     kin = kout;

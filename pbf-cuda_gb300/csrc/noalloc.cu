@@ -9,7 +9,7 @@
 // pbf_create allocates the solver's scratch.
 //
 // How: the scratch lives in one file-scope __device__ array of fixed size,
-// kNoAllocScratchBytes (about 5.7 MB), which is part of this library's device
+// kNoAllocScratchBytes (about 6.2 MB), which is part of this library's device
 // image: every GPU that loads the library holds it until the process exits.
 // It bounds the problem to kNoAllocMaxParticles particles and
 // kNoAllocMaxCells grid cells; larger calls are rejected with
@@ -70,7 +70,8 @@ constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
 constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
 constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
 constexpr size_t kOffMasks = kOffDense + align_up(4 * (kNp / 32 + 1));
-constexpr size_t kNoAllocScratchBytes = kOffMasks + align_up(4 * (size_t)pbf::kMaskWords * kNp);
+constexpr size_t kOffCellFlags = kOffMasks + align_up(4 * (size_t)pbf::kMaskWords * kNp);
+constexpr size_t kNoAllocScratchBytes = kOffCellFlags + align_up(4 * kNc);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -132,6 +133,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.dense = (uint32_t*)(base + kOffDense);
   s.masks = (uint32_t*)(base + kOffMasks);
   s.mask_stride = kNoAllocMaxParticles;
+  s.cell_flags = (uint32_t*)(base + kOffCellFlags);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;
@@ -141,6 +143,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   if ((e = pbf::build_grid(c, G, (const float4*)pos, (const float4*)vel, nullptr, n, g, &perm, nullptr,
                            strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: grid");
+  s.keys_sorted = g.keys_sorted;
   if ((e = pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, s, strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: reorder");
   const int niter = params->niter;

@@ -127,6 +127,7 @@ struct GridScratch {
   uint32_t* cell_start; // [max_cells + 1]  exclusive prefix of cell counts
   uint32_t* radix_counts;   // [256 * max_sort_tiles]
   uint32_t* scan_partials;  // [kMaxScanPartials]
+  const uint32_t* keys_sorted;  // set by build_grid: cell id of each sorted slot (inside keys_a/b)
 };
 
 constexpr int kScanTile = 2048;
@@ -163,6 +164,18 @@ struct SolverScratch {
   uint32_t* dense;     // [dense_list_len(max_particles)] warps handed to the dense kernels
   uint32_t* masks;     // [kMaskWords][mask_stride] the lambda pass's neighbour masks
   int mask_stride;     // >= particles
+  uint32_t* cell_flags;         // [max_cells + 1] CellFlag bits per cell, zeroed by reorder
+  const uint32_t* keys_sorted;  // the grid's sorted cell ids (set before the passes)
+};
+
+// Bits of SolverScratch::cell_flags: the stale cell of a particle whose
+// value can poison a neighbour's sum the way the reference's IEEE arithmetic
+// does.  A particle takes the per-candidate exact path only when its own
+// values or a flagged cell of its window call for it.
+enum CellFlag : uint32_t {
+  kCellLambdaNonFinite = 1u,
+  kCellRhoNotPositive = 2u,  // rho <= 0 or NaN
+  kCellVelNonFinite = 4u,
 };
 
 // Neighbour masks a particle keeps between the lambda and delta_p passes of

@@ -63,6 +63,8 @@ struct PassArgs {
   uint32_t* dense;
   uint32_t* masks;        // neighbour masks: lambda saves them, delta_p reads them
   int mask_stride;
+  uint32_t* cell_flags;   // CellFlag bits per cell
+  const uint32_t* skeys;  // stale cell of each sorted slot
   float* lambda;          // lambda: out;  delta_p: in
   float* rho;             // lambda: out;  xsph: in
   float4* T;              // delta_p: out
@@ -103,6 +105,25 @@ __device__ __forceinline__ int window_total(const SceneGeom& g, const uint32_t* 
     }
   }
   return total;
+}
+
+// Whether a cell of the window carries any of `bits`.
+__device__ __forceinline__ bool window_flagged(const SceneGeom& g,
+                                               const uint32_t* __restrict__ cell_flags, int3 q,
+                                               uint32_t bits) {
+  const int zlo = max(q.z - 1, 0), zhi = min(q.z + 1, g.dims[2] - 1);
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      const int base = g.cell_base + (x * g.dims[1] + y) * g.dims[2];
+      for (int z = zlo; z <= zhi; ++z)
+        if (cell_flags[base + z] & bits) return true;
+    }
+  }
+  return false;
 }
 
 // Chunks of 32 consecutive candidates the window splits into (per run).
@@ -299,8 +320,13 @@ struct LambdaPass {
     const float lam = -(rho / c.pho0 - 1.f) / (grad_l2 + c.lambda_eps);
     a.lambda[i] = lam;
     a.rho[i] = rho;
-    if (!isfinite(lam)) atomicOr(&a.flags[kFlagLambdaNonFinite], 1u);
-    if (!(rho > 0.f) || !isfinite(rho)) atomicOr(&a.flags[kFlagXsphExact], 1u);
+    const uint32_t bits = (isfinite(lam) ? 0u : (uint32_t)kCellLambdaNonFinite) |
+                          (rho > 0.f && isfinite(rho) ? 0u : (uint32_t)kCellRhoNotPositive);
+    if (bits) {
+      atomicOr(&a.cell_flags[a.skeys[i]], bits);
+      if (bits & kCellLambdaNonFinite) atomicOr(&a.flags[kFlagLambdaNonFinite], 1u);
+      if (bits & kCellRhoNotPositive) atomicOr(&a.flags[kFlagXsphExact], 1u);
+    }
   }
 };
 
@@ -372,8 +398,10 @@ struct DeltaPPass {
     const float4 v = make_float4((xf.x - x0.x) * c.inv_dt, (xf.y - x0.y) * c.inv_dt,
                                  (xf.z - x0.z) * c.inv_dt, 0.f);
     a.vel[i] = v;
-    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z))
+    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z)) {
+      atomicOr(&a.cell_flags[a.skeys[i]], (uint32_t)kCellVelNonFinite);
       atomicOr(&a.flags[kFlagXsphExact], 1u);
+    }
     a.pos[i] = x0;
     a.iid[i] = a.iid_s[i];
   }
@@ -438,9 +466,23 @@ template <> struct PassOf<kDeltaP> { using type = DeltaPPass<false>; };
 template <> struct PassOf<kDeltaPFinal> { using type = DeltaPPass<true>; };
 template <> struct PassOf<kXsph> { using type = XsphPass; };
 
-__device__ __forceinline__ bool exact_path(int kind, const uint32_t* flags) {
-  if (kind == kDeltaP || kind == kDeltaPFinal) return flags[kFlagLambdaNonFinite] != 0u;
-  if (kind == kXsph) return flags[kFlagXsphExact] != 0u;
+// Whether particle i must visit every candidate of its window to reproduce the
+// reference's IEEE poisoning (a strict superset of the particles whose sums
+// can be poisoned): only when the step raised the pass's flag and i's own
+// values or a flagged cell of its window could poison its sum.
+__device__ __forceinline__ bool exact_path(int kind, const PassArgs& a, const SceneGeom& g,
+                                           int3 q, int i) {
+  if (kind == kDeltaP || kind == kDeltaPFinal) {
+    if (a.flags[kFlagLambdaNonFinite] == 0u) return false;
+    return !isfinite(a.lambda[i]) || window_flagged(g, a.cell_flags, q, kCellLambdaNonFinite);
+  }
+  if (kind == kXsph) {
+    if (a.flags[kFlagXsphExact] == 0u) return false;
+    const float ri = a.rho[i];
+    const float4 vi = a.V[i];
+    return !(ri > 0.f && isfinite(ri)) || !isfinite(vi.x) || !isfinite(vi.y) || !isfinite(vi.z) ||
+           window_flagged(g, a.cell_flags, q, kCellRhoNotPositive | kCellVelNonFinite);
+  }
   return false;
 }
 
@@ -460,7 +502,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
     return;
   }
   if (!valid) return;
-  const bool exact = exact_path(kKind, a.flags);
+  const bool exact = exact_path(kKind, a, g, q, i);
   P p(a, g, xi, i, exact);
   if (exact) {
     visit_window(g, a.cs, a.n, q, a.X, p);  // non-neighbours matter: visit every candidate
@@ -483,13 +525,13 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
   const uint32_t count = a.flags[a.counter];  // written by this pass's sparse kernel
-  const bool exact = exact_path(kKind, a.flags);
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const int i = (int)a.dense[item] * 32 + lane;
     const bool valid = i < a.n;
     const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
     const int3 q = cell_of(a.c, g, xi);
+    const bool exact = valid && exact_path(kKind, a, g, q, i);
     if (valid) {
       const int total = window_total(g, a.cs, a.n, q);
       const int lo = (int)((long long)total * warp / kDenseWarps);
@@ -540,6 +582,8 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.dense = s.dense;
   a.masks = s.masks;
   a.mask_stride = s.mask_stride;
+  a.cell_flags = s.cell_flags;
+  a.skeys = s.keys_sorted;
   a.lambda = s.lambda;
   a.rho = s.rho;
   return a;
@@ -556,6 +600,8 @@ cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
 
 cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
                     const uint32_t* iid, int n, SolverScratch& s, cudaStream_t stream) {
+  const cudaError_t e = cudaMemsetAsync(s.cell_flags, 0, sizeof(uint32_t) * (c.cells + 1), stream);
+  if (e != cudaSuccess) return e;
   k_reorder<<<(n + 255) / 256, 256, 0, stream>>>(perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
                                                   s.flags);
   return cudaGetLastError();
