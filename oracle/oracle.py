@@ -79,6 +79,9 @@ def lib():
                 fn = getattr(L, f"oracle_predict_{tag}")
                 fn.argtypes = [ctypes.POINTER(OracleParams), rp, rp, ctypes.c_int, rp]
                 fn.restype = ctypes.c_int
+                fn = getattr(L, f"oracle_step_backward_{tag}")
+                fn.argtypes = [ctypes.POINTER(OracleParams), f3, f3, rp, rp, u32, ctypes.c_int, rp, rp, rp, rp, rp, rp]
+                fn.restype = ctypes.c_int
                 fn = getattr(L, f"oracle_threads_{tag}")
                 fn.argtypes = []
                 fn.restype = ctypes.c_int
@@ -175,3 +178,28 @@ def predict(params, pos, vel, prec: str = "f32"):
     if rc != 0:
         raise ValueError("oracle_predict rejected its arguments")
     return out
+
+
+def step_backward(params, ulim, llim, pos, vel, iid, g_npos, g_nvel, prec: str = "f64"):
+    """Reverse pass of one step: the exact transpose of oracle step (neighbour
+    sets and clamp states fixed).  g_npos/g_nvel: adjoints of the step's
+    outputs, in its output (cell) order.  Returns adjoints of the inputs pos
+    and vel (input order) and of the limits ulim, llim."""
+    dt, ct = _dtype(prec)
+    pos = np.ascontiguousarray(pos, dtype=dt)
+    vel = np.ascontiguousarray(vel, dtype=dt)
+    iid = np.ascontiguousarray(iid, dtype=np.uint32)
+    gn = np.ascontiguousarray(g_npos, dtype=dt)
+    gv = np.ascontiguousarray(g_nvel, dtype=dt)
+    n = pos.shape[0]
+    g_pos = np.zeros_like(pos)
+    g_vel = np.zeros_like(vel)
+    gu = np.zeros(3, dtype=dt)
+    gl = np.zeros(3, dtype=dt)
+    op = to_oracle_params(params)
+    fn = getattr(lib(), f"oracle_step_backward_{prec}")
+    rc = fn(ctypes.byref(op), _lim(ulim), _lim(llim), _ptr(pos, ct), _ptr(vel, ct), _ptr(iid, ctypes.c_uint32), n,
+            _ptr(gn, ct), _ptr(gv, ct), _ptr(g_pos, ct), _ptr(g_vel, ct), _ptr(gu, ct), _ptr(gl, ct))
+    if rc != 0:
+        raise ValueError(f"oracle_step_backward_{prec} rejected its arguments (rc={rc})")
+    return {"pos": g_pos, "vel": g_vel, "ulim": gu, "llim": gl}

@@ -537,3 +537,287 @@ int SFX(oracle_threads)(void) {
   return 1;
 #endif
 }
+
+/* ---- reverse pass of one step (adjoint) ------------------------------------------
+ *
+ * The reference has no adjoint; this is the exact transpose of the step above
+ * with the neighbour sets (windows, r < h, |r| >= KERNAL_EPS) and the clamp
+ * states held fixed, written as a scatter over the forward's own pairs.
+ * Kernels: W(q) = a (h^2 - q)^3, W'(q) = -3a (h^2 - q)^2 (q = |r|^2);
+ * spiky F(r) = phi(s) r with phi = b (h - s)^2 / s, s = |r|, whose Jacobian
+ * is J(r) = phi I + (phi'(s) / s) r r^T, phi' = -b (h - s)(h + s) / s^2.
+ * Not supported with k_boundaryDensity != 0 (returns 2).
+ */
+
+typedef struct {
+  real J[6]; /* symmetric 3x3: xx, yy, zz, xy, xz, yz */
+} sym3;
+
+static inline void spiky_jac(const consts* c, const real r[3], real s, sym3* out) {
+  real d = c->h - s;
+  real phi = c->spiky_coef * d * d / s;
+  real dphi = -c->spiky_coef * d * (c->h + s) / (s * s);
+  real k = dphi / s;
+  out->J[0] = phi + k * r[0] * r[0];
+  out->J[1] = phi + k * r[1] * r[1];
+  out->J[2] = phi + k * r[2] * r[2];
+  out->J[3] = k * r[0] * r[1];
+  out->J[4] = k * r[0] * r[2];
+  out->J[5] = k * r[1] * r[2];
+}
+
+static inline void sym3_mul(const sym3* m, const real v[3], real out[3]) {
+  out[0] = m->J[0] * v[0] + m->J[3] * v[1] + m->J[4] * v[2];
+  out[1] = m->J[3] * v[0] + m->J[1] * v[1] + m->J[5] * v[2];
+  out[2] = m->J[4] * v[0] + m->J[5] * v[1] + m->J[2] * v[2];
+}
+
+static inline real dpoly6(const consts* c, real q) { /* dW/dq inside the support */
+  real d = c->h2 - q;
+  return -3 * c->poly6_coef * d * d;
+}
+
+/* Visit the window pairs (i, j) of slot i at positions P (cell of P[i]). */
+#define FOR_WINDOW(c, cs, P, i, j)                                      \
+  for (int dx_ = -1, ind_[3] = {0, 0, 0}; dx_ <= 1; ++dx_)              \
+    if (dx_ == -1 ? (cell_xyz((c), (P) + 4 * (size_t)(i), ind_), 1) : 1) \
+      for (int dy_ = -1; dy_ <= 1; ++dy_)                               \
+        for (int s_ = 0, e_ = 0, ok_ = ((ind_[0] + dx_) >= 0 && (ind_[0] + dx_) < (c)->gd.dims[0] && \
+                                        (ind_[1] + dy_) >= 0 && (ind_[1] + dy_) < (c)->gd.dims[1]) \
+                                           ? (column_run((c), (cs), ind_[0] + dx_, ind_[1] + dy_, ind_[2], &s_, &e_), 1) \
+                                           : 0;                         \
+             ok_; ok_ = 0)                                              \
+          for (int j = s_; j < e_; ++j)
+
+int SFX(oracle_step_backward)(const pbf_params* p, const float ulim[3], const float llim[3],
+                              const real* pos_in, const real* vel_in, const uint32_t* iid_in, int n,
+                              const real* g_npos, const real* g_nvel, real* g_pos, real* g_vel,
+                              real* g_ulim, real* g_llim) {
+  if (!p || n < 0 || p->niter < 1) return 1;
+  if (p->k_boundaryDensity != 0.f) return 2;
+  for (int a = 0; a < 3; ++a) g_ulim[a] = g_llim[a] = 0;
+  if (n == 0) return 0;
+  (void)iid_in;
+  consts c;
+  make_consts(&c, p, ulim, llim);
+  const int K = p->niter;
+  const size_t n4 = 4 * (size_t)n;
+  const real dt = (real)p->dt, pho0 = (real)p->pho0, eps = (real)p->lambda_eps;
+  const real n_corr = (real)p->n_corr, cx = (real)p->c_XSPH;
+  real* S = (real*)malloc(sizeof(real) * n4);
+  real* X0 = (real*)malloc(sizeof(real) * n4); /* sorted input positions */
+  real* XK = (real*)malloc(sizeof(real) * n4 * (size_t)(K + 1)); /* X_0 .. X_K */
+  real* LAM = (real*)malloc(sizeof(real) * (size_t)n * (size_t)K);
+  real* RHO = (real*)malloc(sizeof(real) * (size_t)n * (size_t)K);
+  real* V = (real*)malloc(sizeof(real) * n4);
+  real* gX = (real*)calloc(n4, sizeof(real));    /* adjoint of the current X_k */
+  real* gXn = (real*)calloc(n4, sizeof(real));   /* adjoint of X_{k+1} */
+  real* gX0 = (real*)calloc(n4, sizeof(real));   /* adjoint of the sorted input positions */
+  real* gV = (real*)calloc(n4, sizeof(real));
+  real* gl = (real*)calloc((size_t)n, sizeof(real));
+  real* gr = (real*)calloc((size_t)n, sizeof(real));
+  real* Pb = (real*)calloc(n4, sizeof(real));
+  real* G = (real*)calloc(n4, sizeof(real));
+  real* Sbar = (real*)calloc((size_t)n, sizeof(real));
+  real* Rtot = (real*)calloc((size_t)n, sizeof(real));
+  uint32_t* keys = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t* perm = (uint32_t*)malloc(sizeof(uint32_t) * (size_t)n);
+  uint32_t* cs = (uint32_t*)calloc((size_t)c.gd.cells + 1, sizeof(uint32_t));
+
+  /* ---- forward, recorded ---- */
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      real v = RFMA(dt, c.g[a], vel_in[4 * (size_t)i + a]);
+      S[4 * (size_t)i + a] = RFMA(dt, v, pos_in[4 * (size_t)i + a]);
+    }
+  build_grid(&c, S, n, keys, perm, NULL, NULL);
+  for (int i = 0; i < n; ++i) cs[keys[i] + 1]++;
+  for (int k = 0; k < c.gd.cells; ++k) cs[k + 1] += cs[k];
+  for (int k = 0; k < n; ++k) {
+    memcpy(X0 + 4 * (size_t)k, pos_in + 4 * (size_t)perm[k], sizeof(real) * 4);
+    memcpy(XK + 4 * (size_t)k, S + 4 * (size_t)perm[k], sizeof(real) * 4);
+  }
+  for (int k = 0; k < K; ++k) {
+    lambda_pass(&c, p, XK + n4 * k, cs, n, LAM + (size_t)n * k, RHO + (size_t)n * k);
+    dp_pass(&c, p, XK + n4 * k, cs, n, LAM + (size_t)n * k, XK + n4 * (k + 1));
+  }
+  const real* XF = XK + n4 * K;
+  const real* rho = RHO + (size_t)n * (K - 1);
+  for (int k = 0; k < n; ++k)
+    for (int a = 0; a < 3; ++a) V[4 * (size_t)k + a] = (XF[4 * (size_t)k + a] - X0[4 * (size_t)k + a]) * c.inv_dt;
+
+  /* ---- XSPH: nv_i = v_i + c sum_j (v_j - v_i) w_ij, w = 2 W(q) / (rho_i + rho_j) ---- */
+  for (int i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) {
+      gV[4 * (size_t)i + a] += g_nvel[4 * (size_t)i + a];
+      gXn[4 * (size_t)i + a] = g_npos[4 * (size_t)i + a];
+    }
+  for (int i = 0; i < n; ++i) {
+    const real* xi = XF + 4 * (size_t)i;
+    const real* vi = V + 4 * (size_t)i;
+    const real* gn = g_nvel + 4 * (size_t)i;
+    FOR_WINDOW(&c, cs, XF, i, j) {
+      if (j == i) continue;
+      const real* xj = XF + 4 * (size_t)j;
+      const real* vj = V + 4 * (size_t)j;
+      real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+      real q = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+      if (q >= c.h2) continue;
+      real den = rho[i] + rho[j];
+      real w = 2 * poly6(&c, q) / den;
+      real wb = 0;
+      for (int a = 0; a < 3; ++a) {
+        gV[4 * (size_t)i + a] -= cx * w * gn[a];
+        gV[4 * (size_t)j + a] += cx * w * gn[a];
+        wb += cx * gn[a] * (vj[a] - vi[a]);
+      }
+      real gq = wb * 2 * dpoly6(&c, q) / den;
+      for (int a = 0; a < 3; ++a) {
+        gXn[4 * (size_t)i + a] += gq * 2 * r[a];
+        gXn[4 * (size_t)j + a] -= gq * 2 * r[a];
+      }
+      real grho = wb * (-2 * poly6(&c, q) / (den * den));
+      gr[i] += grho;
+      gr[j] += grho;
+    }
+  }
+  /* ---- v = (X_K - X0) / dt ---- */
+  for (int k = 0; k < n; ++k)
+    for (int a = 0; a < 3; ++a) {
+      gXn[4 * (size_t)k + a] += gV[4 * (size_t)k + a] * c.inv_dt;
+      gX0[4 * (size_t)k + a] -= gV[4 * (size_t)k + a] * c.inv_dt;
+    }
+
+  /* ---- iterations, last to first ---- */
+  for (int k = K - 1; k >= 0; --k) {
+    const real* X = XK + n4 * k;
+    const real* lam = LAM + (size_t)n * k;
+    const real* rk = RHO + (size_t)n * k;
+    memset(gX, 0, sizeof(real) * n4);
+    memset(gl, 0, sizeof(real) * (size_t)n);
+    /* delta_p and its clamps: X_{k+1} = box(X_k + clamp(P / pho0)) */
+    for (int i = 0; i < n; ++i) {
+      const real* xi = X + 4 * (size_t)i;
+      real P[3] = {0, 0, 0};
+      FOR_WINDOW(&c, cs, X, i, j) {
+        if (j == i) continue;
+        const real* xj = X + 4 * (size_t)j;
+        real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+        real corr = c.coef_corr * RPOW(poly6(&c, r[0] * r[0] + r[1] * r[1] + r[2] * r[2]), n_corr);
+        real f[3];
+        spiky(&c, r, f);
+        for (int a = 0; a < 3; ++a) P[a] += (lam[i] + lam[j] + corr) * f[a];
+      }
+      for (int a = 0; a < 3; ++a) {
+        real dpa = P[a] / pho0;
+        real d = RMAX(RMIN(dpa, c.max_dp), -c.max_dp);
+        real u = xi[a] + d;
+        real gu;
+        if (u > c.hi[a]) {
+          g_ulim[a] += gXn[4 * (size_t)i + a];
+          gu = 0;
+        } else if (u < c.lo[a]) {
+          g_llim[a] += gXn[4 * (size_t)i + a];
+          gu = 0;
+        } else {
+          gu = gXn[4 * (size_t)i + a];
+        }
+        gX[4 * (size_t)i + a] += gu;
+        Pb[4 * (size_t)i + a] = (dpa < c.max_dp && dpa > -c.max_dp) ? gu / pho0 : 0;
+      }
+    }
+    for (int i = 0; i < n; ++i) {
+      const real* xi = X + 4 * (size_t)i;
+      const real* pb = Pb + 4 * (size_t)i;
+      FOR_WINDOW(&c, cs, X, i, j) {
+        if (j == i) continue;
+        const real* xj = X + 4 * (size_t)j;
+        real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+        real q = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        real s = RSQRT(q);
+        if (s >= c.h || (double)s < c.kernel_eps) continue;
+        real wq = poly6(&c, q);
+        real corr = c.coef_corr * RPOW(wq, n_corr);
+        real f[3];
+        spiky(&c, r, f);
+        real fp = f[0] * pb[0] + f[1] * pb[1] + f[2] * pb[2];
+        gl[i] += fp;
+        gl[j] += fp;
+        sym3 Jm;
+        spiky_jac(&c, r, s, &Jm);
+        real jp[3];
+        sym3_mul(&Jm, pb, jp);
+        real ds = 2 * c.coef_corr * n_corr * RPOW(wq, n_corr - 1) * dpoly6(&c, q);
+        real lsum = lam[i] + lam[j] + corr;
+        for (int a = 0; a < 3; ++a) {
+          real m = lsum * jp[a] + ds * r[a] * fp;
+          gX[4 * (size_t)i + a] += m;
+          gX[4 * (size_t)j + a] -= m;
+        }
+      }
+    }
+    /* lambda: lambda_i = -(rho_i / pho0 - 1) / (S_i + eps) */
+    for (int i = 0; i < n; ++i) {
+      const real* xi = X + 4 * (size_t)i;
+      real gi[3] = {0, 0, 0}, gj2 = 0;
+      FOR_WINDOW(&c, cs, X, i, j) {
+        const real* xj = X + 4 * (size_t)j;
+        real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+        real f[3];
+        spiky(&c, r, f);
+        for (int a = 0; a < 3; ++a) gi[a] += f[a] / pho0;
+        if (j != i) gj2 += (f[0] * f[0] + f[1] * f[1] + f[2] * f[2]) / (pho0 * pho0);
+      }
+      real Sv = gj2 + gi[0] * gi[0] + gi[1] * gi[1] + gi[2] * gi[2];
+      real D = Sv + eps;
+      real Cb = -gl[i] / D;
+      Sbar[i] = -gl[i] * lam[i] / D;
+      Rtot[i] = (k == K - 1 ? gr[i] : 0) + Cb / pho0;
+      memcpy(G + 4 * (size_t)i, gi, sizeof(real) * 3);
+      (void)rk;
+    }
+    for (int i = 0; i < n; ++i) {
+      const real* xi = X + 4 * (size_t)i;
+      FOR_WINDOW(&c, cs, X, i, j) {
+        if (j == i) continue;
+        const real* xj = X + 4 * (size_t)j;
+        real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+        real q = r[0] * r[0] + r[1] * r[1] + r[2] * r[2];
+        if (q >= c.h2) continue;
+        real dw = dpoly6(&c, q);
+        for (int a = 0; a < 3; ++a) {
+          gX[4 * (size_t)i + a] += Rtot[i] * dw * 2 * r[a];
+          gX[4 * (size_t)j + a] -= Rtot[i] * dw * 2 * r[a];
+        }
+        real s = RSQRT(q);
+        if (s >= c.h || (double)s < c.kernel_eps) continue;
+        real f[3];
+        spiky(&c, r, f);
+        real av[3];
+        for (int a = 0; a < 3; ++a) av[a] = Sbar[i] * (2 * f[a] / pho0 + 2 * G[4 * (size_t)i + a]);
+        sym3 Jm;
+        spiky_jac(&c, r, s, &Jm);
+        real ja[3];
+        sym3_mul(&Jm, av, ja);
+        for (int a = 0; a < 3; ++a) {
+          gX[4 * (size_t)i + a] += ja[a] / pho0;
+          gX[4 * (size_t)j + a] -= ja[a] / pho0;
+        }
+      }
+    }
+    memcpy(gXn, gX, sizeof(real) * n4); /* becomes the adjoint of X_k */
+  }
+  /* ---- x* = x + dt v + dt^2 g, then un-permute ---- */
+  for (int k = 0; k < n; ++k) {
+    const uint32_t q = perm[k];
+    for (int a = 0; a < 3; ++a) {
+      g_pos[4 * (size_t)q + a] = gXn[4 * (size_t)k + a] + gX0[4 * (size_t)k + a];
+      g_vel[4 * (size_t)q + a] = dt * gXn[4 * (size_t)k + a];
+    }
+    g_pos[4 * (size_t)q + 3] = 0;
+    g_vel[4 * (size_t)q + 3] = 0;
+  }
+  free(S); free(X0); free(XK); free(LAM); free(RHO); free(V); free(gX); free(gXn); free(gX0);
+  free(gV); free(gl); free(gr); free(Pb); free(G); free(Sbar); free(Rtot); free(keys); free(perm); free(cs);
+  return 0;
+}
