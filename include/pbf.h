@@ -168,6 +168,38 @@ pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out);
 pbf_status pbf_use_graphs(pbf_solver* s, int on);
 
 /*
+ * Reverse pass (adjoint) of a step, for differentiating through the solver.
+ * No counterpart in the reference.  With the tape on, every pbf_step also
+ * records what its reverse pass needs (positions entering each solver
+ * iteration, each iteration's lambda; about (niter + 1) * 16 + niter * 4
+ * bytes per particle, allocated here once).  pbf_backward then takes the
+ * adjoints of the last step's outputs npos and nvel (device, n float4, the
+ * step's output cell order) and writes the adjoints of its inputs pos and vel
+ * (device, n float4, the step's input order) and of the box limits (g_lim:
+ * device, 6 floats: ulim xyz then llim xyz, through the wall clamp).  The
+ * neighbour sets and clamp states of the forward are held fixed; states must
+ * be finite and k_boundaryDensity 0.  A multi-step rollout is differentiated
+ * by re-running each step with the tape on (from a saved input state) just
+ * before its reverse pass.
+ */
+pbf_status pbf_tape_enable(pbf_solver* s, int on);
+pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, void* g_pos,
+                        void* g_vel, float* g_lim, void* stream);
+
+/*
+ * Poly6 density (mass 1, radius h) of n particles (device float4) at the
+ * centres of a dims[0] x dims[1] x dims[2] lattice of cells spanning
+ * [lo, hi] (device grid, x slowest), and the adjoint of that map: g_grid
+ * (device, one float per node) -> g_pos (device, n float4).  Both are
+ * gathers.  The loss of the inverse problem; no counterpart in the reference.
+ */
+pbf_status pbf_density_grid(const void* pos, int n, const float lo[3], const float hi[3],
+                            const int dims[3], float h, float* grid, void* stream);
+pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], const float hi[3],
+                                     const int dims[3], float h, const float* g_grid, void* g_pos,
+                                     void* stream);
+
+/*
  * Batched ensemble: many independent scenes of uneven particle counts, each
  * with its own box, advanced together, one launch per pass for all scenes.
  * No counterpart in the reference (one Simulator per scene there).

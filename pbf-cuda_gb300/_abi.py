@@ -37,6 +37,10 @@ EXPORTED = (
     "pbf_profile_enable",
     "pbf_profile_read",
     "pbf_use_graphs",
+    "pbf_tape_enable",
+    "pbf_backward",
+    "pbf_density_grid",
+    "pbf_density_grid_backward",
     "pbf_batch_create",
     "pbf_batch_destroy",
     "pbf_batch_set_limits",
@@ -138,6 +142,11 @@ def _declare(L) -> None:
         "pbf_profile_enable": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_profile_read": (ctypes.c_int, [vp, P(PbfStepProfile)]),
         "pbf_use_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pbf_tape_enable": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pbf_backward": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
+        "pbf_density_grid": (ctypes.c_int, [vp, ctypes.c_int, f3, f3, P(ctypes.c_int), ctypes.c_float, vp, vp]),
+        "pbf_density_grid_backward": (ctypes.c_int, [vp, ctypes.c_int, f3, f3, P(ctypes.c_int), ctypes.c_float, vp,
+                                                     vp, vp]),
         "pbf_batch_create": (ctypes.c_int, [P(PbfParams), ctypes.c_int, f3, f3, P(ctypes.c_int), P(vp)]),
         "pbf_batch_destroy": (ctypes.c_int, [vp]),
         "pbf_batch_set_limits": (ctypes.c_int, [vp, ctypes.c_int, f3, f3]),

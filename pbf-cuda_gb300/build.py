@@ -22,7 +22,7 @@ CSRC = HERE / "csrc"
 BUILD_DIR = HERE / "_build"
 LIB_DIR = HERE / "lib"
 LIB = LIB_DIR / "libpbf.so"
-SOURCES = ["api.cu", "grid.cu", "solver.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "grid.cu", "solver.cu", "adjoint.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     *ARCH,

@@ -43,6 +43,18 @@ struct pbf_solver {
   bool use_graph;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
+  // tape of the last step and the reverse pass's scratch (pbf_tape_enable)
+  bool tape;
+  bool tape_valid;
+  int tape_iters;            // iterations the tape buffers hold
+  float4* tape_x;            // (tape_iters + 1) * max_particles
+  float* tape_l;             // tape_iters * max_particles
+  float4* bw4;               // 7 * max_particles: gx, gx_next, gx0, pbar, gs, fix, fixv
+  float* bw1;                // 4 * max_particles: grho, lbar, rtot (+ spare)
+  unsigned long long* bw8;   // 2 * max_particles: packed grid cells, packed current cells
+  float* wall_part;          // 6 * blocks
+  pbf::StepConsts last_c;
+  const uint32_t* last_perm;
 };
 
 namespace {
@@ -216,6 +228,9 @@ void free_all(pbf_solver* s) {
     if (e) cudaEventDestroy(e);
   if (s->exec) cudaGraphExecDestroy(s->exec);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+  void* tape[] = {s->tape_x, s->tape_l, s->bw4, s->bw1, s->bw8, s->wall_part};
+  for (void* p : tape)
+    if (p) cudaFree(p);
 }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
@@ -388,6 +403,10 @@ struct StepPlan {
   int niter;
   cudaEvent_t* ev;     // [kEvFixed] or null
   cudaEvent_t* ev_it;  // [3 * kMaxProfiledIters] or null
+  float4* tape_x;      // record the step for its reverse pass (null: do not)
+  float* tape_l;
+  int tape_stride;     // particles per tape slot
+  const uint32_t** perm_out;  // receives the step's sort permutation
 };
 
 // Enqueues one step on stream st_ (a capturing stream when building the graph).
@@ -409,10 +428,15 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
                            nullptr, st_),
            "pbf_step: grid");
   PBF_EV(P.ev[kEvGrid]);
+  if (P.perm_out) *P.perm_out = perm;
   P.sol->keys_sorted = P.grid->keys_sorted;
   PBF_CUDA(pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, *P.sol, st_),
            "pbf_step: reorder");
   PBF_EV(P.ev[kEvReorder]);
+  const size_t ts = (size_t)P.tape_stride;
+#define PBF_TAPE(dst, src, bytes) \
+  if (P.tape_x) PBF_CUDA(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st_), "pbf_step: tape")
+  PBF_TAPE(P.tape_x, P.sol->xa, sizeof(float4) * n);
   // niter x correctDensity (fluids/Simulator.cpp:55-60), Jacobi ping-pong;
   // updateVelocity fused into the last position update (fluids/Simulator.cpp:62-66)
   const uint32_t* cs = P.grid->cell_start;
@@ -422,9 +446,11 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
   for (int it = 0; it < niter; ++it) {
     if (it < piters) PBF_EV(P.ev_it[3 * it]);
     PBF_CUDA(pbf::launch_lambda(c, G, X, cs, n, sol, 2 * it, st_), "pbf_step: lambda");
+    PBF_TAPE(P.tape_l + ts * it, sol.lambda, sizeof(float) * n);
     if (it < piters) PBF_EV(P.ev_it[3 * it + 1]);
     if (it + 1 < niter) {
       PBF_CUDA(pbf::launch_delta_p(c, G, X, cs, n, sol, 2 * it + 1, T, st_), "pbf_step: delta_p");
+      PBF_TAPE(P.tape_x + ts * (it + 1), T, sizeof(float4) * n);
       float4* t = X;
       X = T;
       T = t;
@@ -432,6 +458,7 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
       PBF_CUDA(pbf::launch_delta_p_final(c, G, X, cs, n, sol, 2 * it + 1, (float4*)pos,
                                          (float4*)npos, (float4*)vel, iid, st_),
                "pbf_step: delta_p");
+      PBF_TAPE(P.tape_x + ts * (it + 1), npos, sizeof(float4) * n);
     }
     if (it < piters) PBF_EV(P.ev_it[3 * it + 2]);
   }
@@ -442,6 +469,7 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
            "pbf_step: xsph");
   PBF_EV(P.ev[kEvEnd]);
 #undef PBF_EV
+#undef PBF_TAPE
   return PBF_OK;
 }
 
@@ -515,6 +543,15 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   P.niter = s->params.niter;
   P.ev = prof ? s->ev : nullptr;
   P.ev_it = prof ? s->ev_it : nullptr;
+  const bool taping = s->tape && s->params.niter <= s->tape_iters;
+  if (s->tape && !taping)
+    return fail(PBF_ERR_CAPACITY, "tape holds %d iterations, params ask for %d (re-enable the tape)",
+                s->tape_iters, s->params.niter);
+  P.tape_x = taping ? s->tape_x : nullptr;
+  P.tape_l = taping ? s->tape_l : nullptr;
+  P.tape_stride = s->max_particles;
+  P.perm_out = &s->last_perm;
+  s->tape_valid = false;
   const pbf::StepConsts& c = P.c;
   st = s->use_graph ? launch_step_graph(P, s->cap_stream, &s->exec, pos, npos, vel, nvel, iid, n, st_)
                     : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
@@ -524,6 +561,87 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
+  s->last_c = c;
+  s->tape_valid = taping;
+  return PBF_OK;
+}
+
+pbf_status pbf_tape_enable(pbf_solver* s, int on) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (!on) {
+    s->tape = false;
+    return PBF_OK;
+  }
+  if (s->params.k_boundaryDensity != 0.f)
+    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
+  s->tape = true;
+  const int iters = s->params.niter;
+  if (iters > pbf::kMaxTapeIters) return fail(PBF_ERR_CAPACITY, "at most %d taped iterations", pbf::kMaxTapeIters);
+  if (iters <= s->tape_iters) return PBF_OK;
+  void* old[] = {s->tape_x, s->tape_l, s->bw4, s->bw1, s->bw8, s->wall_part};
+  for (void* p : old)
+    if (p) cudaFree(p);
+  s->tape_x = nullptr;
+  s->tape_l = nullptr;
+  s->bw4 = nullptr;
+  s->bw1 = nullptr;
+  s->bw8 = nullptr;
+  s->wall_part = nullptr;
+  s->tape_iters = 0;
+  const size_t np = (size_t)(s->max_particles > 0 ? s->max_particles : 1);
+  const size_t blocks = (np + 127) / 128;
+  cudaError_t e = alloc(&s->tape_x, np * (iters + 1));
+  if (e == cudaSuccess) e = alloc(&s->tape_l, np * iters);
+  if (e == cudaSuccess) e = alloc(&s->bw4, np * 7);
+  if (e == cudaSuccess) e = alloc(&s->bw1, np * 4);
+  if (e == cudaSuccess) e = alloc(&s->bw8, np * 2);
+  if (e == cudaSuccess) e = cudaMemset(s->bw4 + 5 * np, 0, sizeof(float4) * 2 * np);
+  if (e == cudaSuccess) e = alloc(&s->wall_part, blocks * 6);
+  if (e != cudaSuccess) {
+    s->tape = false;
+    cudaGetLastError();
+    return cuda_fail(e, "pbf_tape_enable");
+  }
+  s->tape_iters = iters;
+  return PBF_OK;
+}
+
+pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, void* g_pos,
+                        void* g_vel, float* g_lim, void* stream) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (!s->tape_valid) return fail(PBF_ERR_NOT_READY, "the last step was not taped");
+  if (s->params.k_boundaryDensity != 0.f)
+    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
+  if (!g_npos || !g_nvel || !g_pos || !g_vel || !g_lim) return fail(PBF_ERR_INVALID_ARG, "NULL buffer");
+  const int n = s->last_n;
+  const size_t np = (size_t)s->max_particles;
+  pbf::BackwardArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.c = s->last_c;
+  a.G = pbf::Geometry{nullptr, nullptr};
+  a.cs = s->grid.cell_start;
+  a.n = n;
+  a.xs = s->sol.xs;
+  a.rho = s->sol.rho;
+  a.gx = s->bw4;
+  a.gx_next = s->bw4 + np;
+  a.gx0 = s->bw4 + 2 * np;
+  a.pbar = s->bw4 + 3 * np;
+  a.gs = s->bw4 + 4 * np;
+  a.grho = s->bw1;
+  a.lbar = s->bw1 + np;
+  a.rtot = s->bw1 + 2 * np;
+  a.fix = s->bw4 + 5 * np;
+  a.fixv = s->bw4 + 6 * np;
+  a.gcell = s->bw8;
+  a.kcell = s->bw8 + np;
+  a.wall_part = s->wall_part;
+  pbf::BackwardTape t;
+  t.niter = s->params.niter;
+  for (int k = 0; k <= t.niter; ++k) t.X[k] = s->tape_x + np * k;
+  for (int k = 0; k < t.niter; ++k) t.lambda[k] = s->tape_l + np * k;
+  PBF_CUDA(pbf::backward(a, t, s->last_perm, g_npos, g_nvel, g_pos, g_vel, g_lim, (cudaStream_t)stream),
+           "pbf_backward");
   return PBF_OK;
 }
 
@@ -838,6 +956,10 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   P.niter = b->params.niter;
   P.ev = nullptr;
   P.ev_it = nullptr;
+  P.tape_x = nullptr;
+  P.tape_l = nullptr;
+  P.tape_stride = 0;
+  P.perm_out = nullptr;
   st = b->use_graph ? launch_step_graph(P, b->cap_stream, &b->exec, pos, npos, vel, nvel, iid, n, st_)
                     : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
   if (st != PBF_OK) return st;
@@ -857,6 +979,36 @@ pbf_status pbf_batch_get_density(const pbf_batch* b, float* rho, void* stream) {
 pbf_status pbf_batch_use_graphs(pbf_batch* b, int on) {
   if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
   b->use_graph = on != 0;
+  return PBF_OK;
+}
+
+}  // extern "C"
+
+// ---- density grid (the inverse problem's loss) ---------------------------------------
+
+extern "C" {
+
+pbf_status pbf_density_grid(const void* pos, int n, const float lo[3], const float hi[3],
+                            const int dims[3], float h, float* grid, void* stream) {
+  if ((!pos && n > 0) || !lo || !hi || !dims || !grid || n < 0)
+    return fail(PBF_ERR_INVALID_ARG, "NULL argument or n < 0");
+  if (!(h > 0.f) || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
+    return fail(PBF_ERR_INVALID_ARG, "h must be > 0 and dims >= 1");
+  PBF_CUDA(pbf::density_grid((const float4*)pos, n, lo, hi, dims, h, grid, (cudaStream_t)stream),
+           "pbf_density_grid");
+  return PBF_OK;
+}
+
+pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], const float hi[3],
+                                     const int dims[3], float h, const float* g_grid, void* g_pos,
+                                     void* stream) {
+  if ((!pos && n > 0) || !lo || !hi || !dims || !g_grid || (!g_pos && n > 0) || n < 0)
+    return fail(PBF_ERR_INVALID_ARG, "NULL argument or n < 0");
+  if (!(h > 0.f) || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
+    return fail(PBF_ERR_INVALID_ARG, "h must be > 0 and dims >= 1");
+  PBF_CUDA(pbf::density_grid_backward((const float4*)pos, n, lo, hi, dims, h, g_grid, (float4*)g_pos,
+                                      (cudaStream_t)stream),
+           "pbf_density_grid_backward");
   return PBF_OK;
 }
 

@@ -223,6 +223,63 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
 // Kernel launches of one neighbour pass.
 constexpr int kLaunchesPerPass = 2;
 
+// ---- reverse pass (adjoint.cu) ------------------------------------------------------
+
+constexpr int kMaxTapeIters = 64;
+
+// What a taped step keeps for its reverse pass: the positions entering every
+// iteration and the final ones (X[0] = x*, X[niter] = npos), and every
+// iteration's lambda.  The grid, the sorted inputs and the last rho stay in
+// the solver's scratch until the next step.
+struct BackwardTape {
+  int niter;
+  float4* X[kMaxTapeIters + 1];
+  float* lambda[kMaxTapeIters];
+};
+
+struct BackwardArgs {
+  StepConsts c;
+  Geometry G;
+  const uint32_t* cs;
+  int n;
+  const float4* xs;      // sorted input positions
+  const float* rho;      // rho of the last lambda pass
+  const float4* XK;      // final positions (set by backward)
+  const float4* g_npos;  // adjoints of the outputs (set by backward)
+  const float4* g_nvel;
+  float4* gx;       // adjoint of the current positions
+  float4* gx_next;  // adjoint being built for the earlier positions
+  float4* gx0;      // velocity-update part of the sorted inputs' adjoint
+  float* grho;      // adjoint of the last rho (from XSPH)
+  float4* pbar;     // adjoint of the delta_p sums / pho0 ... / pho0
+  float* lbar;      // adjoint of lambda
+  float4* gs;       // G_i (xyz) and Sbar_i (w)
+  float* rtot;      // adjoint of rho_i incl. the constraint's
+  float* wall_part; // [blocks][6] per-block wall adjoints
+  const float4* X0; // predicted positions (the grid's positions; set by backward)
+  unsigned long long* gcell;  // packed grid cell of each particle (cell of X0)
+  unsigned long long* kcell;  // packed cell of the current positions
+  float4* fix;      // scattered adjoints of non-reciprocal pairs: xyz positions, w lambda / rho
+  float4* fixv;     // scattered velocity adjoints of non-reciprocal pairs (XSPH)
+};
+
+// Poly6 density (mass 1, radius h) of the particles at the nodes of a
+// dims[0] x dims[1] x dims[2] lattice of cell centres spanning [lo, hi], and
+// its adjoint w.r.t. the positions (both gather-only).
+cudaError_t density_grid(const float4* pos, int n, const float lo[3], const float hi[3],
+                         const int dims[3], float h, float* grid, cudaStream_t stream);
+cudaError_t density_grid_backward(const float4* pos, int n, const float lo[3], const float hi[3],
+                                  const int dims[3], float h, const float* g_grid, float4* g_pos,
+                                  cudaStream_t stream);
+
+// The reverse pass of the taped step: adjoints of its outputs (npos, nvel,
+// cell order) -> adjoints of its inputs (pos, vel, input order) and of the
+// limits (g_lim = ulim xyz, llim xyz).  fix and fixv start at zero and are
+// left at zero.
+cudaError_t backward(const BackwardArgs& args, const BackwardTape& tape, const uint32_t* perm,
+                     const void* g_npos, const void* g_nvel, void* g_pos, void* g_vel, float* g_lim,
+                     cudaStream_t stream);
+
 // Kernel launches of one build_grid call with n particles and c.cells cells.
 int grid_launches(const StepConsts& c, int n);
 

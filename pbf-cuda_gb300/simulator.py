@@ -132,6 +132,24 @@ class Simulator:
         """Run each step as a CUDA graph (default) or as individual launches."""
         check(self._L.pbf_use_graphs(self._h, int(bool(on))), "pbf_use_graphs")
 
+    def tape(self, on: bool = True) -> None:
+        """Record every following step for its reverse pass (backward)."""
+        check(self._L.pbf_tape_enable(self._h, int(bool(on))), "pbf_tape_enable")
+
+    def backward(self, g_npos: torch.Tensor, g_nvel: torch.Tensor, stream=None):
+        """Reverse pass of the last (taped) step: adjoints of its outputs npos,
+        nvel (its output order) -> adjoints of its inputs pos, vel (its input
+        order) and of the limits (6 floats: ulim xyz, llim xyz)."""
+        n = g_npos.shape[0]
+        for t, name in ((g_npos, "g_npos"), (g_nvel, "g_nvel")):
+            _check_state(t, name, n, 4)
+        g_pos = torch.zeros_like(g_npos)
+        g_vel = torch.zeros_like(g_nvel)
+        g_lim = torch.zeros(6, dtype=torch.float32, device=g_npos.device)
+        check(self._L.pbf_backward(self._h, g_npos.data_ptr(), g_nvel.data_ptr(), g_pos.data_ptr(),
+                                   g_vel.data_ptr(), g_lim.data_ptr(), _stream_handle(stream)), "pbf_backward")
+        return g_pos, g_vel, g_lim
+
     def profile(self, on: bool = True) -> None:
         """Record CUDA events between the phases of every following step."""
         check(self._L.pbf_profile_enable(self._h, int(bool(on))), "pbf_profile_enable")
