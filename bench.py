@@ -484,6 +484,78 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adjoint(args):
+    """fwd+bwd ms/frame of the inverse problem: 15,625 particles (25^3
+    lattice) in a 2 x 1 x 1 box, 60 frames of 2 steps, the loss on a
+    32 x 16 x 16 density grid, checkpoints every 10 frames.  One evaluation =
+    the forward rollout + the density grid + the reverse sweep (which re-runs
+    each 10-frame segment from its checkpoint and each step once more with the
+    tape on) + the adjoint of the grid; timed with CUDA events around whole
+    evaluations.  The forward alone (the same 120 steps through pbf_step,
+    no tape) is timed beside it for the fwd+bwd / fwd ratio."""
+    import torch
+
+    pkg = load_pkg()
+    scene = pkg.scenes.inverse_scene()
+    if args.params == "reference":
+        q = pkg.default_params()
+        q.up[0], q.up[1], q.up[2] = 0.0, 1.0, 0.0
+        q.dt = scene.params.dt
+        scene.params = q
+    stream = torch.cuda.current_stream()
+    ip = pkg.inverse.InverseProblem(scene, frames=args.frames, every=10)
+    ip.make_target()
+    v0 = torch.zeros((ip.n, 3), device="cuda")
+    warm = max(3, min(args.warmup, 3))
+    for _ in range(warm):
+        ip.loss_and_grad(v0, 0.0)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.evals):
+        L, gv, ga = ip.loss_and_grad(v0, 0.0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fb_ms = e0.elapsed_time(e1) / args.evals
+    finite = bool(torch.isfinite(gv).all()) and bool(np.isfinite(ga))
+    ip.close()
+    # forward alone
+    sim = pkg.Simulator(scene.params, scene.ulim, scene.llim, scene.n)
+    st = pkg.ParticleState(scene.pos, scene.vel)
+    for _ in range(warm):
+        st.step(sim)
+    torch.cuda.synchronize()
+    p0 = torch.from_numpy(scene.pos).cuda()
+    iid0 = torch.arange(scene.n, dtype=torch.int32, device="cuda")
+    e0.record(stream)
+    for _ in range(args.evals):
+        st.a_pos[: st.n].copy_(p0)
+        st.a_vel.zero_()
+        st.iid[: st.n].copy_(iid0)
+        st.tictoc = False
+        for k in range(ip.steps):
+            sim.setLim(*ip.limits(0.0)(k))
+            st.step(sim)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    f_ms = e0.elapsed_time(e1) / args.evals
+    sim.close()
+    frames = ip.steps // pkg.inverse.STEPS_PER_FRAME
+    line = {
+        "metric": "fwd+bwd ms/frame", "value": fb_ms / frames, "unit": "ms/frame", "n_gpus": 1,
+        "steps": args.evals, "warmup": warm, "ms_per_step": fb_ms / ip.steps, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"inverse problem: {scene.n} particles (25^3 lattice, spacing 0.04) in a 2x1x1 box, "
+                               f"{frames} frames x 2 steps, {scene.params.niter} iterations, density loss on "
+                               f"32x16x16, checkpoints every 10 frames",
+                   "params": args.params, "particles": scene.n},
+        "forward_ms_per_frame": f_ms / frames,
+        "fwd_bwd_over_fwd": fb_ms / f_ms,
+        "gradient_finite": finite,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,8 +563,11 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=120, help="untimed steps (default: 60 frames x 2 steps)")
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--scene", default="large_sweep", choices=("large_sweep", "double_dam", "dam_break"))
-    ap.add_argument("--workload", choices=("step", "ensemble"), default="step",
-                    help="step: particle-updates/s of one scene; ensemble: scene-steps/s of 256 scenes")
+    ap.add_argument("--workload", choices=("step", "ensemble", "adjoint"), default="step",
+                    help="step: particle-updates/s of one scene; ensemble: scene-steps/s of 256 scenes; "
+                         "adjoint: fwd+bwd ms/frame of the inverse problem")
+    ap.add_argument("--frames", type=int, default=60, help="frames of the inverse problem (adjoint workload)")
+    ap.add_argument("--evals", type=int, default=5, help="timed gradient evaluations (adjoint workload)")
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--params", choices=("scene", "reference"), default="scene",
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
@@ -506,6 +581,8 @@ def main(argv=None):
         ap.error("--warmup must be >= 3")
     if args.workload == "ensemble":
         run_ensemble(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

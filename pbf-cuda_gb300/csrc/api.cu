@@ -417,10 +417,14 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
   const int niter = P.niter;
   const int piters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   const bool prof = P.ev != nullptr;
-  // External: under stream capture the record becomes an event-record node of
-  // the graph (a plain record would only order the capture).
+  // Under stream capture the record must be External to become an
+  // event-record node of the graph (a plain record would only order the
+  // capture); outside capture the flag is not allowed.
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  if (prof) PBF_CUDA(cudaStreamIsCapturing(st_, &cap_status), "pbf_step: capture status");
+  const unsigned ev_flags = cap_status == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : 0u;
 #define PBF_EV(e) \
-  if (prof) PBF_CUDA(cudaEventRecordWithFlags((e), st_, cudaEventRecordExternal), "pbf_step: event")
+  if (prof) PBF_CUDA(cudaEventRecordWithFlags((e), st_, ev_flags), "pbf_step: event")
   PBF_EV(P.ev[kEvStart]);
   // advect + buildGridHash (fluids/Simulator.cpp:46-53)
   const uint32_t* perm = nullptr;

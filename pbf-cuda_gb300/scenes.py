@@ -141,9 +141,17 @@ def large_sweep(seed: int = 0, niter: int = 4) -> Scene:
                  params=scene_params(niter))
 
 
+INVERSE_SPACING = 0.04
+
+
 def inverse_scene(seed: int = 0, niter: int = 4) -> Scene:
+    """15,625 particles (25^3 lattice) in a 2 x 1 x 1 box with the dam-break
+    parameters.  The lattice spacing is 0.04, not 0.05: 25 particles at 0.05
+    span 1.25, more than the box's 1.0 height and depth, while at 0.04 they
+    fill it exactly (the fluid starts ~1.95x denser than rest and spreads
+    into the free half of the box)."""
     rng = np.random.default_rng(seed)
-    pos = lattice((25, 25, 25), (0.0, 0.0, 0.0), rng)
+    pos = lattice((25, 25, 25), (0.0, 0.0, 0.0), rng, spacing=INVERSE_SPACING)
     return Scene("inverse_15k", pos, _zeros_like(pos), (2.0, 1.0, 1.0), (0.0, 0.0, 0.0),
                  params=scene_params(niter))
 

@@ -211,7 +211,7 @@ def test_graph_and_eager_steps_are_identical(pbf, cuda):
     sc = pbf.scenes.dam_break(seed=8)
     p = ref_params(pbf, 3)
     states = []
-    for graphs, prof in ((True, False), (False, False), (True, True)):
+    for graphs, prof in ((True, False), (False, False), (True, True), (False, True)):
         st = pbf.ParticleState(sc.pos, sc.vel)
         with pbf.Simulator(p, (2.0, 1.0, 1.0), (0.0, 0.0, 0.0), sc.n) as sim:
             sim.use_graphs(graphs)
