@@ -214,12 +214,29 @@ cudaError_t alloc(T** p, size_t count) {
   return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
 }
 
+// Group tables for up to max_particles particles (pbf_internal.cuh).
+cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
+  const size_t slots = pbf::group_slots(max_particles);
+  const size_t entries = (size_t)max_particles;
+  cudaError_t e = alloc(&sol.grp_cell, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_off, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_n, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_rep, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_cnt, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_pos, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_sum, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_aux, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_id, (size_t)max_particles);
+  return e;
+}
+
 void free_all(pbf_solver* s) {
   void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
                   s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
                   s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
                   s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense, s->sol.masks,
-                  s->sol.cell_flags};
+                  s->sol.cell_flags, s->sol.grp_cell, s->sol.grp_off, s->sol.grp_n, s->sol.grp_rep, s->sol.grp_cnt,
+                  s->sol.grp_pos, s->sol.grp_sum, s->sol.grp_aux, s->sol.grp_id};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -326,6 +343,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.masks, (size_t)pbf::kMaskWords * np);
   s->sol.mask_stride = (int)np;
   if (e == cudaSuccess) e = alloc(&s->sol.cell_flags, nc);
+  if (e == cudaSuccess) e = alloc_groups(s->sol, max_particles);
   if (e == cudaSuccess) s->num_sms = current_sms();
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
   s->use_graph = true;
@@ -434,6 +452,7 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
   PBF_EV(P.ev[kEvGrid]);
   if (P.perm_out) *P.perm_out = perm;
   P.sol->keys_sorted = P.grid->keys_sorted;
+  P.sol->cell_start = P.grid->cell_start;
   PBF_CUDA(pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, *P.sol, st_),
            "pbf_step: reorder");
   PBF_EV(P.ev[kEvReorder]);
@@ -796,7 +815,8 @@ void batch_free(pbf_batch* b) {
                   b->grid.cell_count, b->grid.cell_start, b->grid.radix_counts,
                   b->grid.scan_partials, b->sol.xs, b->sol.xa, b->sol.xb, b->sol.iid_s,
                   b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->sol.masks,
-                  b->sol.cell_flags, b->d_geom, b->d_sid};
+                  b->sol.cell_flags, b->sol.grp_cell, b->sol.grp_off, b->sol.grp_n, b->sol.grp_rep, b->sol.grp_cnt,
+                  b->sol.grp_pos, b->sol.grp_sum, b->sol.grp_aux, b->sol.grp_id, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -881,6 +901,7 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
   if (e == cudaSuccess) e = alloc(&b->sol.masks, (size_t)pbf::kMaskWords * np);
   b->sol.mask_stride = (int)np;
   if (e == cudaSuccess) e = alloc(&b->sol.cell_flags, nc);
+  if (e == cudaSuccess) e = alloc_groups(b->sol, (int)np);
   if (e == cudaSuccess) e = alloc(&b->d_geom, (size_t)nscenes);
   if (e == cudaSuccess) e = alloc(&b->d_sid, np);
   if (e == cudaSuccess) {

@@ -9,7 +9,7 @@
 // pbf_create allocates the solver's scratch.
 //
 // How: the scratch lives in one file-scope __device__ array of fixed size,
-// kNoAllocScratchBytes (about 6.2 MB), which is part of this library's device
+// kNoAllocScratchBytes (about 6.4 MB), which is part of this library's device
 // image: every GPU that loads the library holds it until the process exits.
 // It bounds the problem to kNoAllocMaxParticles particles and
 // kNoAllocMaxCells grid cells; larger calls are rejected with
@@ -71,7 +71,18 @@ constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
 constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
 constexpr size_t kOffMasks = kOffDense + align_up(4 * (kNp / 32 + 1));
 constexpr size_t kOffCellFlags = kOffMasks + align_up(4 * (size_t)pbf::kMaskWords * kNp);
-constexpr size_t kNoAllocScratchBytes = kOffCellFlags + align_up(4 * kNc);
+constexpr size_t kSlots = (size_t)kNoAllocMaxParticles / pbf::kGroupCell + 1;
+constexpr size_t kEntries = kNp;
+constexpr size_t kOffGrpCell = kOffCellFlags + align_up(4 * kNc);
+constexpr size_t kOffGrpOff = kOffGrpCell + align_up(4 * kSlots);
+constexpr size_t kOffGrpN = kOffGrpOff + align_up(4 * kSlots);
+constexpr size_t kOffGrpRep = kOffGrpN + align_up(4 * kSlots);
+constexpr size_t kOffGrpCnt = kOffGrpRep + align_up(4 * kEntries);
+constexpr size_t kOffGrpPos = kOffGrpCnt + align_up(4 * kEntries);
+constexpr size_t kOffGrpSum = kOffGrpPos + align_up(16 * kEntries);
+constexpr size_t kOffGrpAux = kOffGrpSum + align_up(16 * kEntries);
+constexpr size_t kOffGrpId = kOffGrpAux + align_up(16 * kEntries);
+constexpr size_t kNoAllocScratchBytes = kOffGrpId + align_up(2 * kNp);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -134,6 +145,15 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.masks = (uint32_t*)(base + kOffMasks);
   s.mask_stride = kNoAllocMaxParticles;
   s.cell_flags = (uint32_t*)(base + kOffCellFlags);
+  s.grp_cell = (int*)(base + kOffGrpCell);
+  s.grp_off = (int*)(base + kOffGrpOff);
+  s.grp_n = (int*)(base + kOffGrpN);
+  s.grp_rep = (int*)(base + kOffGrpRep);
+  s.grp_cnt = (int*)(base + kOffGrpCnt);
+  s.grp_pos = (float4*)(base + kOffGrpPos);
+  s.grp_sum = (float4*)(base + kOffGrpSum);
+  s.grp_aux = (float4*)(base + kOffGrpAux);
+  s.grp_id = (uint16_t*)(base + kOffGrpId);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;
@@ -144,6 +164,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
                            strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: grid");
   s.keys_sorted = g.keys_sorted;
+  s.cell_start = g.cell_start;
   if ((e = pbf::reorder(c, perm, (const float4*)pos, (const float4*)vel, iid, n, s, strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: reorder");
   const int niter = params->niter;

@@ -166,6 +166,19 @@ struct SolverScratch {
   int mask_stride;     // >= particles
   uint32_t* cell_flags;         // [max_cells + 1] CellFlag bits per cell, zeroed by reorder
   const uint32_t* keys_sorted;  // the grid's sorted cell ids (set before the passes)
+  const uint32_t* cell_start;   // the grid's cell prefix (set before the passes)
+  // group tables of the cells holding >= kGroupCell particles (one slot each);
+  // slot s owns entries [grp_off[s], grp_off[s] + min(particles, kMaxGroups))
+  // of a pool of max_particles entries
+  int* grp_cell;       // [group_slots] cell of each slot
+  int* grp_off;        // [group_slots] first pool entry of each slot
+  int* grp_n;          // [group_slots] groups in the slot's current table; -1: not grouped
+  int* grp_rep;        // [max_particles] pool: sorted slot of each group's first particle
+  int* grp_cnt;        // [max_particles] pool: particles of each group
+  float4* grp_pos;     // [max_particles] pool: the group's position
+  float4* grp_sum;     // [max_particles] pool: lambda (x) / density (w) of the group
+  float4* grp_aux;     // [max_particles] pool: velocity of the group (xsph)
+  uint16_t* grp_id;    // [max_particles] group of each particle of a grouped cell
 };
 
 // Bits of SolverScratch::cell_flags: the stale cell of a particle whose
@@ -177,6 +190,26 @@ enum CellFlag : uint32_t {
   kCellRhoNotPositive = 2u,  // rho <= 0 or NaN
   kCellVelNonFinite = 4u,
 };
+// Bits kCellSlotShift.. of cell_flags hold 1 + the group slot of a cell that
+// holds >= kGroupCell particles (0: none), set once per step by reorder.
+constexpr int kCellSlotShift = 8;
+
+// Group tables.  Particles piled into one cell often sit at bitwise-identical
+// positions (clamped into a box corner, or collapsed onto one point by the
+// tensile term).  For every cell holding at least kGroupCell particles, each
+// pass first groups its particles by the values that enter a pair term
+// non-linearly (position; position and density for XSPH; for delta_p the
+// lambda pass's groups, kept only where every member has the same lambda),
+// up to kMaxGroups groups (more and the cell stays ungrouped), and a window
+// containing the cell visits each group once with its multiplicity instead
+// of its particles.  XSPH's pair term is linear in v_j: a group carries the
+// sum of its members' velocities, accumulated exactly in fixed point (integer
+// atomics, so the sum does not depend on the order).  This is the
+// reference's sum with its terms grouped: results differ from it by rounding
+// only.
+constexpr int kGroupCell = 512;
+constexpr int kMaxGroups = 512;
+inline size_t group_slots(int max_particles) { return (size_t)max_particles / kGroupCell + 1; }
 
 // Neighbour masks a particle keeps between the lambda and delta_p passes of
 // one iteration: one 32-bit mask per chunk of 32 consecutive candidates.
@@ -191,7 +224,9 @@ enum StepFlag {
   kFlagXsphExact = 1,        // some rho_i <= 0 or non-finite, or some velocity non-finite
   kDenseCount0 = 2,
   kDenseCount1 = 3,
-  kNumFlags = 4
+  kGroupCount = 4,           // cells with a group slot (set by reorder)
+  kGroupPool = 5,            // group pool entries handed out (set by reorder)
+  kNumFlags = 6
 };
 
 // Entries of the dense list: one per warp of 32 consecutive particles.
@@ -221,7 +256,7 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
                         int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream);
 
 // Kernel launches of one neighbour pass.
-constexpr int kLaunchesPerPass = 2;
+constexpr int kLaunchesPerPass = 3;
 
 // ---- reverse pass (adjoint.cu) ------------------------------------------------------
 

@@ -35,6 +35,8 @@
 // candidate's lambda / density / velocity run only when a per-step flag says
 // such a value exists (StepFlag); otherwise candidates outside the cutoff
 // contribute exactly zero and are skipped.
+#include <climits>
+
 #include "pbf_internal.cuh"
 
 namespace pbf {
@@ -76,6 +78,13 @@ struct PassArgs {
   uint32_t* iid;          // delta_p_final: out (permuted inputs)
   const float4* V;        // xsph: velocities
   float4* NV;             // xsph: out
+  // group tables (the dense kernel visits groups of grouped cells)
+  const int* grp_off;
+  const int* grp_n;
+  const int* grp_cnt;
+  const float4* grp_pos;
+  const float4* grp_sum;
+  const float4* grp_aux;
 };
 
 // ---- windows ------------------------------------------------------------------------
@@ -275,6 +284,79 @@ __device__ __forceinline__ void visit_window_chunk(const SceneGeom& g,
   }
 }
 
+// Groups of cell `cell` in the pass's table, or -1 when the cell is visited
+// particle by particle.
+__device__ __forceinline__ int cell_groups(const PassArgs& a, int cell, int& slot) {
+  const uint32_t sl = __ldg(a.cell_flags + cell) >> kCellSlotShift;
+  slot = (int)sl - 1;
+  return sl ? __ldg(a.grp_n + slot) : -1;
+}
+
+// Entries of the window when grouped cells count their groups.
+__device__ __forceinline__ int window_total_grouped(const SceneGeom& g, const PassArgs& a, int3 q) {
+  const int zlo = max(q.z - 1, 0), zhi = min(q.z + 1, g.dims[2] - 1);
+  int total = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      const int base = g.cell_base + (x * g.dims[1] + y) * g.dims[2];
+      for (int z = zlo; z <= zhi; ++z) {
+        int slot;
+        const int ng = cell_groups(a, base + z, slot);
+        if (ng > 0) {
+          total += ng;
+        } else {
+          const int s0 = (int)__ldg(a.cs + base + z);
+          total += max(min((int)__ldg(a.cs + base + z + 1), a.n), s0) - s0;
+        }
+      }
+    }
+  }
+  return total;
+}
+
+// Entries [v_lo, v_hi) of the window in visiting order, grouped cells
+// contributing their groups (p.visit_group) and the other cells their
+// particles (p.visit).  Without grouped cells this visits exactly what
+// visit_window_chunk does, in the same order.
+template <class P>
+__device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const PassArgs& a, int3 q,
+                                                     P& p, int v_lo, int v_hi) {
+  const int zlo = max(q.z - 1, 0), zhi = min(q.z + 1, g.dims[2] - 1);
+  int v0 = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      const int base = g.cell_base + (x * g.dims[1] + y) * g.dims[2];
+      for (int z = zlo; z <= zhi; ++z) {
+        int slot;
+        const int ng = cell_groups(a, base + z, slot);
+        const int s0 = (int)__ldg(a.cs + base + z);
+        const int e0 = max(min((int)__ldg(a.cs + base + z + 1), a.n), s0);
+        const int len = ng > 0 ? ng : e0 - s0;
+        const int lo = max(v_lo, v0), hi = min(v_hi, v0 + len);
+        if (lo < hi) {
+          if (ng > 0) {
+            const int t0 = __ldg(a.grp_off + slot);
+            for (int t = t0 + (lo - v0); t < t0 + (hi - v0); ++t)
+              p.visit_group(__ldg(a.grp_pos + t), __ldg(a.grp_cnt + t), __ldg(a.grp_sum + t),
+                            __ldg(a.grp_aux + t));
+          } else {
+            for (int j = s0 + (lo - v0); j < s0 + (hi - v0); ++j) p.visit(__ldg(a.X + j), j);
+          }
+        }
+        v0 += len;
+      }
+    }
+  }
+}
+
 // ---- the passes: per-candidate visit, partial-sum fields, finish ----------------------
 
 struct LambdaPass {
@@ -304,6 +386,26 @@ struct LambdaPass {
         gy += ay;
         gz += az;
         if (j != i) gl2 += dist2(ax, ay, az);
+      }
+    }
+  }
+  // `cnt` particles at xg.  The group holding i itself lies at r2 = 0 <
+  // keps2 (grouping needs keps2 > 0): no gradient, as the reference's j != i.
+  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4, float4) {
+    const float ex = xi.x - xg.x, ey = xi.y - xg.y, ez = xi.z - xg.z;
+    const float r2 = dist2(ex, ey, ez);
+    if (!(r2 >= c.h2)) {
+      const float fc = (float)cnt;
+      pho += fc * poly6_inside(c, r2);
+      if (!(r2 < c.keps2)) {
+        const float ir = rsqrtf(r2);
+        const float t = c.h - r2 * ir;
+        const float sc = c.spiky_coef_rho0 * t * t * ir;
+        const float ax = sc * ex, ay = sc * ey, az = sc * ez;
+        gx += fc * ax;
+        gy += fc * ay;
+        gz += fc * az;
+        gl2 += fc * dist2(ax, ay, az);
       }
     }
   }
@@ -367,6 +469,22 @@ struct DeltaPPass {
     } else if (exact && j != i) {
       // zero gradient: (lambda_i + lambda_j + s_corr) * 0 is NaN iff a lambda is not finite
       poison |= !isfinite(li) || !isfinite(__ldg(lambda + j));
+    }
+  }
+  // `cnt` particles at xg sharing lambda sum.x (sum.y: the sum over the
+  // group of lambda_j - sum.x, zero for the groups built here).
+  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4 sum, float4) {
+    const float ex = xi.x - xg.x, ey = xi.y - xg.y, ez = xi.z - xg.z;
+    const float r2 = dist2(ex, ey, ez);
+    if (!(r2 >= c.h2) && !(r2 < c.keps2)) {
+      const float wgt = poly6_inside(c, r2);
+      const float corr = c.coef_corr * pow_corr(c, wgt);
+      const float ir = rsqrtf(r2);
+      const float t = c.h - r2 * ir;
+      const float f = ((float)cnt * (li + sum.x + corr) + sum.y) * (c.spiky_coef * t * t * ir);
+      ax = fmaf(f, ex, ax);
+      ay = fmaf(f, ey, ay);
+      az = fmaf(f, ez, az);
     }
   }
   __device__ void store(float* f, int stride) const {
@@ -443,6 +561,19 @@ struct XsphPass {
       px |= bad_den || !isfinite(vj.x - vi.x);
       py |= bad_den || !isfinite(vj.y - vi.y);
       pz |= bad_den || !isfinite(vj.z - vi.z);
+    }
+  }
+  // `cnt` particles at xg sharing the density sum.w and the velocity aux.xyz
+  // (sum.xyz: the sum over the group of v_j - aux.xyz, zero for the groups
+  // built here).
+  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4 sum, float4 aux) {
+    const float r2 = dist2(xi.x - xg.x, xi.y - xg.y, xi.z - xg.z);
+    if (!(r2 >= c.h2)) {
+      const float fc = (float)cnt;
+      const float w2 = 2.f * poly6_inside(c, r2) / (ri + sum.w);
+      ax = fmaf(fmaf(fc, aux.x - vi.x, sum.x), w2, ax);
+      ay = fmaf(fmaf(fc, aux.y - vi.y, sum.y), w2, ay);
+      az = fmaf(fmaf(fc, aux.z - vi.z, sum.z), w2, az);
     }
   }
   __device__ void store(float* f, int stride) const {
@@ -532,12 +663,17 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
     const int3 q = cell_of(a.c, g, xi);
     const bool exact = valid && exact_path(kKind, a, g, q, i);
+    // grouped cells are visited by groups unless i needs every candidate
+    const bool grouped = !exact && a.c.keps2 > 0.f;
     if (valid) {
-      const int total = window_total(g, a.cs, a.n, q);
+      const int total = grouped ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
       const int lo = (int)((long long)total * warp / kDenseWarps);
       const int hi = (int)((long long)total * (warp + 1) / kDenseWarps);
       P p(a, g, xi, i, exact);
-      visit_window_chunk(g, a.cs, a.n, q, a.X, p, lo, hi);
+      if (grouped)
+        visit_window_grouped(g, a, q, p, lo, hi);
+      else
+        visit_window_chunk(g, a.cs, a.n, q, a.X, p, lo, hi);
       p.store(&part[warp][0][lane], 32);
     }
     __syncthreads();
@@ -550,14 +686,27 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   }
 }
 
+// Also registers every cell holding >= kGroupCell particles (its first
+// particle takes a group slot).  flags and cell_flags start at zero.
 __global__ void __launch_bounds__(256)
 k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
           const float4* __restrict__ vel, const uint32_t* __restrict__ iid, int n, StepConsts c,
           float4* __restrict__ xs, float4* __restrict__ xa, uint32_t* __restrict__ iid_s,
-          uint32_t* __restrict__ flags) {
+          uint32_t* __restrict__ flags, const uint32_t* __restrict__ skeys,
+          const uint32_t* __restrict__ cs, uint32_t* __restrict__ cell_flags, int* __restrict__ grp_cell,
+          int* __restrict__ grp_off) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < kNumFlags) flags[k] = 0u;  // the step's flags and counters start clear
   if (k >= n) return;
+  const uint32_t key = skeys[k];
+  const uint32_t pop = cs[key + 1] - cs[key];
+  if ((uint32_t)k == cs[key] && pop >= (uint32_t)kGroupCell) {
+    // one slot per such cell (< n / kGroupCell of them) and min(pop, kMaxGroups)
+    // pool entries (the pool holds n: the cells' populations sum to <= n)
+    const uint32_t slot = atomicAdd(&flags[kGroupCount], 1u);
+    grp_cell[slot] = (int)key;
+    grp_off[slot] = (int)atomicAdd(&flags[kGroupPool], min(pop, (uint32_t)kMaxGroups));
+    atomicOr(&cell_flags[key], (slot + 1u) << kCellSlotShift);
+  }
   const uint32_t p = min(perm[k], (uint32_t)(n - 1));  // a permutation of [0, n): the min never binds
   const float4 x = pos[p];
   const float4 v = vel[p];
@@ -566,6 +715,247 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
   xs[k] = x;
   xa[k] = make_float4(fmaf(c.dt, vx, x.x), fmaf(c.dt, vy, x.y), fmaf(c.dt, vz, x.z), x.w);
   iid_s[k] = iid[p];
+}
+
+// ---- group tables ----------------------------------------------------------------------
+
+enum GroupsWhat { kGroupsPos = 0, kGroupsLambda = 1, kGroupsXsph = 2 };
+
+constexpr int kGroupThreads = 256;
+constexpr int kGroupHash = 2 * kMaxGroups;  // open-addressing slots of a block's hash table
+
+struct GroupArgs {
+  const float4* X;        // positions of the pass
+  const float4* V;        // xsph: velocities
+  const float* rho;       // xsph: densities
+  const float* lambda;    // delta_p: lambda
+  const uint32_t* cs;
+  const uint32_t* count;  // number of slots (flags[kGroupCount])
+  int n;
+  const int* cell;
+  const int* off;
+  int* ng;
+  int* rep;
+  int* cnt;
+  float4* pos;
+  float4* sum;
+  float4* aux;
+  uint16_t* id;
+};
+
+// The key of particle j: the values a pass reads of a neighbour, as bits.
+template <int kWhat>
+struct GroupKey {
+  static constexpr int kWords = kWhat == kGroupsXsph ? 4 : 3;
+  uint32_t w[kWords];
+  __device__ __forceinline__ GroupKey(const GroupArgs& a, int j) {
+    const float4 x = a.X[j];
+    w[0] = __float_as_uint(x.x), w[1] = __float_as_uint(x.y), w[2] = __float_as_uint(x.z);
+    if constexpr (kWhat == kGroupsXsph) w[3] = __float_as_uint(a.rho[j]);
+  }
+  __device__ __forceinline__ bool operator==(const GroupKey& o) const {
+    bool eq = true;
+    for (int k = 0; k < kWords; ++k) eq &= w[k] == o.w[k];
+    return eq;
+  }
+  __device__ __forceinline__ uint32_t hash() const {
+    uint32_t h = 0x9e3779b9u;
+    for (int k = 0; k < kWords; ++k) {
+      h ^= w[k] + 0x7f4a7c15u + (h << 6) + (h >> 2);
+      h *= 0x85ebca6bu;
+    }
+    return h ^ (h >> 15);
+  }
+};
+
+// One block per slot (grid-stride).
+//   kGroupsPos / kGroupsXsph: group the cell's particles by GroupKey in a
+//     shared-memory hash table (the claiming particle of a hash slot holds the
+//     key; integer atomics only), order the groups by their first particle,
+//     and write rep, cnt, pos and each particle's group id; for xsph also
+//     aux = the first particle's velocity v_rep, sum.w = density and sum.xyz
+//     = sum over the group of (v_j - v_rep), in 64-bit fixed point scaled by
+//     a power of two from the group's largest |v_j - v_rep| and count (exact
+//     to 2^-62 of the bound, order-free).  Over kMaxGroups groups, or a
+//     non-finite velocity difference: ng = -1.
+//   kGroupsLambda: keep the kGroupsPos table of the same positions for
+//     delta_p where every member has its group's lambda (sum.x); else ng = -1.
+// Deterministic: the table's contents do not depend on which particle of a
+// group claimed its hash slot.
+template <int kWhat>
+__global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
+  __shared__ int s_owner[kGroupHash];   // claiming particle (cell-relative) or -1
+  __shared__ int s_cnt[kGroupHash];
+  __shared__ int s_first[kGroupHash];   // first particle of the group
+  __shared__ int s_rank[kGroupHash];
+  __shared__ int s_used, s_over;
+  const uint32_t slots = *a.count;
+  for (uint32_t slot = blockIdx.x; slot < slots; slot += gridDim.x) {
+    const int cell = a.cell[slot];
+    const int b = (int)a.cs[cell];
+    const int m = max(min((int)a.cs[cell + 1], a.n) - b, 0);
+    const int t0 = a.off[slot];
+    if constexpr (kWhat == kGroupsLambda) {
+      const int ng = a.ng[slot];
+      if (ng <= 0) continue;
+      if (threadIdx.x == 0) s_over = 0;
+      __syncthreads();
+      bool bad = false;
+      for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+        const int g = a.id[b + k];
+        bad |= g >= ng || __float_as_uint(a.lambda[b + k]) != __float_as_uint(a.lambda[a.rep[t0 + g]]);
+      }
+      if (bad) atomicOr(&s_over, 1);
+      __syncthreads();
+      if (s_over) {
+        if (threadIdx.x == 0) a.ng[slot] = -1;
+      } else {
+        for (int g = threadIdx.x; g < ng; g += kGroupThreads)
+          a.sum[t0 + g] = make_float4(a.lambda[a.rep[t0 + g]], 0.f, 0.f, 0.f);
+      }
+      __syncthreads();
+    } else {
+      for (int h = threadIdx.x; h < kGroupHash; h += kGroupThreads) {
+        s_owner[h] = -1;
+        s_cnt[h] = 0;
+        s_first[h] = INT_MAX;
+      }
+      if (threadIdx.x == 0) s_used = s_over = 0;
+      __syncthreads();
+      for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+        if (*(volatile int*)&s_over) break;
+        const GroupKey<kWhat> key(a, b + k);
+        int h = (int)(key.hash() & (kGroupHash - 1));
+        int found = -1;
+        for (int probe = 0; probe < kGroupHash; ++probe, h = (h + 1) & (kGroupHash - 1)) {
+          int o = *(volatile int*)&s_owner[h];
+          if (o < 0) {
+            o = atomicCAS(&s_owner[h], -1, k);
+            if (o < 0) {  // claimed: a new group
+              if (atomicAdd(&s_used, 1) >= kMaxGroups) atomicOr(&s_over, 1);
+              found = h;
+              break;
+            }
+          }
+          if (GroupKey<kWhat>(a, b + o) == key) {
+            found = h;
+            break;
+          }
+        }
+        if (found < 0) {
+          atomicOr(&s_over, 1);
+          break;
+        }
+        // one atomic per group per warp: the lowest lane holds the lowest k
+        const unsigned same = __match_any_sync(__activemask(), found);
+        if ((threadIdx.x & 31) == __ffs(same) - 1) {
+          atomicAdd(&s_cnt[found], __popc(same));
+          atomicMin(&s_first[found], k);
+        }
+        a.id[b + k] = (uint16_t)found;
+      }
+      __syncthreads();
+      const int ng = s_over ? -1 : s_used;
+      if (ng > 0) {
+        // rank of each group = groups with an earlier first particle
+        for (int h = threadIdx.x; h < kGroupHash; h += kGroupThreads) {
+          if (s_owner[h] < 0) continue;
+          const int f = s_first[h];
+          int r = 0;
+          for (int u = 0; u < kGroupHash; ++u) r += s_owner[u] >= 0 && s_first[u] < f;
+          s_rank[h] = r;
+          const int j = b + f;
+          a.rep[t0 + r] = j;
+          a.cnt[t0 + r] = s_cnt[h];
+          a.pos[t0 + r] = a.X[j];
+        }
+        __syncthreads();
+        for (int k = threadIdx.x; k < m; k += kGroupThreads) a.id[b + k] = (uint16_t)s_rank[a.id[b + k]];
+      }
+      int ngw = ng;
+      if constexpr (kWhat == kGroupsXsph) {
+        __shared__ unsigned s_max[kMaxGroups];
+        __shared__ int s_shift[kMaxGroups];
+        __shared__ float4 s_vrep[kMaxGroups];
+        __shared__ unsigned long long s_acc[kMaxGroups][3];
+        if (ng > 0) {
+          __syncthreads();
+          for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+            s_max[g] = 0u;
+            s_vrep[g] = a.V[a.rep[t0 + g]];
+            s_acc[g][0] = s_acc[g][1] = s_acc[g][2] = 0ull;
+          }
+          __syncthreads();
+          for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+            const int g = a.id[b + k];
+            const float4 v = a.V[b + k], vr = s_vrep[g];
+            const float d = fmaxf(fmaxf(fabsf(v.x - vr.x), fabsf(v.y - vr.y)), fabsf(v.z - vr.z));
+            const bool fin = isfinite(v.x - vr.x) && isfinite(v.y - vr.y) && isfinite(v.z - vr.z);
+            atomicMax(&s_max[g], fin ? __float_as_uint(d) : 0x7f800000u);  // +inf marks non-finite
+          }
+          if (threadIdx.x == 0) s_over = 0;
+          __syncthreads();
+          for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+            const float mx = __uint_as_float(s_max[g]);
+            if (!isfinite(mx)) atomicOr(&s_over, 1);
+            int e = 0;
+            if (mx > 0.f) frexpf(mx, &e);                      // mx < 2^e
+            const int c = 32 - __clz(a.cnt[t0 + g]);           // cnt < 2^c
+            s_shift[g] = 62 - e - c;                           // |sum| * 2^shift < 2^62
+          }
+          __syncthreads();
+          if (!s_over) {
+            for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+              const int g = a.id[b + k];
+              const float4 v = a.V[b + k], vr = s_vrep[g];
+              const int sh = s_shift[g];
+              atomicAdd(&s_acc[g][0], (unsigned long long)llrint(ldexp((double)(v.x - vr.x), sh)));
+              atomicAdd(&s_acc[g][1], (unsigned long long)llrint(ldexp((double)(v.y - vr.y), sh)));
+              atomicAdd(&s_acc[g][2], (unsigned long long)llrint(ldexp((double)(v.z - vr.z), sh)));
+            }
+          }
+          __syncthreads();
+          if (s_over) {
+            ngw = -1;
+          } else {
+            for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+              const int sh = -s_shift[g];
+              a.sum[t0 + g] = make_float4((float)ldexp((double)(long long)s_acc[g][0], sh),
+                                          (float)ldexp((double)(long long)s_acc[g][1], sh),
+                                          (float)ldexp((double)(long long)s_acc[g][2], sh), a.rho[a.rep[t0 + g]]);
+              a.aux[t0 + g] = s_vrep[g];
+            }
+          }
+        }
+      }
+      if (threadIdx.x == 0) a.ng[slot] = ngw;
+      __syncthreads();
+    }
+  }
+}
+
+template <int kWhat>
+cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const float4* X, const float4* V, int n,
+                          cudaStream_t stream) {
+  GroupArgs a;
+  a.X = X;
+  a.V = V;
+  a.rho = s.rho;
+  a.lambda = s.lambda;
+  a.cs = s.cell_start;
+  a.count = s.flags + kGroupCount;
+  a.n = n;
+  a.cell = s.grp_cell;
+  a.off = s.grp_off;
+  a.ng = s.grp_n;
+  a.rep = s.grp_rep;
+  a.cnt = s.grp_cnt;
+  a.pos = s.grp_pos;
+  a.sum = s.grp_sum;
+  a.aux = s.grp_aux;
+  a.id = s.grp_id;
+  k_groups<kWhat><<<c.dense_grid, kGroupThreads, 0, stream>>>(a);
+  return cudaGetLastError();
 }
 
 PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs,
@@ -586,6 +976,12 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.skeys = s.keys_sorted;
   a.lambda = s.lambda;
   a.rho = s.rho;
+  a.grp_off = s.grp_off;
+  a.grp_n = s.grp_n;
+  a.grp_cnt = s.grp_cnt;
+  a.grp_pos = s.grp_pos;
+  a.grp_sum = s.grp_sum;
+  a.grp_aux = s.grp_aux;
   return a;
 }
 
@@ -600,20 +996,26 @@ cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
 
 cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
                     const uint32_t* iid, int n, SolverScratch& s, cudaStream_t stream) {
-  const cudaError_t e = cudaMemsetAsync(s.cell_flags, 0, sizeof(uint32_t) * (c.cells + 1), stream);
+  cudaError_t e = cudaMemsetAsync(s.cell_flags, 0, sizeof(uint32_t) * (c.cells + 1), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(s.flags, 0, sizeof(uint32_t) * kNumFlags, stream);
   if (e != cudaSuccess) return e;
   k_reorder<<<(n + 255) / 256, 256, 0, stream>>>(perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
-                                                  s.flags);
+                                                  s.flags, s.keys_sorted, s.cell_start, s.cell_flags,
+                                                  s.grp_cell, s.grp_off);
   return cudaGetLastError();
 }
 
 cudaError_t launch_lambda(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                           const SolverScratch& s, int pass, cudaStream_t stream) {
+  cudaError_t e = launch_groups<kGroupsPos>(c, s, X, nullptr, n, stream);
+  if (e != cudaSuccess) return e;
   return run_pass<kLambda>(base_args(c, G, X, cs, n, s, pass), stream);
 }
 
 cudaError_t launch_delta_p(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                            const SolverScratch& s, int pass, float4* T, cudaStream_t stream) {
+  cudaError_t e = launch_groups<kGroupsLambda>(c, s, X, nullptr, n, stream);
+  if (e != cudaSuccess) return e;
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.T = T;
   return run_pass<kDeltaP>(a, stream);
@@ -622,6 +1024,8 @@ cudaError_t launch_delta_p(const StepConsts& c, const Geometry& G, const float4*
 cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                                  const SolverScratch& s, int pass, float4* pos, float4* npos,
                                  float4* vel, uint32_t* iid, cudaStream_t stream) {
+  cudaError_t e = launch_groups<kGroupsLambda>(c, s, X, nullptr, n, stream);
+  if (e != cudaSuccess) return e;
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.xs = s.xs;
   a.iid_s = s.iid_s;
@@ -634,6 +1038,8 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const f
 
 cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X, const float4* V, const uint32_t* cs,
                         int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream) {
+  cudaError_t e = launch_groups<kGroupsXsph>(c, s, X, V, n, stream);
+  if (e != cudaSuccess) return e;
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.V = V;
   a.NV = NV;
