@@ -198,15 +198,14 @@ constexpr int kCellSlotShift = 8;
 // positions (clamped into a box corner, or collapsed onto one point by the
 // tensile term).  For every cell holding at least kGroupCell particles, each
 // pass first groups its particles by the values that enter a pair term
-// non-linearly (position; position and density for XSPH; for delta_p the
-// lambda pass's groups, kept only where every member has the same lambda),
-// up to kMaxGroups groups (more and the cell stays ungrouped), and a window
-// containing the cell visits each group once with its multiplicity instead
-// of its particles.  XSPH's pair term is linear in v_j: a group carries the
-// sum of its members' velocities, accumulated exactly in fixed point (integer
-// atomics, so the sum does not depend on the order).  This is the
-// reference's sum with its terms grouped: results differ from it by rounding
-// only.
+// non-linearly (position; position and density for XSPH; delta_p reuses the
+// lambda pass's groups), up to kMaxGroups groups (more and the cell stays
+// ungrouped), and a window containing the cell visits each group once with
+// its multiplicity instead of its particles.  The pair terms are linear in
+// lambda_j (delta_p) and v_j (XSPH): a group carries the sum of its members'
+// values, accumulated exactly in fixed point (integer atomics, so the sum
+// does not depend on the order).  This is the reference's sum with its terms
+// grouped: results differ from it by rounding only.
 constexpr int kGroupCell = 512;
 constexpr int kMaxGroups = 512;
 inline size_t group_slots(int max_particles) { return (size_t)max_particles / kGroupCell + 1; }

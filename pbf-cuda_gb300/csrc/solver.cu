@@ -319,9 +319,9 @@ __device__ __forceinline__ int window_total_grouped(const SceneGeom& g, const Pa
 }
 
 // Entries [v_lo, v_hi) of the window in visiting order, grouped cells
-// contributing their groups (p.visit_group) and the other cells their
-// particles (p.visit).  Without grouped cells this visits exactly what
-// visit_window_chunk does, in the same order.
+// contributing their groups (p.visit_group; `own`: i belongs to the cell) and
+// the other cells their particles (p.visit).  Without grouped cells this
+// visits exactly what visit_window_chunk does, in the same order.
 template <class P>
 __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const PassArgs& a, int3 q,
                                                      P& p, int v_lo, int v_hi) {
@@ -344,9 +344,10 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
         if (lo < hi) {
           if (ng > 0) {
             const int t0 = __ldg(a.grp_off + slot);
+            const bool own = p.i >= s0 && p.i < e0;  // i is one of the cell's particles
             for (int t = t0 + (lo - v0); t < t0 + (hi - v0); ++t)
               p.visit_group(__ldg(a.grp_pos + t), __ldg(a.grp_cnt + t), __ldg(a.grp_sum + t),
-                            __ldg(a.grp_aux + t));
+                            __ldg(a.grp_aux + t), own);
           } else {
             for (int j = s0 + (lo - v0); j < s0 + (hi - v0); ++j) p.visit(__ldg(a.X + j), j);
           }
@@ -391,7 +392,7 @@ struct LambdaPass {
   }
   // `cnt` particles at xg.  The group holding i itself lies at r2 = 0 <
   // keps2 (grouping needs keps2 > 0): no gradient, as the reference's j != i.
-  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4, float4) {
+  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4, float4, bool) {
     const float ex = xi.x - xg.x, ey = xi.y - xg.y, ez = xi.z - xg.z;
     const float r2 = dist2(ex, ey, ez);
     if (!(r2 >= c.h2)) {
@@ -471,9 +472,11 @@ struct DeltaPPass {
       poison |= !isfinite(li) || !isfinite(__ldg(lambda + j));
     }
   }
-  // `cnt` particles at xg sharing lambda sum.x (sum.y: the sum over the
-  // group of lambda_j - sum.x, zero for the groups built here).
-  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4 sum, float4) {
+  // `cnt` particles at xg with lambda_j summing to cnt sum.x + sum.y (each
+  // lambda_j - sum.x finite, or lambda_j the same bits as sum.x).  exact: the
+  // poisoning rule for the group's members j != i (i is a member when it
+  // belongs to the cell and sits at xg).
+  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4 sum, float4, bool own) {
     const float ex = xi.x - xg.x, ey = xi.y - xg.y, ez = xi.z - xg.z;
     const float r2 = dist2(ex, ey, ez);
     if (!(r2 >= c.h2) && !(r2 < c.keps2)) {
@@ -485,6 +488,11 @@ struct DeltaPPass {
       ax = fmaf(f, ex, ax);
       ay = fmaf(f, ey, ay);
       az = fmaf(f, ez, az);
+    } else if (exact) {
+      const bool member = own && __float_as_uint(xi.x) == __float_as_uint(xg.x) &&
+                          __float_as_uint(xi.y) == __float_as_uint(xg.y) &&
+                          __float_as_uint(xi.z) == __float_as_uint(xg.z);
+      if (cnt > (member ? 1 : 0)) poison |= !isfinite(li) || !isfinite(sum.x);
     }
   }
   __device__ void store(float* f, int stride) const {
@@ -566,7 +574,10 @@ struct XsphPass {
   // `cnt` particles at xg sharing the density sum.w and the velocity aux.xyz
   // (sum.xyz: the sum over the group of v_j - aux.xyz, zero for the groups
   // built here).
-  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4 sum, float4 aux) {
+  // exact: the rule for 0 * (v_j - v_i) / (rho_i + rho_j) outside the cutoff;
+  // the group build guarantees that every member's v_j - aux is finite or
+  // that v_j is aux itself, so the first member's velocity decides.
+  __device__ __forceinline__ void visit_group(float4 xg, int cnt, float4 sum, float4 aux, bool) {
     const float r2 = dist2(xi.x - xg.x, xi.y - xg.y, xi.z - xg.z);
     if (!(r2 >= c.h2)) {
       const float fc = (float)cnt;
@@ -574,6 +585,12 @@ struct XsphPass {
       ax = fmaf(fmaf(fc, aux.x - vi.x, sum.x), w2, ax);
       ay = fmaf(fmaf(fc, aux.y - vi.y, sum.y), w2, ay);
       az = fmaf(fmaf(fc, aux.z - vi.z, sum.z), w2, az);
+    } else if (exact) {
+      const float den = ri + sum.w;
+      const bool bad_den = !(den != 0.f) || isnan(den);
+      px |= bad_den || !isfinite(aux.x - vi.x);
+      py |= bad_den || !isfinite(aux.y - vi.y);
+      pz |= bad_den || !isfinite(aux.z - vi.z);
     }
   }
   __device__ void store(float* f, int stride) const {
@@ -663,8 +680,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
     const int3 q = cell_of(a.c, g, xi);
     const bool exact = valid && exact_path(kKind, a, g, q, i);
-    // grouped cells are visited by groups unless i needs every candidate
-    const bool grouped = !exact && a.c.keps2 > 0.f;
+    // grouped cells are visited by groups (the exact rules apply per group)
+    const bool grouped = a.c.keps2 > 0.f;
     if (valid) {
       const int total = grouped ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
       const int lo = (int)((long long)total * warp / kDenseWarps);
@@ -721,7 +738,7 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
 
 enum GroupsWhat { kGroupsPos = 0, kGroupsLambda = 1, kGroupsXsph = 2 };
 
-constexpr int kGroupThreads = 256;
+constexpr int kGroupThreads = 1024;  // one block per grouped cell: many loads in flight
 constexpr int kGroupHash = 2 * kMaxGroups;  // open-addressing slots of a block's hash table
 
 struct GroupArgs {
@@ -777,11 +794,20 @@ struct GroupKey {
 //     = sum over the group of (v_j - v_rep), in 64-bit fixed point scaled by
 //     a power of two from the group's largest |v_j - v_rep| and count (exact
 //     to 2^-62 of the bound, order-free).  Over kMaxGroups groups, or a
-//     non-finite velocity difference: ng = -1.
-//   kGroupsLambda: keep the kGroupsPos table of the same positions for
-//     delta_p where every member has its group's lambda (sum.x); else ng = -1.
+//     non-finite velocity difference (other than between identical bits):
+//     ng = -1.
+//   kGroupsLambda: for the kGroupsPos table of the same positions, sum.x =
+//     lambda_rep and sum.y = sum over the group of (lambda_j - lambda_rep) in
+//     the same fixed point as xsph's velocities; a non-finite difference
+//     (other than between identical bits): ng = -1.
 // Deterministic: the table's contents do not depend on which particle of a
 // group claimed its hash slot.
+// x - x_rep, and 0 where the two are the same bits (so a group whose members
+// share one non-finite value stays grouped).
+__device__ __forceinline__ float dev_from(float x, float xr) {
+  return __float_as_uint(x) == __float_as_uint(xr) ? 0.f : x - xr;
+}
+
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
   __shared__ int s_owner[kGroupHash];   // claiming particle (cell-relative) or -1
@@ -796,22 +822,62 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
     const int m = max(min((int)a.cs[cell + 1], a.n) - b, 0);
     const int t0 = a.off[slot];
     if constexpr (kWhat == kGroupsLambda) {
+      // sum over each group of (lambda_j - lambda_rep) in 64-bit fixed point:
+      // members at one position can still differ in the last bits of lambda
+      // (their windows may have been summed by different kernels)
+      __shared__ unsigned l_max[kMaxGroups];
+      __shared__ int l_shift[kMaxGroups];
+      __shared__ float l_rep[kMaxGroups];
+      __shared__ unsigned long long l_acc[kMaxGroups];
       const int ng = a.ng[slot];
       if (ng <= 0) continue;
+      for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+        l_max[g] = 0u;
+        l_rep[g] = a.lambda[a.rep[t0 + g]];
+        l_acc[g] = 0ull;
+      }
       if (threadIdx.x == 0) s_over = 0;
       __syncthreads();
-      bool bad = false;
       for (int k = threadIdx.x; k < m; k += kGroupThreads) {
         const int g = a.id[b + k];
-        bad |= g >= ng || __float_as_uint(a.lambda[b + k]) != __float_as_uint(a.lambda[a.rep[t0 + g]]);
+        const float d = dev_from(a.lambda[b + k], l_rep[g]);
+        const unsigned bits = isfinite(d) ? __float_as_uint(fabsf(d)) : 0x7f800000u;
+        const unsigned act = __activemask(), same = __match_any_sync(act, g);
+        if (same == act) {
+          const unsigned mx = __reduce_max_sync(act, bits);
+          if ((threadIdx.x & 31) == __ffs(act) - 1) atomicMax(&l_max[g], mx);
+        } else {
+          atomicMax(&l_max[g], bits);
+        }
       }
-      if (bad) atomicOr(&s_over, 1);
+      __syncthreads();
+      for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+        const float mx = __uint_as_float(l_max[g]);
+        if (!isfinite(mx)) atomicOr(&s_over, 1);
+        int e = 0;
+        if (mx > 0.f) frexpf(mx, &e);
+        l_shift[g] = 62 - e - (32 - __clz(a.cnt[t0 + g]));
+      }
+      __syncthreads();
+      if (!s_over) {
+        for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+          const int g = a.id[b + k];
+          long long q = __float2ll_rn(ldexpf(dev_from(a.lambda[b + k], l_rep[g]), l_shift[g]));
+          const unsigned act = __activemask(), same = __match_any_sync(act, g);
+          if (same == act) {
+            for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(act, q, o);
+            if ((threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(&l_acc[g], (unsigned long long)q);
+          } else {
+            atomicAdd(&l_acc[g], (unsigned long long)q);
+          }
+        }
+      }
       __syncthreads();
       if (s_over) {
         if (threadIdx.x == 0) a.ng[slot] = -1;
       } else {
         for (int g = threadIdx.x; g < ng; g += kGroupThreads)
-          a.sum[t0 + g] = make_float4(a.lambda[a.rep[t0 + g]], 0.f, 0.f, 0.f);
+          a.sum[t0 + g] = make_float4(l_rep[g], (float)ldexp((double)(long long)l_acc[g], -l_shift[g]), 0.f, 0.f);
       }
       __syncthreads();
     } else {
@@ -889,9 +955,17 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
           for (int k = threadIdx.x; k < m; k += kGroupThreads) {
             const int g = a.id[b + k];
             const float4 v = a.V[b + k], vr = s_vrep[g];
-            const float d = fmaxf(fmaxf(fabsf(v.x - vr.x), fabsf(v.y - vr.y)), fabsf(v.z - vr.z));
-            const bool fin = isfinite(v.x - vr.x) && isfinite(v.y - vr.y) && isfinite(v.z - vr.z);
-            atomicMax(&s_max[g], fin ? __float_as_uint(d) : 0x7f800000u);  // +inf marks non-finite
+            const float dx = dev_from(v.x, vr.x), dy = dev_from(v.y, vr.y), dz = dev_from(v.z, vr.z);
+            const float d = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
+            const bool fin = isfinite(dx) && isfinite(dy) && isfinite(dz);
+            const unsigned bits = fin ? __float_as_uint(d) : 0x7f800000u;  // +inf marks non-finite
+            const unsigned act = __activemask(), same = __match_any_sync(act, g);
+            if (same == act) {  // the common case: one group for the whole warp
+              const unsigned mx = __reduce_max_sync(act, bits);
+              if ((threadIdx.x & 31) == __ffs(act) - 1) atomicMax(&s_max[g], mx);
+            } else {
+              atomicMax(&s_max[g], bits);
+            }
           }
           if (threadIdx.x == 0) s_over = 0;
           __syncthreads();
@@ -909,9 +983,19 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
               const int g = a.id[b + k];
               const float4 v = a.V[b + k], vr = s_vrep[g];
               const int sh = s_shift[g];
-              atomicAdd(&s_acc[g][0], (unsigned long long)llrint(ldexp((double)(v.x - vr.x), sh)));
-              atomicAdd(&s_acc[g][1], (unsigned long long)llrint(ldexp((double)(v.y - vr.y), sh)));
-              atomicAdd(&s_acc[g][2], (unsigned long long)llrint(ldexp((double)(v.z - vr.z), sh)));
+              // |d| 2^sh < 2^62 is a float without overflow; the scaling is exact
+              long long q[3] = {__float2ll_rn(ldexpf(dev_from(v.x, vr.x), sh)),
+                                __float2ll_rn(ldexpf(dev_from(v.y, vr.y), sh)),
+                                __float2ll_rn(ldexpf(dev_from(v.z, vr.z), sh))};
+              const unsigned act = __activemask(), same = __match_any_sync(act, g);
+              if (same == act) {  // integer sums: any order gives the same result
+                for (int o = 16; o > 0; o >>= 1)
+                  for (int c3 = 0; c3 < 3; ++c3) q[c3] += __shfl_xor_sync(act, q[c3], o);
+                if ((threadIdx.x & 31) == __ffs(act) - 1)
+                  for (int c3 = 0; c3 < 3; ++c3) atomicAdd(&s_acc[g][c3], (unsigned long long)q[c3]);
+              } else {
+                for (int c3 = 0; c3 < 3; ++c3) atomicAdd(&s_acc[g][c3], (unsigned long long)q[c3]);
+              }
             }
           }
           __syncthreads();

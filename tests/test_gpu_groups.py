@@ -112,6 +112,37 @@ def test_corner_cluster_with_distinct_velocities(pbf, oracle, cuda, niter):
     check_fp64(oracle, p, *box, pos, vel, got, conditioned=False)
 
 
+@pytest.mark.parametrize("niter", [1, 3])
+def test_grouped_cells_with_nonfinite_neighbours(pbf, oracle, cuda, niter):
+    """Isolated clusters plus particles with NaN or infinite velocities next
+    to them: the reference's NaN poisoning then reaches the clusters' windows
+    and the exact rules run per group.  The non-finite entries of positions,
+    velocities and densities match the FP64 oracle's exactly; finite
+    positions within 1e-5 h + 3x the reference-order float port's error."""
+    pos, vel = clustered(pbf, seed=6, touching=False)
+    rng = np.random.default_rng(7)
+    for c in [(0.65, 0.65, 0.15), (0.72, 0.72, 0.72)]:
+        near = np.zeros((3, 4), np.float32)
+        near[:, :3] = np.asarray(c) + rng.uniform(-0.05, 0.05, size=(3, 3))
+        bad = np.zeros((3, 4), np.float32)
+        bad[:, :3] = [[np.nan, 0.0, 0.0], [np.inf, 0.0, 0.0], [0.0, -np.inf, np.nan]]
+        pos = np.concatenate([pos, near])
+        vel = np.concatenate([vel, bad])
+    p = ref_params(pbf, niter)
+    box = ((0.8, 0.8, 0.8), (0.0, 0.0, 0.0))
+    got = gpu_step(pbf, p, *box, pos, vel)
+    iid = np.arange(len(pos), dtype=np.uint32)
+    r = oracle.step(p, *box, pos.astype(np.float64), vel.astype(np.float64), iid, "f64")
+    np.testing.assert_array_equal(got["iid"], r["iid"])
+    for k in ("npos", "nvel"):
+        np.testing.assert_array_equal(np.isfinite(got[k][:, :3]), np.isfinite(r[k][:, :3]), err_msg=k)
+    np.testing.assert_array_equal(np.isfinite(got["rho"]), np.isfinite(r["rho"]))
+    fin = np.isfinite(r["npos"][:, :3])
+    r32 = oracle.step(p, *box, pos, vel, iid, "f32")
+    port = np.abs(r32["npos"][:, :3][fin] - r["npos"][:, :3][fin]).max()
+    assert np.abs(got["npos"][:, :3][fin] - r["npos"][:, :3][fin]).max() <= TOL_X + 3 * port
+
+
 def test_grouped_cells_deterministic(pbf, cuda):
     pos, vel = clustered(pbf, seed=2)
     p = ref_params(pbf, 4)
