@@ -168,21 +168,25 @@ pbf_status pbf_profile_read(pbf_solver* s, pbf_step_profile* out);
 pbf_status pbf_use_graphs(pbf_solver* s, int on);
 
 /*
- * Reverse pass (adjoint) of a step, for differentiating through the solver.
- * No counterpart in the reference.  With the tape on, every pbf_step also
- * records what its reverse pass needs (positions entering each solver
- * iteration, each iteration's lambda; about (niter + 1) * 16 + niter * 4
- * bytes per particle, allocated here once).  pbf_backward then takes the
- * adjoints of the last step's outputs npos and nvel (device, n float4, the
- * step's output cell order) and writes the adjoints of its inputs pos and vel
- * (device, n float4, the step's input order) and of the box limits (g_lim:
- * device, 6 floats: ulim xyz then llim xyz, through the wall clamp).  The
- * neighbour sets and clamp states of the forward are held fixed; states must
- * be finite and k_boundaryDensity 0.  A multi-step rollout is differentiated
- * by re-running each step with the tape on (from a saved input state) just
- * before its reverse pass.
+ * Reverse pass (adjoint) of steps, for differentiating through the solver.
+ * No counterpart in the reference.  pbf_tape_enable(s, depth) with depth > 0
+ * turns the tape on as an empty stack of up to `depth` taped steps (at most
+ * 1024; 0 turns it off): every following pbf_step pushes what its reverse
+ * pass needs (positions entering each solver iteration and the final ones,
+ * each iteration's lambda, the sorted inputs, the last density, the sort
+ * permutation and the cell prefix: about (niter + 1) * 16 + niter * 4 + 28
+ * bytes per particle plus 4 per cell, allocated here), and fails with
+ * PBF_ERR_CAPACITY when the stack is full.  pbf_backward pops the most
+ * recent taped step: it takes the adjoints of that step's outputs npos and
+ * nvel (device, n float4, the step's output cell order) and writes the
+ * adjoints of its inputs pos and vel (device, n float4, the step's input
+ * order) and of the box limits (g_lim: device, 6 floats: ulim xyz then llim
+ * xyz, through the wall clamp).  The neighbour sets and clamp states of the
+ * forward are held fixed; k_boundaryDensity must be 0.  A rollout is
+ * differentiated by taping a run of steps and popping them in reverse order
+ * (checkpointing: re-run a segment from a saved state with the tape on).
  */
-pbf_status pbf_tape_enable(pbf_solver* s, int on);
+pbf_status pbf_tape_enable(pbf_solver* s, int depth);
 pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, void* g_pos,
                         void* g_vel, float* g_lim, void* stream);
 

@@ -45,16 +45,18 @@ class Problem:
         return (float(np.float32(self.wall_x(amp, k))), self.box[1], self.box[2]), (0.0, 0.0, 0.0)
 
 
-def rollout(pb: Problem, vel0: np.ndarray, amp: float):
-    """Chained FP64 steps; returns the per-step inputs and the final state."""
-    pos = np.asarray(pb.pos0, np.float64).copy()
+def rollout(pb: Problem, vel0: np.ndarray, amp: float, prec: str = "f64"):
+    """Chained steps (FP64, or "f32": the reference-order float port); returns
+    the per-step inputs and the final state."""
+    dt = np.float64 if prec == "f64" else np.float32
+    pos = np.asarray(pb.pos0, dt).copy()
     vel = np.zeros_like(pos)
     vel[:, :3] = vel0
     iid = np.arange(len(pos), dtype=np.uint32)
     hist = []
     for k in range(pb.steps):
         hist.append((pos, vel, iid))
-        r = oracle.step(pb.params, *pb.limits(amp, k), pos, vel, iid, "f64")
+        r = oracle.step(pb.params, *pb.limits(amp, k), pos, vel, iid, prec)
         pos, vel, iid = r["npos"], r["nvel"], r["iid"]
     return hist, pos, vel, iid
 
@@ -69,9 +71,9 @@ def loss(pb: Problem, vel0: np.ndarray, amp: float, target: np.ndarray) -> float
     return float((r * r).sum())
 
 
-def loss_and_grad(pb: Problem, vel0: np.ndarray, amp: float, target: np.ndarray):
+def loss_and_grad(pb: Problem, vel0: np.ndarray, amp: float, target: np.ndarray, prec: str = "f64"):
     """(loss, d loss / d v0 (n x 3, initial order), d loss / d A)."""
-    hist, pos, _, _ = rollout(pb, vel0, amp)
+    hist, pos, _, _ = rollout(pb, vel0, amp, prec)
     r = density(pb, pos) - target
     h = float(np.float32(pb.params.h))
     gp = oracle.density_grid_backward(pos, (0.0, 0.0, 0.0), pb.box, pb.dims, h, 2.0 * r)
@@ -79,7 +81,7 @@ def loss_and_grad(pb: Problem, vel0: np.ndarray, amp: float, target: np.ndarray)
     g_amp = 0.0
     for k in range(pb.steps - 1, -1, -1):
         pi, vi, ii = hist[k]
-        g = oracle.step_backward(pb.params, *pb.limits(amp, k), pi, vi, ii, gp, gv, "f64")
+        g = oracle.step_backward(pb.params, *pb.limits(amp, k), pi, vi, ii, gp, gv, prec)
         gp, gv = g["pos"], g["vel"]
         g_amp += g["ulim"][0] * pb.dwall_damp(k)
     return float((r * r).sum()), gv[:, :3], g_amp

@@ -13,9 +13,10 @@ Building blocks, all on the GPU through the C ABI:
 On top of them:
 
 * ``Rollout`` — T chained steps with checkpoints every K steps.  The reverse
-  sweep re-runs each K-step segment from its checkpoint, keeping the
-  segment's states, then re-runs every step of it with the tape on and calls
-  the step's reverse pass, last step first.  Memory: T/K + K states.
+  sweep re-runs each K-step segment from its checkpoint with the tape on (a
+  stack of K taped steps) and pops the steps' reverse passes, last step
+  first.  Each step runs twice forward and once backward; memory: T/K
+  checkpoints + K tape records.
 * ``step`` — one step as a ``torch.autograd.Function`` (its backward re-runs
   the step from saved copies of its inputs with the tape on).
 * ``DensityGrid`` — the density grid as a ``torch.autograd.Function``.
@@ -96,6 +97,7 @@ class _Step(torch.autograd.Function):
         p, v, i = pos.detach().clone(), vel.detach().clone(), iid.clone()
         npos = torch.empty_like(p)
         nvel = torch.empty_like(v)
+        sim.tape(0)
         sim.setLim(*lims)
         sim.step(p, npos, v, nvel, i, n)
         ctx.mark_non_differentiable(i)
@@ -110,10 +112,11 @@ class _Step(torch.autograd.Function):
         g_nvel = torch.zeros_like(vel) if g_nvel is None else g_nvel.contiguous()
         npos = torch.empty_like(pos)
         nvel = torch.empty_like(vel)
-        sim.tape(True)
+        sim.tape(1)
         sim.setLim(*ctx.lims)
         sim.step(pos, npos, vel, nvel, iid, n)
         g_pos, g_vel, g_lim = sim.backward(g_npos, g_nvel)
+        sim.tape(0)
         return None, g_pos, g_vel, None, g_lim[:3].cpu(), g_lim[3:].cpu()
 
 
@@ -135,8 +138,9 @@ class Rollout:
     state.  ``backward(g_pos, g_vel)`` takes the adjoints of that final state
     (in its order) and returns the adjoints of the initial pos and vel (in
     their order) and a (steps, 6) tensor of the limits' adjoints per step
-    (ulim xyz, llim xyz).  Every step runs with the tape on so that the
-    solver's CUDA graph stays the same across the sweeps.
+    (ulim xyz, llim xyz).  The forward runs with the tape off; the reverse
+    sweep re-runs each segment from its checkpoint with a tape of ``every``
+    steps and pops their reverse passes.
     """
 
     def __init__(self, sim: Simulator, every: int = 10):
@@ -148,7 +152,6 @@ class Rollout:
         self._steps = 0
         self._limits: Optional[Callable[[int], Limits]] = None
         self._n = 0
-        sim.tape(True)
 
     def _advance(self, pos, vel, iid, k):
         """One step from (pos, vel, iid), which it leaves permuted; returns the new state."""
@@ -165,6 +168,7 @@ class Rollout:
         self._steps = int(steps)
         self._limits = limits
         self._ckpt = []
+        self.sim.tape(0)
         pos, vel, iid = pos.clone(), vel.clone(), iid.clone()
         for k in range(self._steps):
             if k % self.every == 0:
@@ -176,18 +180,15 @@ class Rollout:
         g_pos = g_pos.contiguous().clone()
         g_vel = g_vel.contiguous().clone()
         g_lim = torch.zeros((self._steps, 6), dtype=torch.float32, device=g_pos.device)
+        self.sim.tape(self.every)
         for seg in range(len(self._ckpt) - 1, -1, -1):
             start = seg * self.every
             end = min(start + self.every, self._steps)
-            states = []
             pos, vel, iid = (t.clone() for t in self._ckpt[seg])
             for k in range(start, end):
-                states.append((pos.clone(), vel.clone(), iid.clone()))
-                if k + 1 < end:
-                    pos, vel, iid = self._advance(pos, vel, iid, k)
+                pos, vel, iid = self._advance(pos, vel, iid, k)
             for k in range(end - 1, start - 1, -1):
-                pos, vel, iid = states[k - start]
-                self._advance(pos, vel, iid, k)
                 g_pos, g_vel, gl = self.sim.backward(g_pos, g_vel)
                 g_lim[k] = gl
+        self.sim.tape(0)
         return g_pos, g_vel, g_lim

@@ -38,6 +38,8 @@ namespace pbf {
 namespace {
 
 constexpr int kThreads = 128;
+// Below this many particles a warp shares each particle (see lane_sum).
+constexpr int kWarpPerParticleBelow = 131072;
 
 __device__ __forceinline__ void column_run(const SceneGeom& g, const uint32_t* __restrict__ cs,
                                            int n, int x, int y, int z, int& s, int& e) {
@@ -47,10 +49,11 @@ __device__ __forceinline__ void column_run(const SceneGeom& g, const uint32_t* _
   e = max(min((int)__ldg(cs + base + zhi + 1), n), s);
 }
 
-// f(j) for every candidate of the window of cell q, in order.
+// f(j) for every candidate of the window of cell q, in order; with stride L,
+// lane `lane` takes every L-th candidate of each run.
 template <class F>
 __device__ __forceinline__ void for_window(const SceneGeom& g, const uint32_t* __restrict__ cs,
-                                           int n, int3 q, F&& f) {
+                                           int n, int3 q, F&& f, int lane = 0, int stride = 1) {
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
     if (x < 0 || x >= g.dims[0]) continue;
@@ -59,7 +62,7 @@ __device__ __forceinline__ void for_window(const SceneGeom& g, const uint32_t* _
       if (y < 0 || y >= g.dims[1]) continue;
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
-      for (int j = s; j < e; ++j) f(j);
+      for (int j = s + lane; j < e; j += stride) f(j);
     }
   }
 }
@@ -96,6 +99,22 @@ __device__ __forceinline__ void atomic_add3(float4* p, float x, float y, float z
   atomicAdd(&p->z, z);
 }
 
+// L lanes share one particle (L = 1, or a whole warp for small steps, where
+// one thread per particle would leave most SMs idle): its lanes split the
+// window and add their sums in a fixed tree, so lane 0 holds the result.
+template <int L>
+__device__ __forceinline__ float lane_sum(float v) {
+  if constexpr (L > 1) {
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
+template <int L>
+__device__ __forceinline__ Vec lane_sum(Vec v) {
+  return {lane_sum<L>(v.x), lane_sum<L>(v.y), lane_sum<L>(v.z)};
+}
+
 // phi(s) and phi'(s) / s of the spiky gradient F = phi r (|r| = s).
 __device__ __forceinline__ void spiky_parts(const StepConsts& c, float s, float& phi, float& k) {
   const float d = c.h - s;
@@ -119,10 +138,12 @@ k_bwd_cells(BackwardArgs a, const float4* __restrict__ X, unsigned long long* __
 
 // ---- XSPH and the velocity update --------------------------------------------------
 
+template <int L>
 __global__ void __launch_bounds__(kThreads)
 k_bwd_xsph(BackwardArgs a) {
   const StepConsts& c = a.c;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = t / L, lane = t % L;
   if (i >= a.n) return;
   const float4 xi = ld4(a.XK, i), x0i = ld4(a.xs, i), gi = ld4(a.g_nvel, i);
   const float4 vi = make_float4((xi.x - x0i.x) * c.inv_dt, (xi.y - x0i.y) * c.inv_dt,
@@ -130,7 +151,7 @@ k_bwd_xsph(BackwardArgs a) {
   const float ri = a.rho[i];
   const unsigned long long gci = a.gcell[i];
   const SceneGeom g = geom_of(c, a.G, i);
-  Vec vb = {gi.x, gi.y, gi.z}, xb = {0.f, 0.f, 0.f};
+  Vec vb = {0.f, 0.f, 0.f}, xb = {0.f, 0.f, 0.f};
   float rb = 0.f;
   for_window(g, a.cs, a.n, cell_of(c, g, xi), [&](int j) {
     if (j == i) return;
@@ -172,7 +193,12 @@ k_bwd_xsph(BackwardArgs a) {
       atomic_add3(a.fix + j, -own * dq * r.x, -own * dq * r.y, -own * dq * r.z);
       atomicAdd(&a.fix[j].w, own * dr);
     }
-  });
+  }, lane, L);
+  vb = lane_sum<L>(vb);
+  xb = lane_sum<L>(xb);
+  rb = lane_sum<L>(rb);
+  if (lane != 0) return;
+  vb = {gi.x + vb.x, gi.y + vb.y, gi.z + vb.z};  // nv_i = v_i + ...: the identity part
   // v = (X_K - X0) / dt: the position adjoint of the step's output plus XSPH's
   const float4 gp = ld4(a.g_npos, i);
   a.gx[i] = make_float4(gp.x + xb.x + vb.x * c.inv_dt, gp.y + xb.y + vb.y * c.inv_dt,
@@ -213,17 +239,19 @@ k_bwd_fix(BackwardArgs a) {
 // Recomputes P_i (the forward's sum), applies the clamps' transposes.  Writes
 // Pbar, starts the X_k adjoint with ubar, and adds this block's wall
 // adjoints to wall_part[block][6] (ulim xyz, llim xyz).
+template <int L>
 __global__ void __launch_bounds__(kThreads)
 k_bwd_dp1(BackwardArgs a, const float4* __restrict__ X, const float* __restrict__ lam) {
   const StepConsts& c = a.c;
   __shared__ float wall[6][kThreads];
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / L, lane = tid % L;
   float w6[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float Px = 0.f, Py = 0.f, Pz = 0.f;
   if (i < a.n) {
     const float4 xi = ld4(X, i);
     const float li = lam[i];
     const SceneGeom g = geom_of(c, a.G, i);
-    float Px = 0.f, Py = 0.f, Pz = 0.f;
     for_window(g, a.cs, a.n, cell_of(c, g, xi), [&](int j) {
       const float4 xj = ld4(X, j);
       const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
@@ -237,7 +265,14 @@ k_bwd_dp1(BackwardArgs a, const float4* __restrict__ X, const float* __restrict_
         Py = fmaf(f, ey, Py);
         Pz = fmaf(f, ez, Pz);
       }
-    });
+    }, lane, L);
+    Px = lane_sum<L>(Px);
+    Py = lane_sum<L>(Py);
+    Pz = lane_sum<L>(Pz);
+  }
+  if (i < a.n && lane == 0) {
+    const float4 xi = ld4(X, i);
+    const SceneGeom g = geom_of(c, a.G, i);
     const float4 gn = ld4(a.gx, i);  // adjoint of X_{k+1}
     const float P[3] = {Px, Py, Pz}, x[3] = {xi.x, xi.y, xi.z}, gin[3] = {gn.x, gn.y, gn.z};
     float ub[3], pb[3];
@@ -263,15 +298,17 @@ k_bwd_dp1(BackwardArgs a, const float4* __restrict__ X, const float* __restrict_
   __syncthreads();
   if (threadIdx.x < 6) {
     float sum = 0.f;
-    for (int t = 0; t < kThreads; ++t) sum += wall[threadIdx.x][t];
+    for (int k = 0; k < kThreads; ++k) sum += wall[threadIdx.x][k];
     a.wall_part[blockIdx.x * 6 + threadIdx.x] = sum;
   }
 }
 
+template <int L>
 __global__ void __launch_bounds__(kThreads)
 k_bwd_dp2(BackwardArgs a, const float4* __restrict__ X, const float* __restrict__ lam) {
   const StepConsts& c = a.c;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / L, lane = tid % L;
   if (i >= a.n) return;
   const float4 xi = ld4(X, i), pbi4 = ld4(a.pbar, i);
   const Vec pbi = {pbi4.x, pbi4.y, pbi4.z};
@@ -317,7 +354,10 @@ k_bwd_dp2(BackwardArgs a, const float4* __restrict__ X, const float* __restrict_
       atomic_add3(a.fix + j, -oi.x, -oi.y, -oi.z);
       atomicAdd(&a.fix[j].w, fi);
     }
-  });
+  }, lane, L);
+  xb = lane_sum<L>(xb);
+  lb = lane_sum<L>(lb);
+  if (lane != 0) return;
   const float4 u = ld4(a.gx_next, i);
   a.gx_next[i] = make_float4(u.x + xb.x, u.y + xb.y, u.z + xb.z, 0.f);
   a.lbar[i] = lb;
@@ -325,10 +365,12 @@ k_bwd_dp2(BackwardArgs a, const float4* __restrict__ X, const float* __restrict_
 
 // ---- lambda ------------------------------------------------------------------------
 
+template <int L>
 __global__ void __launch_bounds__(kThreads)
 k_bwd_lam1(BackwardArgs a, const float4* __restrict__ X, const float* __restrict__ lam, int last) {
   const StepConsts& c = a.c;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / L, lane = tid % L;
   if (i >= a.n) return;
   const float4 xi = ld4(X, i);
   const SceneGeom g = geom_of(c, a.G, i);
@@ -346,7 +388,12 @@ k_bwd_lam1(BackwardArgs a, const float4* __restrict__ X, const float* __restrict
       gz += sc * ez;
       if (j != i) gl2 += dist2(sc * ex, sc * ey, sc * ez);
     }
-  });
+  }, lane, L);
+  gx = lane_sum<L>(gx);
+  gy = lane_sum<L>(gy);
+  gz = lane_sum<L>(gz);
+  gl2 = lane_sum<L>(gl2);
+  if (lane != 0) return;
   const float D = gl2 + dist2(gx, gy, gz) + c.lambda_eps;
   const float lb = a.lbar[i];
   const float cbar = -lb / D;
@@ -355,10 +402,12 @@ k_bwd_lam1(BackwardArgs a, const float4* __restrict__ X, const float* __restrict
   a.rtot[i] = (last ? a.grho[i] : 0.f) + cbar / c.pho0;
 }
 
+template <int L>
 __global__ void __launch_bounds__(kThreads)
 k_bwd_lam2(BackwardArgs a, const float4* __restrict__ X) {
   const StepConsts& c = a.c;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = tid / L, lane = tid % L;
   if (i >= a.n) return;
   const float4 xi = ld4(X, i), gsi = ld4(a.gs, i);
   const float rti = a.rtot[i];
@@ -411,7 +460,9 @@ k_bwd_lam2(BackwardArgs a, const float4* __restrict__ X) {
       }
     }
     if (!recip) atomic_add3(a.fix + j, sx, sy, sz);
-  });
+  }, lane, L);
+  xb = lane_sum<L>(xb);
+  if (lane != 0) return;
   const float4 u = ld4(a.gx_next, i);
   a.gx_next[i] = make_float4(u.x + xb.x, u.y + xb.y, u.z + xb.z, 0.f);
 }
@@ -544,31 +595,22 @@ cudaError_t density_grid_backward(const float4* pos, int n, const float lo[3], c
   return cudaGetLastError();
 }
 
-cudaError_t backward(const BackwardArgs& args, const BackwardTape& t, const uint32_t* perm,
-                     const void* g_npos, const void* g_nvel, void* g_pos, void* g_vel,
-                     float* g_lim, cudaStream_t stream) {
-  BackwardArgs a = args;
-  a.g_npos = (const float4*)g_npos;
-  a.g_nvel = (const float4*)g_nvel;
-  const int blocks = (a.n + kThreads - 1) / kThreads;
-  cudaError_t e = cudaMemsetAsync(g_lim, 0, sizeof(float) * 6, stream);
-  if (e != cudaSuccess) return e;
-  a.XK = t.X[t.niter];
-  a.X0 = t.X[0];
+template <int L>
+cudaError_t run_backward(BackwardArgs a, const BackwardTape& t, const uint32_t* perm, void* g_pos,
+                         void* g_vel, float* g_lim, cudaStream_t stream) {
+  const int blocks = (int)(((long long)a.n * L + kThreads - 1) / kThreads);
   const int blocks256 = (a.n + 255) / 256;
-  k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.X0, a.gcell);
-  k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.XK, a.kcell);
-  k_bwd_xsph<<<blocks, kThreads, 0, stream>>>(a);
+  k_bwd_xsph<L><<<blocks, kThreads, 0, stream>>>(a);
   k_bwd_fix_xsph<<<blocks256, 256, 0, stream>>>(a);
   for (int k = t.niter - 1; k >= 0; --k) {
     const float4* X = t.X[k];
     const float* lam = t.lambda[k];
-    k_bwd_dp1<<<blocks, kThreads, 0, stream>>>(a, X, lam);  // also the packed cells of X_k
+    k_bwd_dp1<L><<<blocks, kThreads, 0, stream>>>(a, X, lam);  // also the packed cells of X_k
     k_bwd_wall<<<1, 32, 0, stream>>>(a.wall_part, blocks, g_lim);
-    k_bwd_dp2<<<blocks, kThreads, 0, stream>>>(a, X, lam);
+    k_bwd_dp2<L><<<blocks, kThreads, 0, stream>>>(a, X, lam);
     k_bwd_fix<true><<<blocks256, 256, 0, stream>>>(a);
-    k_bwd_lam1<<<blocks, kThreads, 0, stream>>>(a, X, lam, k == t.niter - 1);
-    k_bwd_lam2<<<blocks, kThreads, 0, stream>>>(a, X);
+    k_bwd_lam1<L><<<blocks, kThreads, 0, stream>>>(a, X, lam, k == t.niter - 1);
+    k_bwd_lam2<L><<<blocks, kThreads, 0, stream>>>(a, X);
     k_bwd_fix<false><<<blocks256, 256, 0, stream>>>(a);
     // the adjoint of X_k becomes the input of the next (earlier) iteration
     float4* tmp = a.gx;
@@ -577,6 +619,25 @@ cudaError_t backward(const BackwardArgs& args, const BackwardTape& t, const uint
   }
   k_bwd_out<<<(a.n + 255) / 256, 256, 0, stream>>>(a, perm, (float4*)g_pos, (float4*)g_vel);
   return cudaGetLastError();
+}
+
+
+cudaError_t backward(const BackwardArgs& args, const BackwardTape& t, const uint32_t* perm,
+                     const void* g_npos, const void* g_nvel, void* g_pos, void* g_vel,
+                     float* g_lim, cudaStream_t stream) {
+  BackwardArgs a = args;
+  a.g_npos = (const float4*)g_npos;
+  a.g_nvel = (const float4*)g_nvel;
+  cudaError_t e = cudaMemsetAsync(g_lim, 0, sizeof(float) * 6, stream);
+  if (e != cudaSuccess) return e;
+  a.XK = t.X[t.niter];
+  a.X0 = t.X[0];
+  const int blocks256 = (a.n + 255) / 256;
+  k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.X0, a.gcell);
+  k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.XK, a.kcell);
+  if (a.n < kWarpPerParticleBelow)
+    return run_backward<32>(a, t, perm, g_pos, g_vel, g_lim, stream);
+  return run_backward<1>(a, t, perm, g_pos, g_vel, g_lim, stream);
 }
 
 }  // namespace pbf

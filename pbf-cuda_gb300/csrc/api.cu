@@ -22,6 +22,9 @@
 enum { kEvStart, kEvGrid, kEvReorder, kEvXsphStart, kEvEnd, kEvFixed };
 constexpr int kMaxProfiledIters = 64;
 
+// Taped steps a solver's tape can hold (pbf_tape_enable).
+constexpr int kMaxTapeDepth = 1024;
+
 struct pbf_solver {
   pbf_params params;
   float ulim[3], llim[3];
@@ -43,17 +46,23 @@ struct pbf_solver {
   bool use_graph;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
-  // tape of the last step and the reverse pass's scratch (pbf_tape_enable)
-  bool tape;
-  bool tape_valid;
-  int tape_iters;            // iterations the tape buffers hold
-  float4* tape_x;            // (tape_iters + 1) * max_particles
-  float* tape_l;             // tape_iters * max_particles
+  // the tape (pbf_tape_enable): a stack of taped steps, each record holding
+  // what the step's reverse pass needs, and the reverse pass's scratch
+  int tape_depth;            // records the stack holds; 0: tape off
+  int tape_top;              // records on the stack
+  int tape_cap;              // records allocated
+  int tape_iters;            // iterations a record holds
+  size_t tape_rec;           // bytes per record
+  unsigned char* tape_mem;   // tape_cap records
+  struct TapeMeta {
+    pbf::StepConsts c;
+    int n;
+    int niter;
+  } tape_meta[kMaxTapeDepth];
   float4* bw4;               // 7 * max_particles: gx, gx_next, gx0, pbar, gs, fix, fixv
   float* bw1;                // 4 * max_particles: grho, lbar, rtot (+ spare)
   unsigned long long* bw8;   // 2 * max_particles: packed grid cells, packed current cells
   float* wall_part;          // 6 * blocks
-  pbf::StepConsts last_c;
   const uint32_t* last_perm;
 };
 
@@ -214,6 +223,24 @@ cudaError_t alloc(T** p, size_t count) {
   return cudaMalloc((void**)p, sizeof(T) * (count ? count : 1));
 }
 
+// Layout of one tape record (256-byte aligned parts): positions entering each
+// iteration and the final ones X[0..iters], each iteration's lambda, the
+// sorted inputs, the last lambda pass's density, the sort permutation and the
+// grid's cell prefix.
+struct TapeLayout {
+  size_t x, l, xs, rho, perm, cs, bytes;
+  TapeLayout(size_t np, size_t cells1, int iters) {
+    auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+    x = 0;
+    l = x + up(sizeof(float4) * np * (iters + 1));
+    xs = l + up(sizeof(float) * np * iters);
+    rho = xs + up(sizeof(float4) * np);
+    perm = rho + up(sizeof(float) * np);
+    cs = perm + up(sizeof(uint32_t) * np);
+    bytes = cs + up(sizeof(uint32_t) * cells1);
+  }
+};
+
 // Group tables for up to max_particles particles (pbf_internal.cuh).
 cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
   const size_t slots = pbf::group_slots(max_particles);
@@ -245,7 +272,7 @@ void free_all(pbf_solver* s) {
     if (e) cudaEventDestroy(e);
   if (s->exec) cudaGraphExecDestroy(s->exec);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
-  void* tape[] = {s->tape_x, s->tape_l, s->bw4, s->bw1, s->bw8, s->wall_part};
+  void* tape[] = {s->tape_mem, s->bw4, s->bw1, s->bw8, s->wall_part};
   for (void* p : tape)
     if (p) cudaFree(p);
 }
@@ -421,9 +448,9 @@ struct StepPlan {
   int niter;
   cudaEvent_t* ev;     // [kEvFixed] or null
   cudaEvent_t* ev_it;  // [3 * kMaxProfiledIters] or null
-  float4* tape_x;      // record the step for its reverse pass (null: do not)
-  float* tape_l;
-  int tape_stride;     // particles per tape slot
+  unsigned char* tape;  // the tape record this step fills (null: not taped)
+  size_t tape_x, tape_l, tape_xs, tape_rho, tape_perm, tape_cs;  // its parts (byte offsets)
+  int tape_stride;     // particles per part slot
   const uint32_t** perm_out;  // receives the step's sort permutation
 };
 
@@ -457,9 +484,11 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
            "pbf_step: reorder");
   PBF_EV(P.ev[kEvReorder]);
   const size_t ts = (size_t)P.tape_stride;
+  float4* tape_x = P.tape ? (float4*)(P.tape + P.tape_x) : nullptr;
+  float* tape_l = P.tape ? (float*)(P.tape + P.tape_l) : nullptr;
 #define PBF_TAPE(dst, src, bytes) \
-  if (P.tape_x) PBF_CUDA(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st_), "pbf_step: tape")
-  PBF_TAPE(P.tape_x, P.sol->xa, sizeof(float4) * n);
+  if (P.tape) PBF_CUDA(cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToDevice, st_), "pbf_step: tape")
+  PBF_TAPE(tape_x, P.sol->xa, sizeof(float4) * n);
   // niter x correctDensity (fluids/Simulator.cpp:55-60), Jacobi ping-pong;
   // updateVelocity fused into the last position update (fluids/Simulator.cpp:62-66)
   const uint32_t* cs = P.grid->cell_start;
@@ -469,11 +498,11 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
   for (int it = 0; it < niter; ++it) {
     if (it < piters) PBF_EV(P.ev_it[3 * it]);
     PBF_CUDA(pbf::launch_lambda(c, G, X, cs, n, sol, 2 * it, st_), "pbf_step: lambda");
-    PBF_TAPE(P.tape_l + ts * it, sol.lambda, sizeof(float) * n);
+    PBF_TAPE(tape_l + ts * it, sol.lambda, sizeof(float) * n);
     if (it < piters) PBF_EV(P.ev_it[3 * it + 1]);
     if (it + 1 < niter) {
       PBF_CUDA(pbf::launch_delta_p(c, G, X, cs, n, sol, 2 * it + 1, T, st_), "pbf_step: delta_p");
-      PBF_TAPE(P.tape_x + ts * (it + 1), T, sizeof(float4) * n);
+      PBF_TAPE(tape_x + ts * (it + 1), T, sizeof(float4) * n);
       float4* t = X;
       X = T;
       T = t;
@@ -481,7 +510,7 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
       PBF_CUDA(pbf::launch_delta_p_final(c, G, X, cs, n, sol, 2 * it + 1, (float4*)pos,
                                          (float4*)npos, (float4*)vel, iid, st_),
                "pbf_step: delta_p");
-      PBF_TAPE(P.tape_x + ts * (it + 1), npos, sizeof(float4) * n);
+      PBF_TAPE(tape_x + ts * (it + 1), npos, sizeof(float4) * n);
     }
     if (it < piters) PBF_EV(P.ev_it[3 * it + 2]);
   }
@@ -491,6 +520,11 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
                             (float4*)nvel, st_),
            "pbf_step: xsph");
   PBF_EV(P.ev[kEvEnd]);
+  // the rest of the record: sorted inputs, last density, permutation, cell prefix
+  PBF_TAPE(P.tape + P.tape_xs, P.sol->xs, sizeof(float4) * n);
+  PBF_TAPE(P.tape + P.tape_rho, P.sol->rho, sizeof(float) * n);
+  PBF_TAPE(P.tape + P.tape_perm, perm, sizeof(uint32_t) * n);
+  PBF_TAPE(P.tape + P.tape_cs, P.grid->cell_start, sizeof(uint32_t) * (c.cells + 1));
 #undef PBF_EV
 #undef PBF_TAPE
   return PBF_OK;
@@ -566,15 +600,21 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   P.niter = s->params.niter;
   P.ev = prof ? s->ev : nullptr;
   P.ev_it = prof ? s->ev_it : nullptr;
-  const bool taping = s->tape && s->params.niter <= s->tape_iters;
-  if (s->tape && !taping)
-    return fail(PBF_ERR_CAPACITY, "tape holds %d iterations, params ask for %d (re-enable the tape)",
+  const bool taping = s->tape_depth > 0;
+  if (taping && s->params.niter > s->tape_iters)
+    return fail(PBF_ERR_CAPACITY, "tape records hold %d iterations, params ask for %d (re-enable the tape)",
                 s->tape_iters, s->params.niter);
-  P.tape_x = taping ? s->tape_x : nullptr;
-  P.tape_l = taping ? s->tape_l : nullptr;
+  if (taping && s->params.k_boundaryDensity != 0.f)
+    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
+  if (taping && s->tape_top >= s->tape_depth)
+    return fail(PBF_ERR_CAPACITY, "the tape holds %d taped steps: run pbf_backward or re-enable the tape",
+                s->tape_depth);
+  const TapeLayout tl((size_t)s->max_particles, (size_t)s->max_cells + 1, s->tape_iters);
+  P.tape = taping ? s->tape_mem + tl.bytes * (size_t)s->tape_top : nullptr;
+  P.tape_x = tl.x, P.tape_l = tl.l, P.tape_xs = tl.xs, P.tape_rho = tl.rho, P.tape_perm = tl.perm;
+  P.tape_cs = tl.cs;
   P.tape_stride = s->max_particles;
   P.perm_out = &s->last_perm;
-  s->tape_valid = false;
   const pbf::StepConsts& c = P.c;
   st = s->use_graph ? launch_step_graph(P, s->cap_stream, &s->exec, pos, npos, vel, nvel, iid, n, st_)
                     : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
@@ -584,68 +624,76 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
-  s->last_c = c;
-  s->tape_valid = taping;
+  if (taping) {
+    s->tape_meta[s->tape_top] = {c, n, niter};
+    ++s->tape_top;
+  }
   return PBF_OK;
 }
 
-pbf_status pbf_tape_enable(pbf_solver* s, int on) {
+pbf_status pbf_tape_enable(pbf_solver* s, int depth) {
   if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
-  if (!on) {
-    s->tape = false;
+  s->tape_top = 0;
+  if (depth <= 0) {
+    s->tape_depth = 0;
     return PBF_OK;
   }
+  s->tape_depth = 0;
   if (s->params.k_boundaryDensity != 0.f)
     return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
-  s->tape = true;
+  if (depth > kMaxTapeDepth) return fail(PBF_ERR_CAPACITY, "at most %d taped steps", kMaxTapeDepth);
   const int iters = s->params.niter;
   if (iters > pbf::kMaxTapeIters) return fail(PBF_ERR_CAPACITY, "at most %d taped iterations", pbf::kMaxTapeIters);
-  if (iters <= s->tape_iters) return PBF_OK;
-  void* old[] = {s->tape_x, s->tape_l, s->bw4, s->bw1, s->bw8, s->wall_part};
-  for (void* p : old)
-    if (p) cudaFree(p);
-  s->tape_x = nullptr;
-  s->tape_l = nullptr;
-  s->bw4 = nullptr;
-  s->bw1 = nullptr;
-  s->bw8 = nullptr;
-  s->wall_part = nullptr;
-  s->tape_iters = 0;
   const size_t np = (size_t)(s->max_particles > 0 ? s->max_particles : 1);
-  const size_t blocks = (np + 127) / 128;
-  cudaError_t e = alloc(&s->tape_x, np * (iters + 1));
-  if (e == cudaSuccess) e = alloc(&s->tape_l, np * iters);
-  if (e == cudaSuccess) e = alloc(&s->bw4, np * 7);
-  if (e == cudaSuccess) e = alloc(&s->bw1, np * 4);
-  if (e == cudaSuccess) e = alloc(&s->bw8, np * 2);
-  if (e == cudaSuccess) e = cudaMemset(s->bw4 + 5 * np, 0, sizeof(float4) * 2 * np);
-  if (e == cudaSuccess) e = alloc(&s->wall_part, blocks * 6);
-  if (e != cudaSuccess) {
-    s->tape = false;
-    cudaGetLastError();
-    return cuda_fail(e, "pbf_tape_enable");
+  if (!s->bw4) {
+    const size_t blocks = (np * 32 + 127) / 128;  // the reverse kernels' blocks at 32 lanes per particle
+    cudaError_t e = alloc(&s->bw4, np * 7);
+    if (e == cudaSuccess) e = alloc(&s->bw1, np * 4);
+    if (e == cudaSuccess) e = alloc(&s->bw8, np * 2);
+    if (e == cudaSuccess) e = cudaMemset(s->bw4 + 5 * np, 0, sizeof(float4) * 2 * np);
+    if (e == cudaSuccess) e = alloc(&s->wall_part, blocks * 6);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "pbf_tape_enable");
+    }
   }
-  s->tape_iters = iters;
+  if (depth > s->tape_cap || iters > s->tape_iters) {
+    if (s->tape_mem) cudaFree(s->tape_mem);
+    s->tape_mem = nullptr;
+    s->tape_cap = 0;
+    const int it = iters > s->tape_iters ? iters : s->tape_iters;
+    const int cap = depth > s->tape_cap ? depth : s->tape_cap;
+    const TapeLayout tl(np, (size_t)s->max_cells + 1, it);
+    cudaError_t e = alloc(&s->tape_mem, tl.bytes * (size_t)cap);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return cuda_fail(e, "pbf_tape_enable");
+    }
+    s->tape_iters = it;
+    s->tape_cap = cap;
+  }
+  s->tape_depth = depth;
   return PBF_OK;
 }
 
 pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, void* g_pos,
                         void* g_vel, float* g_lim, void* stream) {
   if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
-  if (!s->tape_valid) return fail(PBF_ERR_NOT_READY, "the last step was not taped");
-  if (s->params.k_boundaryDensity != 0.f)
-    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
+  if (s->tape_top <= 0) return fail(PBF_ERR_NOT_READY, "no taped step to reverse");
   if (!g_npos || !g_nvel || !g_pos || !g_vel || !g_lim) return fail(PBF_ERR_INVALID_ARG, "NULL buffer");
-  const int n = s->last_n;
+  const int slot = s->tape_top - 1;
+  const pbf_solver::TapeMeta& m = s->tape_meta[slot];
   const size_t np = (size_t)s->max_particles;
+  const TapeLayout tl(np, (size_t)s->max_cells + 1, s->tape_iters);
+  unsigned char* rec = s->tape_mem + tl.bytes * (size_t)slot;
   pbf::BackwardArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.c = s->last_c;
+  a.c = m.c;
   a.G = pbf::Geometry{nullptr, nullptr};
-  a.cs = s->grid.cell_start;
-  a.n = n;
-  a.xs = s->sol.xs;
-  a.rho = s->sol.rho;
+  a.cs = (const uint32_t*)(rec + tl.cs);
+  a.n = m.n;
+  a.xs = (const float4*)(rec + tl.xs);
+  a.rho = (const float*)(rec + tl.rho);
   a.gx = s->bw4;
   a.gx_next = s->bw4 + np;
   a.gx0 = s->bw4 + 2 * np;
@@ -660,11 +708,15 @@ pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, v
   a.kcell = s->bw8 + np;
   a.wall_part = s->wall_part;
   pbf::BackwardTape t;
-  t.niter = s->params.niter;
-  for (int k = 0; k <= t.niter; ++k) t.X[k] = s->tape_x + np * k;
-  for (int k = 0; k < t.niter; ++k) t.lambda[k] = s->tape_l + np * k;
-  PBF_CUDA(pbf::backward(a, t, s->last_perm, g_npos, g_nvel, g_pos, g_vel, g_lim, (cudaStream_t)stream),
+  t.niter = m.niter;
+  float4* X = (float4*)(rec + tl.x);
+  float* L = (float*)(rec + tl.l);
+  for (int k = 0; k <= t.niter; ++k) t.X[k] = X + np * k;
+  for (int k = 0; k < t.niter; ++k) t.lambda[k] = L + np * k;
+  PBF_CUDA(pbf::backward(a, t, (const uint32_t*)(rec + tl.perm), g_npos, g_nvel, g_pos, g_vel, g_lim,
+                         (cudaStream_t)stream),
            "pbf_backward");
+  s->tape_top = slot;
   return PBF_OK;
 }
 
@@ -981,8 +1033,8 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   P.niter = b->params.niter;
   P.ev = nullptr;
   P.ev_it = nullptr;
-  P.tape_x = nullptr;
-  P.tape_l = nullptr;
+  P.tape = nullptr;
+  P.tape_x = P.tape_l = P.tape_xs = P.tape_rho = P.tape_perm = P.tape_cs = 0;
   P.tape_stride = 0;
   P.perm_out = nullptr;
   st = b->use_graph ? launch_step_graph(P, b->cap_stream, &b->exec, pos, npos, vel, nvel, iid, n, st_)

@@ -261,10 +261,8 @@ constexpr int kLaunchesPerPass = 3;
 
 constexpr int kMaxTapeIters = 64;
 
-// What a taped step keeps for its reverse pass: the positions entering every
-// iteration and the final ones (X[0] = x*, X[niter] = npos), and every
-// iteration's lambda.  The grid, the sorted inputs and the last rho stay in
-// the solver's scratch until the next step.
+// The positions entering every iteration and the final ones of a taped step
+// (X[0] = x*, X[niter] = npos), and every iteration's lambda.
 struct BackwardTape {
   int niter;
   float4* X[kMaxTapeIters + 1];

@@ -23,8 +23,10 @@
 // and returns; the dense kernel then gives each listed warp a block of
 // kDenseWarps warps, each walking one contiguous chunk of every lane's
 // window, and adds the chunks' partial sums in chunk order in shared memory.
-// Both orders are fixed, so results stay deterministic; they differ from the
-// reference's sequential sums only by rounding.
+// Steps of fewer than kDenseAllBelow particles send every warp to the dense
+// kernel (one thread per particle would leave most SMs idle).  Both orders
+// are fixed, so results stay deterministic; they differ from the reference's
+// sequential sums only by rounding.
 //
 // IEEE semantics follow the reference's: its kernels evaluate every
 // candidate of the window, so a NaN distance (from a NaN position) poisons
@@ -47,6 +49,9 @@ constexpr int kSparseThreads = 128;
 constexpr int kDenseWarps = 8;                  // chunks of a dense warp's windows
 constexpr int kDenseThreads = 32 * kDenseWarps;
 constexpr int kDenseWindow = 512;               // candidates above which a warp goes dense
+// Below this many particles one thread per particle leaves most of the GPU
+// idle: every warp then takes the dense kernel (8 warps per 32 particles).
+constexpr int kDenseAllBelow = 131072;
 constexpr int kMaxFields = 6;                   // partial-sum fields of the largest pass
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -61,6 +66,7 @@ struct PassArgs {
   int n;
   int counter;            // flags word holding this pass's dense-list length
   int next_counter;       // the other one, cleared for the next pass
+  int dense_all;          // every warp takes the dense kernel (small n)
   uint32_t* flags;
   uint32_t* dense;
   uint32_t* masks;        // neighbour masks: lambda saves them, delta_p reads them
@@ -639,6 +645,7 @@ __device__ __forceinline__ bool exact_path(int kind, const PassArgs& a, const Sc
 template <int kKind>
 __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
   using P = typename PassOf<kKind>::type;
+  if (a.dense_all) return;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = i < a.n;
   const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -672,9 +679,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   static_assert(P::kFields <= kMaxFields, "partial-sum fields");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
-  const uint32_t count = a.flags[a.counter];  // written by this pass's sparse kernel
+  // the warps the sparse kernel listed, or all of them
+  const uint32_t count = a.dense_all ? (uint32_t)((a.n + 31) / 32) : a.flags[a.counter];
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
-    const int i = (int)a.dense[item] * 32 + lane;
+    const int i = (int)(a.dense_all ? item : a.dense[item]) * 32 + lane;
     const bool valid = i < a.n;
     const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
@@ -1050,6 +1058,7 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.X = X;
   a.cs = cs;
   a.n = n;
+  a.dense_all = n < kDenseAllBelow;
   a.counter = kDenseCount0 + (pass & 1);
   a.next_counter = kDenseCount0 + ((pass + 1) & 1);
   a.flags = s.flags;

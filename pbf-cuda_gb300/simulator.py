@@ -132,14 +132,17 @@ class Simulator:
         """Run each step as a CUDA graph (default) or as individual launches."""
         check(self._L.pbf_use_graphs(self._h, int(bool(on))), "pbf_use_graphs")
 
-    def tape(self, on: bool = True) -> None:
-        """Record every following step for its reverse pass (backward)."""
-        check(self._L.pbf_tape_enable(self._h, int(bool(on))), "pbf_tape_enable")
+    def tape(self, depth=1) -> None:
+        """Record the following steps for their reverse passes: a stack of up
+        to ``depth`` taped steps (True: 1; 0 / False: tape off), emptied here.
+        ``backward`` pops the most recent one."""
+        check(self._L.pbf_tape_enable(self._h, int(depth)), "pbf_tape_enable")
 
     def backward(self, g_npos: torch.Tensor, g_nvel: torch.Tensor, stream=None):
-        """Reverse pass of the last (taped) step: adjoints of its outputs npos,
-        nvel (its output order) -> adjoints of its inputs pos, vel (its input
-        order) and of the limits (6 floats: ulim xyz, llim xyz)."""
+        """Reverse pass of the most recent taped step (popped from the tape):
+        adjoints of its outputs npos, nvel (its output order) -> adjoints of its
+        inputs pos, vel (its input order) and of the limits (6 floats: ulim
+        xyz, llim xyz)."""
         n = g_npos.shape[0]
         for t, name in ((g_npos, "g_npos"), (g_nvel, "g_nvel")):
             _check_state(t, name, n, 4)

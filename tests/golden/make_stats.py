@@ -32,7 +32,7 @@ def constraint_stats(rho: np.ndarray, rho0: float):
     return (float(c.mean()) if c.size else 0.0, float(c.max()) if c.size else 0.0, int((~fin).sum()))
 
 
-SEEDS = tuple(range(12))
+SEEDS = tuple(range(32))
 
 
 def cases(pbf, seed=0):

@@ -1,7 +1,7 @@
 """GPU tests of the inverse problem (pbf_cuda_gb300.inverse): the GPU
-gradient of the reduced problem against the FP64 oracle's (itself checked
-against finite differences on the CPU), and one optimisation step of the
-full-size problem."""
+gradient of the reduced problem and of one frame of the full-size problem
+against the FP64 oracle's pipeline (itself checked against finite
+differences on the CPU), and one full-size step's reverse pass."""
 from __future__ import annotations
 
 import numpy as np
@@ -31,27 +31,42 @@ def test_inverse_gradient_matches_oracle(pbf, cuda):
     assert abs(gag - ga) <= 2e-3 * abs(ga)
 
 
-def test_inverse_full_size_short_horizon_descends(pbf, cuda):
-    """15,625 particles (the inverse scene), the reference's default solver
-    parameters, 2 frames: a small step along the negative gradient lowers the
-    loss.  (Over tens of frames the step's adjoint grows by orders of
-    magnitude per frame, in the FP64 oracle as on the GPU, and overflows
-    float32; the horizon here keeps it finite.)"""
+def test_inverse_full_size_matches_oracle(pbf, cuda):
+    """The inverse scene at full size (15,625 particles), the reference's
+    parameters, one frame (2 steps): loss within 1e-3 and gradient error
+    percentiles within 3x those of the reference-order float port, both
+    against the FP64 pipeline of the oracle.  (The compressed start makes the
+    step's Jacobian large, and over tens of frames the adjoint grows by orders
+    of magnitude per frame, in FP64 as on the GPU; the tight gradient check is
+    the reduced problem's.)"""
     import torch
+    from oracle import inverse as oinv
 
     p = pbf.default_params()
     p.up[0], p.up[1], p.up[2] = 0.0, 1.0, 0.0
     scene = pbf.scenes.inverse_scene()
     scene.params = p
-    with pbf.inverse.InverseProblem(scene, frames=2, every=1) as ip:
-        ip.make_target()
-        v0 = torch.zeros((ip.n, 3), device="cuda")
-        L0, gv, ga = ip.loss_and_grad(v0, 0.0)
-        assert torch.isfinite(gv).all() and np.isfinite(ga)
-        assert gv.abs().max() > 0
-        step = 1e-3 / float(gv.abs().max())
-        L1 = ip.loss(v0 - step * gv, 0.0)
-        assert L1 < L0, (L0, L1)
+    pb = oinv.Problem(p, scene.pos.astype(np.float64), scene.ulim, (32, 16, 16), 2)
+    vt = np.random.default_rng(1).normal(0.0, 0.2, size=(scene.n, 3))
+    _, pt, _, _ = oinv.rollout(pb, vt, 0.3)
+    target = oinv.density(pb, pt)
+    v0 = np.random.default_rng(3).normal(0.0, 0.05, size=(scene.n, 3))
+    L, gv, _ = oinv.loss_and_grad(pb, v0, 0.0, target)
+    _, gv32, _ = oinv.loss_and_grad(pb, v0, 0.0, target, "f32")
+    with pbf.inverse.InverseProblem(scene, frames=1, every=1) as ip:
+        ip.target = torch.from_numpy(target.astype(np.float32)).cuda()
+        Lg, gvg, gag = ip.loss_and_grad(torch.from_numpy(v0.astype(np.float32)), 0.0)
+        torch.cuda.synchronize()
+    assert np.isfinite(gag) and np.isfinite(gvg.cpu().numpy()).all()
+    assert abs(Lg - L) <= 1e-3 * L
+    # float arithmetic of any order lands far from FP64 on a few particles of
+    # this compressed start (the reference-order float port: 99th percentile
+    # 4e-2 of the largest component): percentiles within 3x the port's
+    scale = np.abs(gv).max()
+    e_gpu = np.abs(gvg.cpu().numpy() - gv).ravel()
+    e_port = np.abs(gv32 - gv).ravel()
+    for q in (50, 90, 99):
+        assert np.percentile(e_gpu, q) <= 3 * np.percentile(e_port, q) + 1e-4 * scale, q
 
 
 def test_backward_full_size_one_step_matches_oracle(pbf, oracle, cuda):

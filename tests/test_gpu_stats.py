@@ -1,11 +1,11 @@
 """Statistical parity over long runs: 300 frames (600 steps) of the 8,000-particle
-dam break, 12 jitter seeds, against the reference's own kernels
+dam break, 32 jitter seeds, against the reference's own kernels
 (tests/golden/stats_*.npz, made by tests/golden/make_stats.py).
 
 Trajectories diverge chaotically (FP32 rounding differences grow, and the
 fluid settles into one of several layered packings), so runs are compared
 through the per-step mean and max of the compression max(C_i, 0),
-C_i = rho_i / rho0 - 1, averaged over the 600 steps and the 12 seeds:
+C_i = rho_i / rho0 - 1, averaged over the 600 steps and the 32 seeds:
   * the reference's own parameters: both within 1% of the reference;
   * the dam-break parameters (the fluid collapses into dense clusters and the
     reference's seeds alone spread by +-30%): within three combined standard
