@@ -184,9 +184,13 @@ def run_reference(args):
 
 def workload_config(scene, args) -> dict:
     p = scene.params
+    if scene.name == "large_sweep_1m":
+        what = ("128x64x128 lattice (d=0.05, +-0.005 jitter) in a 12.8x6.4x6.4 box, x-max wall "
+                "x_w(t)=12.8-1.6(1-cos(2 pi t/4s))")
+    else:
+        what = f"{scene.pos.shape[0]} particles in a {'x'.join(f'{u:g}' for u in scene.ulim)} box"
     return {
-        "workload": f"{scene.name}: {scene.n} particles, 128x64x128 lattice (d=0.05, +-0.005 jitter) in a "
-                    f"12.8x6.4x6.4 box, x-max wall x_w(t)=12.8-1.6(1-cos(2 pi t/4s)), h=0.1, "
+        "workload": f"{scene.name}: {scene.n} particles, {what}, h=0.1, "
                     f"{p.niter} solver iterations, dt=1/120 s (2 steps per 1/60 s frame)",
         "particles": scene.n, "niter": p.niter, "params": args.params,
         "pho0": round(float(p.pho0), 3), "lambda_eps": float(p.lambda_eps), "k_corr": round(float(p.k_corr), 6),
@@ -258,7 +262,8 @@ def run_ours(args):
 
     # -- end to end through the public API with host buffers ------------------------
     e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps, stream)
-    alt = measure_reference_params(pkg, torch, args, stream) if args.params == "scene" else None
+    alt = (measure_reference_params(pkg, torch, args, stream)
+           if args.params == "scene" and args.scene == "large_sweep" else None)
 
     value = world * n * args.steps / (total_ms / 1e3)
     if rank != 0:
@@ -288,11 +293,18 @@ def run_ours(args):
     # the initial lattice, and the GPU is timed on exactly those steps beside it.
     from oracle import oracle
 
-    cpu_steps_max = max(1, min(args.cpu_steps, args.steps))
-    cpu_rate, cpu_steps, cpu_s = cpu_port_rate(oracle, scene, scene.pos, scene.vel,
-                                               np.arange(n, dtype=np.uint32), 0.0, args.cpu_budget,
-                                               cpu_steps_max)
-    gpu_same = gpu_rate_first_steps(pkg, torch, scene, cpu_steps, stream)
+    cpu_line = None
+    if args.cpu_steps > 0:
+        cpu_steps_max = min(args.cpu_steps, args.steps)
+        cpu_rate, cpu_steps, cpu_s = cpu_port_rate(oracle, scene, scene.pos, scene.vel,
+                                                   np.arange(n, dtype=np.uint32), 0.0, args.cpu_budget,
+                                                   cpu_steps_max)
+        gpu_same = gpu_rate_first_steps(pkg, torch, scene, cpu_steps, stream)
+        cpu_line = {"value": cpu_rate, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
+                    "sample": f"the workload's first {cpu_steps} steps from the initial lattice, {n} "
+                              f"particles ({cpu_s:.1f} s of CPU time); the GPU on the same steps: "
+                              f"{gpu_same:.4g} {UNIT}",
+                    "gpu_same_sample": gpu_same}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -303,11 +315,7 @@ def run_ours(args):
                      "algorithmic_bytes_per_launch": alg[kernel], "launch_ms": launch_ms,
                      "traffic": ncu_traffic(kernel)},
         "phases_ms": phases,
-        "cpu_baseline": {"value": cpu_rate, "unit": UNIT, "cores": oracle.threads(), "kind": "port",
-                         "sample": f"the workload's first {cpu_steps} steps from the initial lattice, {n} "
-                                   f"particles ({cpu_s:.1f} s of CPU time); the GPU on the same steps: "
-                                   f"{gpu_same:.4g} {UNIT}",
-                         "gpu_same_sample": gpu_same},
+        "cpu_baseline": cpu_line,
         "e2e": e2e,
         "gpu_launches": launches * args.steps,
         "clocks": clk,
@@ -562,7 +570,7 @@ def main(argv=None):
     ap.add_argument("--steps", type=int, default=240, help="timed steps (default: 120 frames x 2 steps)")
     ap.add_argument("--warmup", type=int, default=120, help="untimed steps (default: 60 frames x 2 steps)")
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
-    ap.add_argument("--scene", default="large_sweep", choices=("large_sweep", "double_dam", "dam_break"))
+    ap.add_argument("--scene", default="large_sweep", choices=("large_sweep", "double_dam", "dam_break", "clustered"))
     ap.add_argument("--workload", choices=("step", "ensemble", "adjoint"), default="step",
                     help="step: particle-updates/s of one scene; ensemble: scene-steps/s of 256 scenes; "
                          "adjoint: fwd+bwd ms/frame of the inverse problem")
@@ -573,7 +581,8 @@ def main(argv=None):
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
-    ap.add_argument("--cpu-steps", type=int, default=3, help="most steps the CPU baseline times")
+    ap.add_argument("--cpu-steps", type=int, default=3,
+                    help="most steps the CPU baseline times (0: no CPU baseline, for profiling runs)")
     ap.add_argument("--cpu-warmup-steps", type=int, default=3, help="most warm-up steps of the reference arm")
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
     args = ap.parse_args(argv)

@@ -245,6 +245,7 @@ struct TapeLayout {
 cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
   const size_t slots = pbf::group_slots(max_particles);
   const size_t entries = (size_t)max_particles;
+  sol.grp_pool = max_particles;
   cudaError_t e = alloc(&sol.grp_cell, slots);
   if (e == cudaSuccess) e = alloc(&sol.grp_off, slots);
   if (e == cudaSuccess) e = alloc(&sol.grp_n, slots);
@@ -253,7 +254,10 @@ cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
   if (e == cudaSuccess) e = alloc(&sol.grp_pos, entries);
   if (e == cudaSuccess) e = alloc(&sol.grp_sum, entries);
   if (e == cudaSuccess) e = alloc(&sol.grp_aux, entries);
-  if (e == cudaSuccess) e = alloc(&sol.grp_id, (size_t)max_particles);
+  if (e == cudaSuccess) e = alloc(&sol.grp_id, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_hash, 8 * entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_max, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_acc, 3 * entries);
   return e;
 }
 
@@ -263,7 +267,8 @@ void free_all(pbf_solver* s) {
                   s->grid.scan_partials, s->sol.xs, s->sol.xa, s->sol.xb, s->sol.iid_s,
                   s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense, s->sol.masks,
                   s->sol.cell_flags, s->sol.grp_cell, s->sol.grp_off, s->sol.grp_n, s->sol.grp_rep, s->sol.grp_cnt,
-                  s->sol.grp_pos, s->sol.grp_sum, s->sol.grp_aux, s->sol.grp_id};
+                  s->sol.grp_pos, s->sol.grp_sum, s->sol.grp_aux, s->sol.grp_id, s->sol.grp_hash,
+                  s->sol.grp_max, s->sol.grp_acc};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -868,7 +873,8 @@ void batch_free(pbf_batch* b) {
                   b->grid.scan_partials, b->sol.xs, b->sol.xa, b->sol.xb, b->sol.iid_s,
                   b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->sol.masks,
                   b->sol.cell_flags, b->sol.grp_cell, b->sol.grp_off, b->sol.grp_n, b->sol.grp_rep, b->sol.grp_cnt,
-                  b->sol.grp_pos, b->sol.grp_sum, b->sol.grp_aux, b->sol.grp_id, b->d_geom, b->d_sid};
+                  b->sol.grp_pos, b->sol.grp_sum, b->sol.grp_aux, b->sol.grp_id, b->sol.grp_hash,
+                  b->sol.grp_max, b->sol.grp_acc, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);

@@ -9,7 +9,7 @@
 // pbf_create allocates the solver's scratch.
 //
 // How: the scratch lives in one file-scope __device__ array of fixed size,
-// kNoAllocScratchBytes (about 6.4 MB), which is part of this library's device
+// kNoAllocScratchBytes (about 10.2 MB), which is part of this library's device
 // image: every GPU that loads the library holds it until the process exits.
 // It bounds the problem to kNoAllocMaxParticles particles and
 // kNoAllocMaxCells grid cells; larger calls are rejected with
@@ -82,7 +82,10 @@ constexpr size_t kOffGrpPos = kOffGrpCnt + align_up(4 * kEntries);
 constexpr size_t kOffGrpSum = kOffGrpPos + align_up(16 * kEntries);
 constexpr size_t kOffGrpAux = kOffGrpSum + align_up(16 * kEntries);
 constexpr size_t kOffGrpId = kOffGrpAux + align_up(16 * kEntries);
-constexpr size_t kNoAllocScratchBytes = kOffGrpId + align_up(2 * kNp);
+constexpr size_t kOffGrpHash = kOffGrpId + align_up(4 * kNp);
+constexpr size_t kOffGrpMax = kOffGrpHash + align_up(4 * 8 * kNp);
+constexpr size_t kOffGrpAcc = kOffGrpMax + align_up(4 * kNp);
+constexpr size_t kNoAllocScratchBytes = kOffGrpAcc + align_up(8 * 3 * kNp);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -145,6 +148,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.masks = (uint32_t*)(base + kOffMasks);
   s.mask_stride = kNoAllocMaxParticles;
   s.cell_flags = (uint32_t*)(base + kOffCellFlags);
+  s.grp_pool = kNoAllocMaxParticles;
   s.grp_cell = (int*)(base + kOffGrpCell);
   s.grp_off = (int*)(base + kOffGrpOff);
   s.grp_n = (int*)(base + kOffGrpN);
@@ -153,7 +157,10 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.grp_pos = (float4*)(base + kOffGrpPos);
   s.grp_sum = (float4*)(base + kOffGrpSum);
   s.grp_aux = (float4*)(base + kOffGrpAux);
-  s.grp_id = (uint16_t*)(base + kOffGrpId);
+  s.grp_id = (int*)(base + kOffGrpId);
+  s.grp_hash = (int*)(base + kOffGrpHash);
+  s.grp_max = (unsigned*)(base + kOffGrpMax);
+  s.grp_acc = (unsigned long long*)(base + kOffGrpAcc);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;

@@ -168,17 +168,22 @@ struct SolverScratch {
   const uint32_t* keys_sorted;  // the grid's sorted cell ids (set before the passes)
   const uint32_t* cell_start;   // the grid's cell prefix (set before the passes)
   // group tables of the cells holding >= kGroupCell particles (one slot each);
-  // slot s owns entries [grp_off[s], grp_off[s] + min(particles, kMaxGroups))
-  // of a pool of max_particles entries
+  // slot s of population p owns entries [grp_off[s], grp_off[s] + p) of the
+  // pools of max_particles entries and [2 grp_off[s], 2 grp_off[s] + 2 p) of
+  // each hash table part
+  int grp_pool;        // pool entries (max_particles)
   int* grp_cell;       // [group_slots] cell of each slot
   int* grp_off;        // [group_slots] first pool entry of each slot
   int* grp_n;          // [group_slots] groups in the slot's current table; -1: not grouped
   int* grp_rep;        // [max_particles] pool: sorted slot of each group's first particle
   int* grp_cnt;        // [max_particles] pool: particles of each group
   float4* grp_pos;     // [max_particles] pool: the group's position
-  float4* grp_sum;     // [max_particles] pool: lambda (x) / density (w) of the group
-  float4* grp_aux;     // [max_particles] pool: velocity of the group (xsph)
-  uint16_t* grp_id;    // [max_particles] group of each particle of a grouped cell
+  float4* grp_sum;     // [max_particles] pool: pass sums of the group (see solver.cu)
+  float4* grp_aux;     // [max_particles] pool: velocity of the group's first particle (xsph)
+  int* grp_id;         // [max_particles] group of each particle of a grouped cell
+  int* grp_hash;       // [4][2 max_particles] hash tables: owner, count, first particle, rank
+  unsigned* grp_max;   // [max_particles] pool: largest deviation of a group (fixed-point scale)
+  unsigned long long* grp_acc;  // [3 max_particles] pool: fixed-point sums
 };
 
 // Bits of SolverScratch::cell_flags: the stale cell of a particle whose
@@ -199,15 +204,15 @@ constexpr int kCellSlotShift = 8;
 // tensile term).  For every cell holding at least kGroupCell particles, each
 // pass first groups its particles by the values that enter a pair term
 // non-linearly (position; position and density for XSPH; delta_p reuses the
-// lambda pass's groups), up to kMaxGroups groups (more and the cell stays
-// ungrouped), and a window containing the cell visits each group once with
-// its multiplicity instead of its particles.  The pair terms are linear in
-// lambda_j (delta_p) and v_j (XSPH): a group carries the sum of its members'
-// values, accumulated exactly in fixed point (integer atomics, so the sum
-// does not depend on the order).  This is the reference's sum with its terms
-// grouped: results differ from it by rounding only.
+// lambda pass's groups) in a hash table with room for every particle, orders
+// the groups by their first particle, and a window containing the cell
+// visits each group once with its multiplicity instead of its particles.
+// The pair terms are linear in lambda_j (delta_p) and v_j (XSPH): a group
+// carries the sum of its members' values, accumulated exactly in fixed point
+// (integer atomics, so the sum does not depend on the order).  This is the
+// reference's sum with its terms grouped: results differ from it by
+// rounding only.
 constexpr int kGroupCell = 512;
-constexpr int kMaxGroups = 512;
 inline size_t group_slots(int max_particles) { return (size_t)max_particles / kGroupCell + 1; }
 
 // Neighbour masks a particle keeps between the lambda and delta_p passes of

@@ -725,11 +725,11 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
   const uint32_t key = skeys[k];
   const uint32_t pop = cs[key + 1] - cs[key];
   if ((uint32_t)k == cs[key] && pop >= (uint32_t)kGroupCell) {
-    // one slot per such cell (< n / kGroupCell of them) and min(pop, kMaxGroups)
-    // pool entries (the pool holds n: the cells' populations sum to <= n)
+    // one slot per such cell (< n / kGroupCell of them) and `pop` pool entries
+    // (the pool holds n: the cells' populations sum to <= n)
     const uint32_t slot = atomicAdd(&flags[kGroupCount], 1u);
     grp_cell[slot] = (int)key;
-    grp_off[slot] = (int)atomicAdd(&flags[kGroupPool], min(pop, (uint32_t)kMaxGroups));
+    grp_off[slot] = (int)atomicAdd(&flags[kGroupPool], pop);
     atomicOr(&cell_flags[key], (slot + 1u) << kCellSlotShift);
   }
   const uint32_t p = min(perm[k], (uint32_t)(n - 1));  // a permutation of [0, n): the min never binds
@@ -747,7 +747,7 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
 enum GroupsWhat { kGroupsPos = 0, kGroupsLambda = 1, kGroupsXsph = 2 };
 
 constexpr int kGroupThreads = 1024;  // one block per grouped cell: many loads in flight
-constexpr int kGroupHash = 2 * kMaxGroups;  // open-addressing slots of a block's hash table
+constexpr int kGroupWarps = kGroupThreads / 32;
 
 struct GroupArgs {
   const float4* X;        // positions of the pass
@@ -757,6 +757,7 @@ struct GroupArgs {
   const uint32_t* cs;
   const uint32_t* count;  // number of slots (flags[kGroupCount])
   int n;
+  int np;                 // pool entries (the hash table parts are 2 np long)
   const int* cell;
   const int* off;
   int* ng;
@@ -765,10 +766,13 @@ struct GroupArgs {
   float4* pos;
   float4* sum;
   float4* aux;
-  uint16_t* id;
+  int* id;
+  int* hash;
+  unsigned* gmax;
+  unsigned long long* acc;
 };
 
-// The key of particle j: the values a pass reads of a neighbour, as bits.
+// The key of particle j: the values that enter a pair term non-linearly.
 template <int kWhat>
 struct GroupKey {
   static constexpr int kWords = kWhat == kGroupsXsph ? 4 : 3;
@@ -793,36 +797,115 @@ struct GroupKey {
   }
 };
 
-// One block per slot (grid-stride).
-//   kGroupsPos / kGroupsXsph: group the cell's particles by GroupKey in a
-//     shared-memory hash table (the claiming particle of a hash slot holds the
-//     key; integer atomics only), order the groups by their first particle,
-//     and write rep, cnt, pos and each particle's group id; for xsph also
-//     aux = the first particle's velocity v_rep, sum.w = density and sum.xyz
-//     = sum over the group of (v_j - v_rep), in 64-bit fixed point scaled by
-//     a power of two from the group's largest |v_j - v_rep| and count (exact
-//     to 2^-62 of the bound, order-free).  Over kMaxGroups groups, or a
-//     non-finite velocity difference (other than between identical bits):
-//     ng = -1.
-//   kGroupsLambda: for the kGroupsPos table of the same positions, sum.x =
-//     lambda_rep and sum.y = sum over the group of (lambda_j - lambda_rep) in
-//     the same fixed point as xsph's velocities; a non-finite difference
-//     (other than between identical bits): ng = -1.
-// Deterministic: the table's contents do not depend on which particle of a
-// group claimed its hash slot.
 // x - x_rep, and 0 where the two are the same bits (so a group whose members
-// share one non-finite value stays grouped).
+// share one non-finite value keeps it).
 __device__ __forceinline__ float dev_from(float x, float xr) {
   return __float_as_uint(x) == __float_as_uint(xr) ? 0.f : x - xr;
 }
 
+// Exclusive prefix of `flag` over the block in thread order; `total` gets the sum.
+__device__ __forceinline__ int block_scan(int flag, int* sh, int& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned ball = __ballot_sync(0xffffffffu, flag);
+  const int in_warp = __popc(ball & ((1u << lane) - 1u));
+  __syncthreads();
+  if (lane == 0) sh[warp] = __popc(ball);
+  __syncthreads();
+  if (warp == 0) {
+    const int v = lane < kGroupWarps ? sh[lane] : 0;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane < kGroupWarps) sh[32 + lane] = x - v;  // exclusive
+    if (lane == kGroupWarps - 1) sh[64] = x;
+  }
+  __syncthreads();
+  total = sh[64];
+  return sh[32 + warp] + in_warp;
+}
+
+// Fixed-point sums over the groups of slot (t0 .. t0 + ng) of the values val(k)
+// (k = cell-relative particle) minus the group's first particle's value
+// rep_val(g), C components: exact to 2^-62 of the bound max|dev| * count,
+// order-free.  Writes out(g, c, sum) for each group; false if some deviation
+// is not finite (other than between identical bits).
+template <int C, class Val, class RepVal, class Out>
+__device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val val, RepVal rep_val, Out out,
+                           int* s_flag) {
+  if (threadIdx.x == 0) *s_flag = 0;
+  for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+    a.gmax[t0 + g] = 0u;
+    for (int c = 0; c < C; ++c) a.acc[3 * (t0 + g) + c] = 0ull;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+    const int g = a.id[b + k];
+    float d = 0.f;
+    bool fin = true;
+    for (int c = 0; c < C; ++c) {
+      const float e = dev_from(val(k, c), rep_val(g, c));
+      fin &= isfinite(e);
+      d = fmaxf(d, fabsf(e));
+    }
+    const unsigned bits = fin ? __float_as_uint(d) : 0x7f800000u;  // +inf marks non-finite
+    const unsigned act = __activemask(), same = __match_any_sync(act, g);
+    const unsigned mx = __reduce_max_sync(same, bits);
+    if ((threadIdx.x & 31) == __ffs(same) - 1) atomicMax(&a.gmax[t0 + g], mx);
+  }
+  __syncthreads();
+  for (int g = threadIdx.x; g < ng; g += kGroupThreads)
+    if (!isfinite(__uint_as_float(a.gmax[t0 + g]))) atomicOr(s_flag, 1);
+  __syncthreads();
+  if (*s_flag) return false;
+  for (int k = threadIdx.x; k < m; k += kGroupThreads) {
+    const int g = a.id[b + k];
+    const float mx = __uint_as_float(a.gmax[t0 + g]);
+    int e = 0;
+    if (mx > 0.f) frexpf(mx, &e);                         // mx < 2^e
+    const int sh = 62 - e - (32 - __clz(a.cnt[t0 + g]));  // |sum| 2^sh < 2^62
+    const unsigned act = __activemask(), same = __match_any_sync(act, g);
+    for (int c = 0; c < C; ++c) {
+      // |dev| 2^sh < 2^62 is a float without overflow; the scaling is exact
+      long long q = __float2ll_rn(ldexpf(dev_from(val(k, c), rep_val(g, c)), sh));
+      if (same == act) {  // integer sums: any order gives the same result
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(act, q, o);
+        if ((threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(&a.acc[3 * (t0 + g) + c], (unsigned long long)q);
+      } else {
+        atomicAdd(&a.acc[3 * (t0 + g) + c], (unsigned long long)q);
+      }
+    }
+  }
+  __syncthreads();
+  for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+    const float mx = __uint_as_float(a.gmax[t0 + g]);
+    int e = 0;
+    if (mx > 0.f) frexpf(mx, &e);
+    const int sh = 62 - e - (32 - __clz(a.cnt[t0 + g]));
+    for (int c = 0; c < C; ++c)
+      out(g, c, (float)ldexp((double)(long long)a.acc[3 * (t0 + g) + c], -sh));
+  }
+  __syncthreads();
+  return true;
+}
+
+// One block per slot (grid-stride).
+//   kGroupsPos / kGroupsXsph: insert every particle of the cell into the
+//     slot's hash table (2 entries per particle, in global memory: the
+//     claiming particle of an entry holds the key; integer atomics only),
+//     number the groups in order of their first particle (an ordered block
+//     scan), write rep, cnt, pos and each particle's group id; for xsph also
+//     aux = the first particle's velocity v_rep, sum.w = density and sum.xyz
+//     = sum over the group of (v_j - v_rep) in fixed point (group_sums).
+//   kGroupsLambda: for the kGroupsPos table of the same positions, sum.x =
+//     lambda_rep and sum.y = sum over the group of (lambda_j - lambda_rep).
+// A non-finite deviation in a sum: ng = -1 (the cell is visited per particle).
+// Deterministic: no result depends on which particle claimed an entry.
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
-  __shared__ int s_owner[kGroupHash];   // claiming particle (cell-relative) or -1
-  __shared__ int s_cnt[kGroupHash];
-  __shared__ int s_first[kGroupHash];   // first particle of the group
-  __shared__ int s_rank[kGroupHash];
-  __shared__ int s_used, s_over;
+  __shared__ int sh[80];
+  __shared__ int s_flag;
   const uint32_t slots = *a.count;
   for (uint32_t slot = blockIdx.x; slot < slots; slot += gridDim.x) {
     const int cell = a.cell[slot];
@@ -830,84 +913,41 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
     const int m = max(min((int)a.cs[cell + 1], a.n) - b, 0);
     const int t0 = a.off[slot];
     if constexpr (kWhat == kGroupsLambda) {
-      // sum over each group of (lambda_j - lambda_rep) in 64-bit fixed point:
-      // members at one position can still differ in the last bits of lambda
-      // (their windows may have been summed by different kernels)
-      __shared__ unsigned l_max[kMaxGroups];
-      __shared__ int l_shift[kMaxGroups];
-      __shared__ float l_rep[kMaxGroups];
-      __shared__ unsigned long long l_acc[kMaxGroups];
       const int ng = a.ng[slot];
       if (ng <= 0) continue;
-      for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-        l_max[g] = 0u;
-        l_rep[g] = a.lambda[a.rep[t0 + g]];
-        l_acc[g] = 0ull;
-      }
-      if (threadIdx.x == 0) s_over = 0;
-      __syncthreads();
-      for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-        const int g = a.id[b + k];
-        const float d = dev_from(a.lambda[b + k], l_rep[g]);
-        const unsigned bits = isfinite(d) ? __float_as_uint(fabsf(d)) : 0x7f800000u;
-        const unsigned act = __activemask(), same = __match_any_sync(act, g);
-        if (same == act) {
-          const unsigned mx = __reduce_max_sync(act, bits);
-          if ((threadIdx.x & 31) == __ffs(act) - 1) atomicMax(&l_max[g], mx);
-        } else {
-          atomicMax(&l_max[g], bits);
-        }
-      }
-      __syncthreads();
-      for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-        const float mx = __uint_as_float(l_max[g]);
-        if (!isfinite(mx)) atomicOr(&s_over, 1);
-        int e = 0;
-        if (mx > 0.f) frexpf(mx, &e);
-        l_shift[g] = 62 - e - (32 - __clz(a.cnt[t0 + g]));
-      }
-      __syncthreads();
-      if (!s_over) {
-        for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-          const int g = a.id[b + k];
-          long long q = __float2ll_rn(ldexpf(dev_from(a.lambda[b + k], l_rep[g]), l_shift[g]));
-          const unsigned act = __activemask(), same = __match_any_sync(act, g);
-          if (same == act) {
-            for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(act, q, o);
-            if ((threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(&l_acc[g], (unsigned long long)q);
-          } else {
-            atomicAdd(&l_acc[g], (unsigned long long)q);
-          }
-        }
-      }
-      __syncthreads();
-      if (s_over) {
-        if (threadIdx.x == 0) a.ng[slot] = -1;
-      } else {
-        for (int g = threadIdx.x; g < ng; g += kGroupThreads)
-          a.sum[t0 + g] = make_float4(l_rep[g], (float)ldexp((double)(long long)l_acc[g], -l_shift[g]), 0.f, 0.f);
-      }
+      const bool ok = group_sums<1>(
+          a, b, m, t0, ng, [&](int k, int) { return a.lambda[b + k]; },
+          [&](int g, int) { return a.lambda[a.rep[t0 + g]]; },
+          [&](int g, int, float v) { a.sum[t0 + g] = make_float4(a.lambda[a.rep[t0 + g]], v, 0.f, 0.f); },
+          &s_flag);
+      if (!ok && threadIdx.x == 0) a.ng[slot] = -1;
       __syncthreads();
     } else {
-      for (int h = threadIdx.x; h < kGroupHash; h += kGroupThreads) {
-        s_owner[h] = -1;
-        s_cnt[h] = 0;
-        s_first[h] = INT_MAX;
+      if (m == 0) {
+        if (threadIdx.x == 0) a.ng[slot] = -1;
+        continue;
       }
-      if (threadIdx.x == 0) s_used = s_over = 0;
+      const int H = 2 * m;
+      int* h_owner = a.hash + 2 * t0;
+      int* h_cnt = h_owner + 2 * a.np;
+      int* h_first = h_owner + 4 * a.np;
+      int* h_rank = h_owner + 6 * a.np;
+      for (int h = threadIdx.x; h < H; h += kGroupThreads) {
+        h_owner[h] = -1;
+        h_cnt[h] = 0;
+        h_first[h] = INT_MAX;
+      }
       __syncthreads();
       for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-        if (*(volatile int*)&s_over) break;
         const GroupKey<kWhat> key(a, b + k);
-        int h = (int)(key.hash() & (kGroupHash - 1));
+        int h = (int)(key.hash() % (uint32_t)H);
         int found = -1;
-        for (int probe = 0; probe < kGroupHash; ++probe, h = (h + 1) & (kGroupHash - 1)) {
-          int o = *(volatile int*)&s_owner[h];
+        for (int probe = 0; probe < H; ++probe, h = h + 1 == H ? 0 : h + 1) {
+          int o = *(volatile int*)&h_owner[h];
           if (o < 0) {
-            o = atomicCAS(&s_owner[h], -1, k);
-            if (o < 0) {  // claimed: a new group
-              if (atomicAdd(&s_used, 1) >= kMaxGroups) atomicOr(&s_over, 1);
-              found = h;
+            o = atomicCAS(&h_owner[h], -1, k);
+            if (o < 0) {
+              found = h;  // claimed: a new group
               break;
             }
           }
@@ -916,109 +956,52 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
             break;
           }
         }
-        if (found < 0) {
-          atomicOr(&s_over, 1);
-          break;
-        }
-        // one atomic per group per warp: the lowest lane holds the lowest k
-        const unsigned same = __match_any_sync(__activemask(), found);
+        // H = 2m entries for at most m keys: a probe always ends
+        const unsigned act = __activemask(), same = __match_any_sync(act, found);
         if ((threadIdx.x & 31) == __ffs(same) - 1) {
-          atomicAdd(&s_cnt[found], __popc(same));
-          atomicMin(&s_first[found], k);
+          atomicAdd(&h_cnt[found], __popc(same));
+          atomicMin(&h_first[found], k);  // the lowest lane holds the lowest k
         }
-        a.id[b + k] = (uint16_t)found;
+        a.id[b + k] = found;
       }
       __syncthreads();
-      const int ng = s_over ? -1 : s_used;
-      if (ng > 0) {
-        // rank of each group = groups with an earlier first particle
-        for (int h = threadIdx.x; h < kGroupHash; h += kGroupThreads) {
-          if (s_owner[h] < 0) continue;
-          const int f = s_first[h];
-          int r = 0;
-          for (int u = 0; u < kGroupHash; ++u) r += s_owner[u] >= 0 && s_first[u] < f;
-          s_rank[h] = r;
-          const int j = b + f;
-          a.rep[t0 + r] = j;
-          a.cnt[t0 + r] = s_cnt[h];
-          a.pos[t0 + r] = a.X[j];
+      // groups in order of their first particle: an ordered scan over the particles
+      int ng = 0;
+      for (int k0 = 0; k0 < m; k0 += kGroupThreads) {
+        const int k = k0 + threadIdx.x;
+        const int h = k < m ? a.id[b + k] : 0;
+        const bool first = k < m && h_first[h] == k;
+        int total;
+        const int r = ng + block_scan(first, sh, total);
+        if (first) {
+          h_rank[h] = r;
+          a.rep[t0 + r] = b + k;
+          a.cnt[t0 + r] = h_cnt[h];
+          a.pos[t0 + r] = a.X[b + k];
+          if constexpr (kWhat == kGroupsXsph) a.aux[t0 + r] = a.V[b + k];
         }
-        __syncthreads();
-        for (int k = threadIdx.x; k < m; k += kGroupThreads) a.id[b + k] = (uint16_t)s_rank[a.id[b + k]];
+        ng += total;
       }
+      __syncthreads();
+      for (int k = threadIdx.x; k < m; k += kGroupThreads) a.id[b + k] = h_rank[a.id[b + k]];
+      __syncthreads();
       int ngw = ng;
       if constexpr (kWhat == kGroupsXsph) {
-        __shared__ unsigned s_max[kMaxGroups];
-        __shared__ int s_shift[kMaxGroups];
-        __shared__ float4 s_vrep[kMaxGroups];
-        __shared__ unsigned long long s_acc[kMaxGroups][3];
-        if (ng > 0) {
-          __syncthreads();
-          for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-            s_max[g] = 0u;
-            s_vrep[g] = a.V[a.rep[t0 + g]];
-            s_acc[g][0] = s_acc[g][1] = s_acc[g][2] = 0ull;
-          }
-          __syncthreads();
-          for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-            const int g = a.id[b + k];
-            const float4 v = a.V[b + k], vr = s_vrep[g];
-            const float dx = dev_from(v.x, vr.x), dy = dev_from(v.y, vr.y), dz = dev_from(v.z, vr.z);
-            const float d = fmaxf(fmaxf(fabsf(dx), fabsf(dy)), fabsf(dz));
-            const bool fin = isfinite(dx) && isfinite(dy) && isfinite(dz);
-            const unsigned bits = fin ? __float_as_uint(d) : 0x7f800000u;  // +inf marks non-finite
-            const unsigned act = __activemask(), same = __match_any_sync(act, g);
-            if (same == act) {  // the common case: one group for the whole warp
-              const unsigned mx = __reduce_max_sync(act, bits);
-              if ((threadIdx.x & 31) == __ffs(act) - 1) atomicMax(&s_max[g], mx);
-            } else {
-              atomicMax(&s_max[g], bits);
-            }
-          }
-          if (threadIdx.x == 0) s_over = 0;
-          __syncthreads();
-          for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-            const float mx = __uint_as_float(s_max[g]);
-            if (!isfinite(mx)) atomicOr(&s_over, 1);
-            int e = 0;
-            if (mx > 0.f) frexpf(mx, &e);                      // mx < 2^e
-            const int c = 32 - __clz(a.cnt[t0 + g]);           // cnt < 2^c
-            s_shift[g] = 62 - e - c;                           // |sum| * 2^shift < 2^62
-          }
-          __syncthreads();
-          if (!s_over) {
-            for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-              const int g = a.id[b + k];
-              const float4 v = a.V[b + k], vr = s_vrep[g];
-              const int sh = s_shift[g];
-              // |d| 2^sh < 2^62 is a float without overflow; the scaling is exact
-              long long q[3] = {__float2ll_rn(ldexpf(dev_from(v.x, vr.x), sh)),
-                                __float2ll_rn(ldexpf(dev_from(v.y, vr.y), sh)),
-                                __float2ll_rn(ldexpf(dev_from(v.z, vr.z), sh))};
-              const unsigned act = __activemask(), same = __match_any_sync(act, g);
-              if (same == act) {  // integer sums: any order gives the same result
-                for (int o = 16; o > 0; o >>= 1)
-                  for (int c3 = 0; c3 < 3; ++c3) q[c3] += __shfl_xor_sync(act, q[c3], o);
-                if ((threadIdx.x & 31) == __ffs(act) - 1)
-                  for (int c3 = 0; c3 < 3; ++c3) atomicAdd(&s_acc[g][c3], (unsigned long long)q[c3]);
-              } else {
-                for (int c3 = 0; c3 < 3; ++c3) atomicAdd(&s_acc[g][c3], (unsigned long long)q[c3]);
+        const bool ok = group_sums<3>(
+            a, b, m, t0, ng,
+            [&](int k, int c) { const float4 v = a.V[b + k]; return c == 0 ? v.x : (c == 1 ? v.y : v.z); },
+            [&](int g, int c) { const float4 v = a.aux[t0 + g]; return c == 0 ? v.x : (c == 1 ? v.y : v.z); },
+            [&](int g, int c, float v) {
+              float4& s4 = a.sum[t0 + g];
+              if (c == 0) s4.x = v;
+              if (c == 1) s4.y = v;
+              if (c == 2) {
+                s4.z = v;
+                s4.w = a.rho[a.rep[t0 + g]];
               }
-            }
-          }
-          __syncthreads();
-          if (s_over) {
-            ngw = -1;
-          } else {
-            for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-              const int sh = -s_shift[g];
-              a.sum[t0 + g] = make_float4((float)ldexp((double)(long long)s_acc[g][0], sh),
-                                          (float)ldexp((double)(long long)s_acc[g][1], sh),
-                                          (float)ldexp((double)(long long)s_acc[g][2], sh), a.rho[a.rep[t0 + g]]);
-              a.aux[t0 + g] = s_vrep[g];
-            }
-          }
-        }
+            },
+            &s_flag);
+        if (!ok) ngw = -1;
       }
       if (threadIdx.x == 0) a.ng[slot] = ngw;
       __syncthreads();
@@ -1037,6 +1020,7 @@ cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const flo
   a.cs = s.cell_start;
   a.count = s.flags + kGroupCount;
   a.n = n;
+  a.np = s.grp_pool;
   a.cell = s.grp_cell;
   a.off = s.grp_off;
   a.ng = s.grp_n;
@@ -1046,6 +1030,9 @@ cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const flo
   a.sum = s.grp_sum;
   a.aux = s.grp_aux;
   a.id = s.grp_id;
+  a.hash = s.grp_hash;
+  a.gmax = s.grp_max;
+  a.acc = s.grp_acc;
   k_groups<kWhat><<<c.dense_grid, kGroupThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }

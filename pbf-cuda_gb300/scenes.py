@@ -141,6 +141,32 @@ def large_sweep(seed: int = 0, niter: int = 4) -> Scene:
                  params=scene_params(niter))
 
 
+def clustered(seed: int = 0, niter: int = 4) -> Scene:
+    """1,048,576 particles in the 12.8 x 6.4 x 6.4 box in the state the
+    dam-break parameters drive large scenes into: a 64^3 lattice of fluid
+    plus 786,432 particles collapsed onto six points (cells of 131,072
+    particles at one position: three box corners, two wall points, one point
+    in the fluid), each cluster moving as one.  The profiling case of the
+    grouped-cell path."""
+    rng = np.random.default_rng(seed)
+    lat = lattice((64, 64, 64), (0.0, 0.0, 0.0), rng)
+    pts = [(12.799, 0.001, 0.001), (12.799, 0.001, 6.399), (0.001, 0.001, 6.399),
+           (6.4, 0.001, 3.2), (12.799, 3.2, 3.2), (1.6, 1.2, 1.6)]
+    k = 131072
+    parts, vparts = [lat], [np.zeros_like(lat)]
+    for c in pts:
+        blk = np.zeros((k, 4), np.float32)
+        blk[:, :3] = c
+        parts.append(blk)
+        v = np.zeros((k, 4), np.float32)
+        v[:, :3] = rng.normal(0.0, 0.1, size=3)
+        vparts.append(v)
+    order = rng.permutation(sum(len(q) for q in parts))
+    pos = np.concatenate(parts)[order]
+    vel = np.concatenate(vparts)[order]
+    return Scene("clustered_1m", pos, vel, (12.8, 6.4, 6.4), (0.0, 0.0, 0.0), params=scene_params(niter))
+
+
 INVERSE_SPACING = 0.04
 
 
@@ -172,5 +198,6 @@ SCENES = {
     "dam_break": dam_break,
     "double_dam": double_dam,
     "large_sweep": large_sweep,
+    "clustered": clustered,
     "inverse": inverse_scene,
 }
