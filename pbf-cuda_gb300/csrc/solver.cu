@@ -894,18 +894,23 @@ __device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val
 //   kGroupsPos / kGroupsXsph: insert every particle of the cell into the
 //     slot's hash table (2 entries per particle, in global memory: the
 //     claiming particle of an entry holds the key; integer atomics only),
-//     number the groups in order of their first particle (an ordered block
-//     scan), write rep, cnt, pos and each particle's group id; for xsph also
+//     number the groups in order of their first particle (by counting in
+//     shared memory, or for over kGroupList groups by an ordered block scan),
+//     write rep, cnt, pos and each particle's group id; for xsph also
 //     aux = the first particle's velocity v_rep, sum.w = density and sum.xyz
 //     = sum over the group of (v_j - v_rep) in fixed point (group_sums).
 //   kGroupsLambda: for the kGroupsPos table of the same positions, sum.x =
 //     lambda_rep and sum.y = sum over the group of (lambda_j - lambda_rep).
 // A non-finite deviation in a sum: ng = -1 (the cell is visited per particle).
 // Deterministic: no result depends on which particle claimed an entry.
+constexpr int kGroupList = 4096;  // groups ranked in shared memory; more: an ordered scan
+
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
   __shared__ int sh[80];
-  __shared__ int s_flag;
+  __shared__ int s_flag, s_ng;
+  __shared__ int s_list[kGroupList];   // hash entries claimed (any order)
+  __shared__ int s_first[kGroupList];  // their first particles
   const uint32_t slots = *a.count;
   for (uint32_t slot = blockIdx.x; slot < slots; slot += gridDim.x) {
     const int cell = a.cell[slot];
@@ -937,6 +942,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
         h_cnt[h] = 0;
         h_first[h] = INT_MAX;
       }
+      if (threadIdx.x == 0) s_ng = 0;
       __syncthreads();
       for (int k = threadIdx.x; k < m; k += kGroupThreads) {
         const GroupKey<kWhat> key(a, b + k);
@@ -948,6 +954,8 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
             o = atomicCAS(&h_owner[h], -1, k);
             if (o < 0) {
               found = h;  // claimed: a new group
+              const int e = atomicAdd(&s_ng, 1);
+              if (e < kGroupList) s_list[e] = h;
               break;
             }
           }
@@ -965,9 +973,25 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
         a.id[b + k] = found;
       }
       __syncthreads();
-      // groups in order of their first particle: an ordered scan over the particles
-      int ng = 0;
-      for (int k0 = 0; k0 < m; k0 += kGroupThreads) {
+      // groups in order of their first particle: few groups are ranked by
+      // counting in shared memory, many by an ordered scan over the particles
+      int ng = s_ng;
+      if (ng <= kGroupList) {
+        for (int e = threadIdx.x; e < ng; e += kGroupThreads) s_first[e] = h_first[s_list[e]];
+        __syncthreads();
+        for (int e = threadIdx.x; e < ng; e += kGroupThreads) {
+          const int f = s_first[e], h = s_list[e];
+          int r = 0;
+          for (int u = 0; u < ng; ++u) r += s_first[u] < f;
+          h_rank[h] = r;
+          a.rep[t0 + r] = b + f;
+          a.cnt[t0 + r] = h_cnt[h];
+          a.pos[t0 + r] = a.X[b + f];
+          if constexpr (kWhat == kGroupsXsph) a.aux[t0 + r] = a.V[b + f];
+        }
+      }
+      if (ng > kGroupList) ng = 0;
+      for (int k0 = 0; s_ng > kGroupList && k0 < m; k0 += kGroupThreads) {
         const int k = k0 + threadIdx.x;
         const int h = k < m ? a.id[b + k] : 0;
         const bool first = k < m && h_first[h] == k;

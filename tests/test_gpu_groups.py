@@ -143,6 +143,28 @@ def test_grouped_cells_with_nonfinite_neighbours(pbf, oracle, cuda, niter):
     assert np.abs(got["npos"][:, :3][fin] - r["npos"][:, :3][fin]).max() <= TOL_X + 3 * port
 
 
+@pytest.mark.parametrize("distinct", [1000, 6000])
+def test_grouped_cell_with_many_groups(pbf, oracle, cuda, distinct):
+    """One cell holding `distinct` random positions, each taken by 1-3
+    particles: groups ranked in shared memory (up to 4096 groups) or by the
+    ordered block scan (more).  Error percentiles against FP64 as for
+    touching clusters (the pile is ill-conditioned)."""
+    rng = np.random.default_rng(distinct)
+    base = rng.uniform(0.405, 0.495, size=(distinct, 3)).astype(np.float32)
+    reps = rng.integers(1, 4, size=distinct)
+    pts = np.repeat(base, reps, axis=0)
+    pos = np.zeros((len(pts), 4), np.float32)
+    pos[:, :3] = pts
+    lat = pbf.scenes.lattice((6, 6, 6), (0.1, 0.1, 0.5), rng)
+    pos = np.concatenate([pos, lat])
+    vel = np.zeros_like(pos)
+    pos = pos[rng.permutation(len(pos))]
+    p = ref_params(pbf, 2)
+    box = ((0.9, 0.9, 0.9), (0.0, 0.0, 0.0))
+    got = gpu_step(pbf, p, *box, pos, vel)
+    check_fp64(oracle, p, *box, pos, vel, got, conditioned=False)
+
+
 def test_grouped_cells_deterministic(pbf, cuda):
     pos, vel = clustered(pbf, seed=2)
     p = ref_params(pbf, 4)
