@@ -431,8 +431,9 @@ def run_ensemble(args):
     """Ensemble scenes/s: 256 independent dam-break scenes (a x b x c lattices,
     a, b, c uniform in [12, 40], each in its own (2a d, 2b d, 2c d) box), one
     scene-step = one scene advanced one step.  Batched (pbf_batch_step: one
-    launch per pass for all scenes) vs one scene per launch (256 solvers
-    stepped in turn), same steps, same stream, CUDA events."""
+    launch per pass for all scenes, dense-kernel choices from
+    pbf_batch_autotune after the warm-up) vs one scene per launch (256
+    solvers stepped in turn), same steps, same stream, CUDA events."""
     import torch
 
     pkg = load_pkg()
@@ -446,11 +447,12 @@ def run_ensemble(args):
     stream = torch.cuda.current_stream()
     counts = [sc.n for sc in scenes]
     pos = np.concatenate([sc.pos for sc in scenes])
-    # batched
+    # batched, with the dense-kernel choices autotuned on the warmed-up state
     st = pkg.ParticleState(pos, np.zeros_like(pos))
     ens = pkg.Ensemble(p, [sc.ulim for sc in scenes], [sc.llim for sc in scenes], counts)
     for _ in range(args.warmup):
         st.step(ens)
+    tuning = ens.autotune(st.pos, st.vel, st.iid, steps=2)
     torch.cuda.synchronize()
     torch.cuda._sleep(5_000_000)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -486,6 +488,7 @@ def run_ensemble(args):
         "config": {"workload": f"{len(scenes)} dam-break scenes, a,b,c ~ U{{12..40}} (seed 0), "
                                f"{sum(counts)} particles, {p.niter} iterations, dt=1/120 s",
                    "params": args.params, "particles": sum(counts)},
+        "autotune": tuning,
         "one_scene_per_launch": {"value": k / (single_ms / 1e3), "ms_per_step": single_ms / args.steps},
         "batched_over_per_scene": single_ms / batched_ms,
     }

@@ -230,6 +230,30 @@ pbf_status pbf_batch_get_density(const pbf_batch* b, float* rho, void* stream);
 pbf_status pbf_batch_use_graphs(pbf_batch* b, int on);
 
 /*
+ * Autotuning (no counterpart in the reference).  Times a few choices of how
+ * the neighbour passes split their work -- the window size above which a
+ * warp's 32 particles take the dense kernel (a block of 8 warps splitting
+ * each window), and whether every warp does -- by running `steps` steps per
+ * choice from copies of the caller's state (pos, vel, iid: device, n entries;
+ * they are not modified), and keeps the fastest for the solver's following
+ * steps.  The choices change the order in which window sums are added, so
+ * results differ by rounding only.  The trial steps are not taped.  The cell
+ * size stays h: with the reference's stale grid, another cell size would
+ * change which neighbours a step sees.
+ */
+typedef struct pbf_tuning {
+  int dense_window;   /* candidates above which a warp takes the dense kernel */
+  int dense_all;      /* 1: every warp takes the dense kernel */
+  float ms_per_step;  /* the chosen configuration's time per step */
+  float ms_default;   /* the default configuration's time per step */
+} pbf_tuning;
+
+pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
+                        pbf_tuning* out, void* stream);
+pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, const uint32_t* iid, int steps,
+                              pbf_tuning* out, void* stream);
+
+/*
  * One step, same contract and results as pbf_step, for callers that cannot
  * allocate device memory (no pbf_solver, so no pbf_create).  It has no
  * counterpart in the reference.  It calls no cudaMalloc or cudaFree: its

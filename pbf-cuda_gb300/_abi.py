@@ -47,6 +47,8 @@ EXPORTED = (
     "pbf_batch_step",
     "pbf_batch_get_density",
     "pbf_batch_use_graphs",
+    "pbf_autotune",
+    "pbf_batch_autotune",
     "pbf_step_noalloc",
 )
 
@@ -108,6 +110,16 @@ class PbfStepProfile(ctypes.Structure):
         return {name: getattr(self, name) for name, _ in self._fields_}
 
 
+class PbfTuning(ctypes.Structure):
+    """Mirror of ``pbf_tuning`` (include/pbf.h)."""
+
+    _fields_ = [("dense_window", ctypes.c_int), ("dense_all", ctypes.c_int),
+                ("ms_per_step", ctypes.c_float), ("ms_default", ctypes.c_float)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class PbfError(RuntimeError):
     """A pbf_* call returned a status other than PBF_OK."""
 
@@ -153,6 +165,8 @@ def _declare(L) -> None:
         "pbf_batch_step": (ctypes.c_int, [vp, vp, vp, vp, vp, vp, vp]),
         "pbf_batch_get_density": (ctypes.c_int, [vp, vp, vp]),
         "pbf_batch_use_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pbf_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]),
+        "pbf_batch_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, vp, vp]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
     }
     for name, (res, args) in sig.items():

@@ -64,6 +64,9 @@ struct pbf_solver {
   unsigned long long* bw8;   // 2 * max_particles: packed grid cells, packed current cells
   float* wall_part;          // 6 * blocks
   const uint32_t* last_perm;
+  // dense-kernel choices (pbf_autotune); tune_window 0: the defaults
+  int tune_window;
+  int tune_all;
 };
 
 namespace {
@@ -204,6 +207,8 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   c.geom = make_geom(p, ulim, llim, dims, 0);
   c.cells = dims[0] * dims[1] * dims[2];
   c.dense_grid = 4 * (num_sms > 0 ? num_sms : 1);
+  c.dense_window = pbf::kDefaultDenseWindow;
+  c.dense_all = -1;
   return c;
 }
 
@@ -348,6 +353,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   pbf_solver* s = new (std::nothrow) pbf_solver;
   if (!s) return fail(PBF_ERR_CAPACITY, "host allocation failed");
   std::memset(s, 0, sizeof(*s));
+  s->tune_all = -1;
   s->params = *params;
   std::memcpy(s->ulim, ulim, sizeof(s->ulim));
   std::memcpy(s->llim, llim, sizeof(s->llim));
@@ -599,6 +605,8 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   s->prof_iters = 0;
   StepPlan P;
   P.c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
+  if (s->tune_window > 0) P.c.dense_window = s->tune_window;
+  P.c.dense_all = s->tune_all;
   P.G = pbf::Geometry{nullptr, nullptr};
   P.grid = &s->grid;
   P.sol = &s->sol;
@@ -863,6 +871,8 @@ struct pbf_batch {
   bool use_graph;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
+  int tune_window = 0;  // dense-kernel choices (pbf_batch_autotune); 0: the defaults
+  int tune_all = -1;
 };
 
 namespace {
@@ -1033,6 +1043,8 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   int unit_dims[3] = {1, 1, 1};
   P.c = make_consts(b->params, &b->ulim[0], &b->llim[0], unit_dims, b->num_sms);
   P.c.cells = (int)cells;
+  if (b->tune_window > 0) P.c.dense_window = b->tune_window;
+  P.c.dense_all = b->tune_all;
   P.G = pbf::Geometry{b->d_geom, b->d_sid};
   P.grid = &b->grid;
   P.sol = &b->sol;
@@ -1092,6 +1104,130 @@ pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], 
   PBF_CUDA(pbf::density_grid_backward((const float4*)pos, n, lo, hi, dims, h, g_grid, (float4*)g_pos,
                                       (cudaStream_t)stream),
            "pbf_density_grid_backward");
+  return PBF_OK;
+}
+
+}  // extern "C"
+
+// ---- autotuning ------------------------------------------------------------------------
+
+namespace {
+
+// Candidate dense-kernel choices, timed by pbf_autotune / pbf_batch_autotune.
+constexpr int kTuneWindows[] = {256, 512, 1024, 2048};
+
+// Runs `steps` steps per candidate on copies of (pos, vel, iid) through
+// step(window, all, bufs...) and returns the fastest choice.
+template <class Step>
+pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid, int steps, cudaStream_t st,
+                    Step step, pbf_tuning* out) {
+  if (!pos || !vel || !iid || !out || n <= 0 || steps < 1)
+    return fail(PBF_ERR_INVALID_ARG, "NULL argument, n <= 0 or steps < 1");
+  float4 *p[2] = {nullptr, nullptr}, *v[2] = {nullptr, nullptr};
+  uint32_t* id = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = alloc(&p[0], (size_t)n);
+  if (e == cudaSuccess) e = alloc(&p[1], (size_t)n);
+  if (e == cudaSuccess) e = alloc(&v[0], (size_t)n);
+  if (e == cudaSuccess) e = alloc(&v[1], (size_t)n);
+  if (e == cudaSuccess) e = alloc(&id, (size_t)n);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  pbf_status result = PBF_OK;
+  float best = -1.f, def_ms = -1.f;
+  int best_w = pbf::kDefaultDenseWindow, best_all = -1;
+  for (int all = 0; all <= 1 && e == cudaSuccess && result == PBF_OK; ++all) {
+    for (int w : kTuneWindows) {
+      if (all == 1 && w != pbf::kDefaultDenseWindow) continue;  // the window plays no part then
+      e = cudaMemcpyAsync(p[0], pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(v[0], vel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(id, iid, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) break;
+      int cur = 0;
+      float ms = 0.f;
+      for (int k = -1; k < steps && result == PBF_OK; ++k) {  // one untimed step first
+        if (k == 0) e = cudaEventRecord(e0, st);
+        result = step(w, all, p[cur], p[1 - cur], v[cur], v[1 - cur], id, st);
+        cur = 1 - cur;
+      }
+      if (result != PBF_OK) break;
+      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (e != cudaSuccess) break;
+      ms /= (float)steps;
+      const bool is_default = w == pbf::kDefaultDenseWindow && all == (n < pbf::kDenseAllBelow ? 1 : 0);
+      if (is_default) def_ms = ms;
+      if (best < 0.f || ms < best) {
+        best = ms;
+        best_w = w;
+        best_all = all;
+      }
+    }
+  }
+  for (void* q : {(void*)p[0], (void*)p[1], (void*)v[0], (void*)v[1], (void*)id})
+    if (q) cudaFree(q);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (result != PBF_OK) return result;
+  if (e != cudaSuccess) return cuda_fail(e, "pbf_autotune");
+  out->dense_window = best_w;
+  out->dense_all = best_all;
+  out->ms_per_step = best;
+  out->ms_default = def_ms;
+  return PBF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
+                        pbf_tuning* out, void* stream) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
+  const int depth = s->tape_depth, top = s->tape_top;
+  s->tape_depth = 0;  // the trial steps are not taped
+  const int w0 = s->tune_window, a0 = s->tune_all;
+  const pbf_status st = autotune(
+      n, pos, vel, iid, steps, (cudaStream_t)stream,
+      [&](int w, int all, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+        s->tune_window = w;
+        s->tune_all = all;
+        return pbf_step(s, p, np, v, nv, id, n, strm);
+      },
+      out);
+  s->tape_depth = depth;
+  s->tape_top = top;
+  if (st != PBF_OK) {
+    s->tune_window = w0;
+    s->tune_all = a0;
+    return st;
+  }
+  s->tune_window = out->dense_window;
+  s->tune_all = out->dense_all;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, const uint32_t* iid, int steps,
+                              pbf_tuning* out, void* stream) {
+  if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+  const int w0 = b->tune_window, a0 = b->tune_all;
+  const pbf_status st = autotune(
+      b->n, pos, vel, iid, steps, (cudaStream_t)stream,
+      [&](int w, int all, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+        b->tune_window = w;
+        b->tune_all = all;
+        return pbf_batch_step(b, p, np, v, nv, id, strm);
+      },
+      out);
+  if (st != PBF_OK) {
+    b->tune_window = w0;
+    b->tune_all = a0;
+    return st;
+  }
+  b->tune_window = out->dense_window;
+  b->tune_all = out->dense_all;
   return PBF_OK;
 }
 

@@ -42,6 +42,8 @@ struct StepConsts {
   float g[3];              // gravity vector = -g * up
   int cells;               // cells of all scenes
   int dense_grid;          // blocks of the dense neighbour kernels (a multiple of the SM count)
+  int dense_window;        // candidates above which a warp takes the dense kernel
+  int dense_all;           // 1: every warp takes the dense kernel; 0: never; -1: by particle count
   SceneGeom geom;          // the box of a single-scene step
 };
 
@@ -258,6 +260,11 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const f
 // XSPH: nvel = vel + c sum_j 2 (v_j - v_i) W / (rho_i + rho_j).
 cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X, const float4* V, const uint32_t* cs,
                         int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream);
+
+// Candidates above which a warp takes the dense kernel, and the particle
+// count below which every warp does (defaults; pbf_autotune can override).
+constexpr int kDefaultDenseWindow = 512;
+constexpr int kDenseAllBelow = 131072;
 
 // Kernel launches of one neighbour pass.
 constexpr int kLaunchesPerPass = 3;

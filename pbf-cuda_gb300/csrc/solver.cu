@@ -18,13 +18,13 @@
 //
 // Each pass is two kernels.  The sparse kernel gives every particle one
 // thread and walks its window in a compact loop (fluid at rest: ~200
-// candidates).  A warp in which some window exceeds kDenseWindow candidates
+// candidates).  A warp in which some window exceeds dense_window candidates
 // (particles piled into a few cells) instead appends itself to a dense list
 // and returns; the dense kernel then gives each listed warp a block of
 // kDenseWarps warps, each walking one contiguous chunk of every lane's
 // window, and adds the chunks' partial sums in chunk order in shared memory.
 // Steps of fewer than kDenseAllBelow particles send every warp to the dense
-// kernel (one thread per particle would leave most SMs idle).  Both orders
+// kernel by default (one thread per particle would leave most SMs idle).  Both orders
 // are fixed, so results stay deterministic; they differ from the reference's
 // sequential sums only by rounding.
 //
@@ -48,10 +48,10 @@ namespace {
 constexpr int kSparseThreads = 128;
 constexpr int kDenseWarps = 8;                  // chunks of a dense warp's windows
 constexpr int kDenseThreads = 32 * kDenseWarps;
-constexpr int kDenseWindow = 512;               // candidates above which a warp goes dense
-// Below this many particles one thread per particle leaves most of the GPU
-// idle: every warp then takes the dense kernel (8 warps per 32 particles).
-constexpr int kDenseAllBelow = 131072;
+// Below kDenseAllBelow particles one thread per particle leaves most of the
+// GPU idle: by default every warp then takes the dense kernel (8 warps per 32
+// particles).  StepConsts::dense_window / dense_all override the defaults
+// (pbf_autotune).
 constexpr int kMaxFields = 6;                   // partial-sum fields of the largest pass
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -652,7 +652,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
   const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
   const int3 q = cell_of(a.c, g, xi);
   const int total = valid ? window_total(g, a.cs, a.n, q) : 0;
-  if (__any_sync(kFull, total > kDenseWindow)) {
+  if (__any_sync(kFull, total > a.c.dense_window)) {
     if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(i >> 5);
     return;
   }
@@ -1069,7 +1069,7 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.X = X;
   a.cs = cs;
   a.n = n;
-  a.dense_all = n < kDenseAllBelow;
+  a.dense_all = c.dense_all >= 0 ? c.dense_all : n < kDenseAllBelow;
   a.counter = kDenseCount0 + (pass & 1);
   a.next_counter = kDenseCount0 + ((pass + 1) & 1);
   a.flags = s.flags;

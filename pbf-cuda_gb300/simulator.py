@@ -13,7 +13,7 @@ from typing import Optional, Sequence
 
 import torch
 
-from ._abi import PBF_ERR_NOT_READY, PbfParams, PbfStepProfile, check, lib
+from ._abi import PBF_ERR_NOT_READY, PbfParams, PbfStepProfile, PbfTuning, check, lib
 
 
 def _vec3(v: Sequence[float]) -> ctypes.Array:
@@ -153,6 +153,18 @@ class Simulator:
                                    g_vel.data_ptr(), g_lim.data_ptr(), _stream_handle(stream)), "pbf_backward")
         return g_pos, g_vel, g_lim
 
+    def autotune(self, pos: torch.Tensor, vel: torch.Tensor, iid: torch.Tensor, nparticle: Optional[int] = None,
+                 steps: int = 3, stream=None) -> dict:
+        """Time the dense-kernel choices on copies of this state (pbf_autotune)
+        and keep the fastest; returns the choice and its time per step."""
+        n = pos.shape[0] if nparticle is None else int(nparticle)
+        for t, name, cols in ((pos, "pos", 4), (vel, "vel", 4), (iid, "iid", None)):
+            _check_state(t, name, n, cols)
+        out = PbfTuning()
+        check(self._L.pbf_autotune(self._h, pos.data_ptr(), vel.data_ptr(), iid.data_ptr(), n, int(steps),
+                                   ctypes.byref(out), _stream_handle(stream)), "pbf_autotune")
+        return out.as_dict()
+
     def profile(self, on: bool = True) -> None:
         """Record CUDA events between the phases of every following step."""
         check(self._L.pbf_profile_enable(self._h, int(bool(on))), "pbf_profile_enable")
@@ -268,6 +280,14 @@ class Ensemble:
         check(self._L.pbf_batch_get_density(self._h, out.data_ptr(), _stream_handle(stream)),
               "pbf_batch_get_density")
         return out[: self.n]
+
+    def autotune(self, pos: torch.Tensor, vel: torch.Tensor, iid: torch.Tensor, steps: int = 3,
+                 stream=None) -> dict:
+        """pbf_batch_autotune on copies of this state; returns the choice."""
+        out = PbfTuning()
+        check(self._L.pbf_batch_autotune(self._h, pos.data_ptr(), vel.data_ptr(), iid.data_ptr(), int(steps),
+                                         ctypes.byref(out), _stream_handle(stream)), "pbf_batch_autotune")
+        return out.as_dict()
 
     def use_graphs(self, on: bool = True) -> None:
         check(self._L.pbf_batch_use_graphs(self._h, int(bool(on))), "pbf_batch_use_graphs")
