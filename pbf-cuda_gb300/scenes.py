@@ -14,9 +14,13 @@ iids for a box) with seeded numpy jitter and y up:
                 box whose x-max wall moves as x_w(t) = 12.8 - 1.6 (1 - cos(2 pi t / 4 s))
   ensemble      256 independent a x b x c lattices, a, b, c uniform in [12, 40],
                 each in its own (2a d, 2b d, 2c d) box
-  inverse       15,625 particles: 25x25x25 lattice in a 2.0 x 1.0 x 1.0 box
+  inverse       15,625 particles: 25x25x25 lattice (spacing 0.04) in a 2.0 x 1.0 x 1.0 box
+  clustered     1,048,576 particles: a 64^3 lattice plus six collapsed clusters
+                in the large sweep's box (the grouped-cell profiling case)
 
 Lattice spacing d = 0.05, jitter uniform +-0.005 per coordinate, velocities 0.
+save_state / load_state keep a particle state (float4 positions, float4
+velocities, uint32 iids) in one raw binary file for fixtures and restarts.
 """
 from __future__ import annotations
 
@@ -201,3 +205,50 @@ SCENES = {
     "clustered": clustered,
     "inverse": inverse_scene,
 }
+
+
+# ---- particle state files ---------------------------------------------------------------
+
+_STATE_MAGIC = b"PBFSTATE"
+
+
+def save_state(path, pos, vel, iid) -> None:
+    """Write n particles to `path`: the 8-byte magic, n (uint64, little
+    endian), then pos (n x 4 float32), vel (n x 4 float32), iid (n uint32),
+    all little endian.  Accepts numpy arrays or CUDA tensors (copied to the
+    host); (n, 3) arrays get w = 0."""
+    def host(a, dtype, cols):
+        a = a.detach().cpu().numpy() if hasattr(a, "detach") else np.asarray(a)
+        a = np.asarray(a, dtype=dtype)
+        if cols and a.shape[1] == 3:
+            a = np.concatenate([a, np.zeros((a.shape[0], 1), dtype)], 1)
+        return np.ascontiguousarray(a)
+    p = host(pos, "<f4", 4)
+    v = host(vel, "<f4", 4)
+    i = host(iid, "<u4", 0).reshape(-1)
+    n = p.shape[0]
+    if v.shape != (n, 4) or i.shape != (n,):
+        raise ValueError("pos, vel and iid must hold the same number of particles")
+    with open(path, "wb") as f:
+        f.write(_STATE_MAGIC)
+        f.write(np.uint64(n).astype("<u8").tobytes())
+        f.write(p.tobytes())
+        f.write(v.tobytes())
+        f.write(i.tobytes())
+
+
+def load_state(path):
+    """Read a file written by save_state: (pos (n, 4) float32, vel (n, 4)
+    float32, iid (n,) uint32)."""
+    with open(path, "rb") as f:
+        if f.read(8) != _STATE_MAGIC:
+            raise ValueError(f"{path}: not a particle state file")
+        n = int(np.frombuffer(f.read(8), "<u8")[0])
+        body = f.read()
+    need = n * (16 + 16 + 4)
+    if len(body) != need:
+        raise ValueError(f"{path}: {len(body)} bytes of particle data, expected {need}")
+    pos = np.frombuffer(body, "<f4", n * 4, 0).reshape(n, 4).astype(np.float32)
+    vel = np.frombuffer(body, "<f4", n * 4, n * 16).reshape(n, 4).astype(np.float32)
+    iid = np.frombuffer(body, "<u4", n, n * 32).astype(np.uint32)
+    return pos, vel, iid

@@ -4,6 +4,7 @@ from __future__ import annotations
 import math
 
 import numpy as np
+import pytest
 
 
 def test_rest_density_is_the_lattice_poly6_sum(pbf):
@@ -73,3 +74,22 @@ def test_scene_params(pbf):
     assert p.n_corr == 4.0 and abs(p.c_XSPH - 0.01) < 1e-9
     assert list(p.up) == [0.0, 1.0, 0.0]
     assert abs(p.dt - 1.0 / 120.0) < 1e-9
+
+
+def test_state_file_round_trip(pbf, tmp_path):
+    s = pbf.scenes
+    sc = s.dam_break(seed=2)
+    rng = np.random.default_rng(0)
+    vel = rng.normal(size=(sc.n, 3)).astype(np.float32)
+    iid = rng.permutation(sc.n).astype(np.uint32)
+    path = tmp_path / "state.bin"
+    s.save_state(path, sc.pos, vel, iid)
+    assert path.stat().st_size == 16 + sc.n * 36
+    pos2, vel2, iid2 = s.load_state(path)
+    np.testing.assert_array_equal(pos2, sc.pos)
+    np.testing.assert_array_equal(vel2[:, :3], vel)
+    assert np.all(vel2[:, 3] == 0)
+    np.testing.assert_array_equal(iid2, iid)
+    path.write_bytes(path.read_bytes()[:-4])
+    with pytest.raises(ValueError):
+        s.load_state(path)
