@@ -777,6 +777,7 @@ template <int kWhat>
 struct GroupKey {
   static constexpr int kWords = kWhat == kGroupsXsph ? 4 : 3;
   uint32_t w[kWords];
+  GroupKey() = default;
   __device__ __forceinline__ GroupKey(const GroupArgs& a, int j) {
     const float4 x = a.X[j];
     w[0] = __float_as_uint(x.x), w[1] = __float_as_uint(x.y), w[2] = __float_as_uint(x.z);
@@ -831,15 +832,25 @@ __device__ __forceinline__ int block_scan(int flag, int* sh, int& total) {
 // rep_val(g), C components: exact to 2^-62 of the bound max|dev| * count,
 // order-free.  Writes out(g, c, sum) for each group; false if some deviation
 // is not finite (other than between identical bits).
-template <int C, class Val, class RepVal, class Out>
-__device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val val, RepVal rep_val, Out out,
-                           int* s_flag) {
+// `cache` (kGroupCacheFloats floats of shared memory) holds the groups'
+// first-particle values when they fit, saving two dependent loads per particle.
+constexpr int kGroupCacheFloats = 2 * 4096;
+
+template <int C, class Val, class RepVal0, class Out>
+__device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val val, RepVal0 rep_val0, Out out,
+                           int* s_flag, float* cache) {
+  const bool cached = ng * C <= kGroupCacheFloats;
   if (threadIdx.x == 0) *s_flag = 0;
   for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
     a.gmax[t0 + g] = 0u;
-    for (int c = 0; c < C; ++c) a.acc[3 * (t0 + g) + c] = 0ull;
+    for (int c = 0; c < C; ++c) {
+      a.acc[3 * (t0 + g) + c] = 0ull;
+      if (cached) cache[g * C + c] = rep_val0(g, c);
+    }
   }
   __syncthreads();
+  auto rep_val = [&](int g, int c) { return cached ? cache[g * C + c] : rep_val0(g, c); };
+#pragma unroll 4
   for (int k = threadIdx.x; k < m; k += kGroupThreads) {
     const int g = a.id[b + k];
     float d = 0.f;
@@ -859,6 +870,7 @@ __device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val
     if (!isfinite(__uint_as_float(a.gmax[t0 + g]))) atomicOr(s_flag, 1);
   __syncthreads();
   if (*s_flag) return false;
+#pragma unroll 4
   for (int k = threadIdx.x; k < m; k += kGroupThreads) {
     const int g = a.id[b + k];
     const float mx = __uint_as_float(a.gmax[t0 + g]);
@@ -909,8 +921,10 @@ template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
   __shared__ int sh[80];
   __shared__ int s_flag, s_ng;
-  __shared__ int s_list[kGroupList];   // hash entries claimed (any order)
-  __shared__ int s_first[kGroupList];  // their first particles
+  __shared__ int s_buf[2 * kGroupList];  // the build's claimed entries and their first
+                                         // particles, then group_sums' cache
+  int* s_list = s_buf;                   // hash entries claimed (any order)
+  int* s_first = s_buf + kGroupList;     // their first particles
   const uint32_t slots = *a.count;
   for (uint32_t slot = blockIdx.x; slot < slots; slot += gridDim.x) {
     const int cell = a.cell[slot];
@@ -924,7 +938,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
           a, b, m, t0, ng, [&](int k, int) { return a.lambda[b + k]; },
           [&](int g, int) { return a.lambda[a.rep[t0 + g]]; },
           [&](int g, int, float v) { a.sum[t0 + g] = make_float4(a.lambda[a.rep[t0 + g]], v, 0.f, 0.f); },
-          &s_flag);
+          &s_flag, reinterpret_cast<float*>(s_buf));
       if (!ok && threadIdx.x == 0) a.ng[slot] = -1;
       __syncthreads();
     } else {
@@ -944,33 +958,56 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
       }
       if (threadIdx.x == 0) s_ng = 0;
       __syncthreads();
-      for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-        const GroupKey<kWhat> key(a, b + k);
-        int h = (int)(key.hash() % (uint32_t)H);
-        int found = -1;
-        for (int probe = 0; probe < H; ++probe, h = h + 1 == H ? 0 : h + 1) {
-          int o = *(volatile int*)&h_owner[h];
-          if (o < 0) {
-            o = atomicCAS(&h_owner[h], -1, k);
-            if (o < 0) {
-              found = h;  // claimed: a new group
-              const int e = atomicAdd(&s_ng, 1);
-              if (e < kGroupList) s_list[e] = h;
-              break;
+      // kUnroll particles per thread per round: their loads are independent,
+      // so several probe chains are in flight at once
+      constexpr int kUnroll = 4;
+      for (int k0 = threadIdx.x; k0 < m; k0 += kUnroll * kGroupThreads) {
+        int found[kUnroll];
+        GroupKey<kWhat> key[kUnroll];
+        int h[kUnroll], o[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+          const int k = min(k0 + u * kGroupThreads, m - 1);
+          key[u] = GroupKey<kWhat>(a, b + k);
+          h[u] = (int)(key[u].hash() % (uint32_t)H);
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) o[u] = *(volatile int*)&h_owner[h[u]];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)  // the common case: the first entry holds the key
+          found[u] = o[u] >= 0 && GroupKey<kWhat>(a, b + o[u]) == key[u] ? h[u] : -1;
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+          const int k = k0 + u * kGroupThreads;
+          if (k < m && found[u] < 0) {
+            int hh = h[u];
+            for (int probe = 0; probe < H; ++probe, hh = hh + 1 == H ? 0 : hh + 1) {
+              int ow = *(volatile int*)&h_owner[hh];
+              if (ow < 0) {
+                ow = atomicCAS(&h_owner[hh], -1, k);
+                if (ow < 0) {
+                  found[u] = hh;  // claimed: a new group
+                  const int e = atomicAdd(&s_ng, 1);
+                  if (e < kGroupList) s_list[e] = hh;
+                  break;
+                }
+              }
+              if (GroupKey<kWhat>(a, b + ow) == key[u]) {
+                found[u] = hh;
+                break;
+              }
             }
+            // H = 2m entries for at most m keys: a probe always ends
           }
-          if (GroupKey<kWhat>(a, b + o) == key) {
-            found = h;
-            break;
+          if (k < m) {
+            const unsigned act = __activemask(), same = __match_any_sync(act, found[u]);
+            if ((threadIdx.x & 31) == __ffs(same) - 1) {
+              atomicAdd(&h_cnt[found[u]], __popc(same));
+              atomicMin(&h_first[found[u]], k);  // the lowest lane holds the lowest k
+            }
+            a.id[b + k] = found[u];
           }
         }
-        // H = 2m entries for at most m keys: a probe always ends
-        const unsigned act = __activemask(), same = __match_any_sync(act, found);
-        if ((threadIdx.x & 31) == __ffs(same) - 1) {
-          atomicAdd(&h_cnt[found], __popc(same));
-          atomicMin(&h_first[found], k);  // the lowest lane holds the lowest k
-        }
-        a.id[b + k] = found;
       }
       __syncthreads();
       // groups in order of their first particle: few groups are ranked by
@@ -1024,7 +1061,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
                 s4.w = a.rho[a.rep[t0 + g]];
               }
             },
-            &s_flag);
+            &s_flag, reinterpret_cast<float*>(s_buf));
         if (!ok) ngw = -1;
       }
       if (threadIdx.x == 0) a.ng[slot] = ngw;
