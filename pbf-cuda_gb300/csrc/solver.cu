@@ -866,10 +866,19 @@ __device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val
     if ((threadIdx.x & 31) == __ffs(same) - 1) atomicMax(&a.gmax[t0 + g], mx);
   }
   __syncthreads();
-  for (int g = threadIdx.x; g < ng; g += kGroupThreads)
-    if (!isfinite(__uint_as_float(a.gmax[t0 + g]))) atomicOr(s_flag, 1);
+  for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+    const unsigned mx = a.gmax[t0 + g];
+    if (!isfinite(__uint_as_float(mx))) atomicOr(s_flag, 1);
+    if (mx != 0u) atomicOr(s_flag, 2);
+  }
   __syncthreads();
-  if (*s_flag) return false;
+  if (*s_flag & 1) return false;
+  if (!(*s_flag & 2)) {  // every member equals its group's first: all sums are 0
+    for (int g = threadIdx.x; g < ng; g += kGroupThreads)
+      for (int c = 0; c < C; ++c) out(g, c, 0.f);
+    __syncthreads();
+    return true;
+  }
 #pragma unroll 4
   for (int k = threadIdx.x; k < m; k += kGroupThreads) {
     const int g = a.id[b + k];
