@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 1
+#define PBF_ABI_VERSION 2
 
 typedef enum pbf_status {
   PBF_OK = 0,
@@ -61,6 +61,8 @@ typedef struct pbf_params {
   float lim_eps;             /* wall clamp inset; reference LIM_EPS = 1e-3 */
   float kernel_eps;          /* spiky-gradient cutoff; reference KERNAL_EPS = 1e-4 */
   float max_dp;              /* per-component delta_p clamp; reference MAX_DP = 0.1 */
+  float vorticity_eps;       /* vorticity confinement strength; 0 (default): off, as the
+                                reference, which has none (README.md:14 lists it as missing) */
 } pbf_params;
 
 typedef struct pbf_solver pbf_solver;

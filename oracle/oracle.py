@@ -44,6 +44,7 @@ class OracleParams(ctypes.Structure):
         ("lim_eps", ctypes.c_float),
         ("kernel_eps", ctypes.c_float),
         ("max_dp", ctypes.c_float),
+        ("vorticity_eps", ctypes.c_float),
     ]
 
 

@@ -429,6 +429,69 @@ static void xsph_pass(const consts* c, const pbf_params* p, const real* X, const
   }
 }
 
+/* Vorticity confinement (no counterpart in the reference; Macklin and
+ * Mueller 2013, eqs. 15-16) after XSPH, on its output U (positions X):
+ * omega_i = sum_{j != i} (u_j - u_i) x g_ij, eta_i = sum_{j != i} |omega_j| g_ij
+ * with g_ij = spiky(x_i - x_j) over the same windows, then
+ * u_i += dt eps (eta_i / |eta_i|) x omega_i. */
+static void vorticity_pass(const consts* c, const pbf_params* p, const real* X, const uint32_t* cs, int n,
+                           real* U) {
+  real* W = (real*)malloc(sizeof(real) * 4 * (size_t)(n > 0 ? n : 1));
+  for (int pass = 0; pass < 2; ++pass) {
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < n; ++i) {
+      const real* xi = X + 4 * (size_t)i;
+      const real* ui = U + 4 * (size_t)i;
+      int ind[3];
+      cell_xyz(c, xi, ind);
+      real acc[3] = {0, 0, 0};
+      for (int dx = -1; dx <= 1; ++dx) {
+        int x = ind[0] + dx;
+        if (x < 0 || x >= c->gd.dims[0]) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+          int y = ind[1] + dy;
+          if (y < 0 || y >= c->gd.dims[1]) continue;
+          int s, e;
+          column_run(c, cs, x, y, ind[2], &s, &e);
+          for (int j = s; j < e; ++j) {
+            if (j == i) continue;
+            const real* xj = X + 4 * (size_t)j;
+            real r[3] = {xi[0] - xj[0], xi[1] - xj[1], xi[2] - xj[2]};
+            real g[3];
+            spiky(c, r, g);
+            if (pass == 0) {
+              const real* uj = U + 4 * (size_t)j;
+              real d[3] = {uj[0] - ui[0], uj[1] - ui[1], uj[2] - ui[2]};
+              acc[0] += d[1] * g[2] - d[2] * g[1];
+              acc[1] += d[2] * g[0] - d[0] * g[2];
+              acc[2] += d[0] * g[1] - d[1] * g[0];
+            } else {
+              const real m = W[4 * (size_t)j + 3];
+              for (int a = 0; a < 3; ++a) acc[a] += m * g[a];
+            }
+          }
+        }
+      }
+      if (pass == 0) {
+        real* w = W + 4 * (size_t)i;
+        w[0] = acc[0], w[1] = acc[1], w[2] = acc[2];
+        w[3] = RSQRT(acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2]);
+      } else {
+        real len = RSQRT(acc[0] * acc[0] + acc[1] * acc[1] + acc[2] * acc[2]);
+        if (!(len > 0) || !isfinite(len)) continue;
+        const real* w = W + 4 * (size_t)i;
+        real nx = acc[0] / len, ny = acc[1] / len, nz = acc[2] / len;
+        real sc = (real)p->dt * (real)p->vorticity_eps;
+        real* u = U + 4 * (size_t)i;
+        u[0] += sc * (ny * w[2] - nz * w[1]);
+        u[1] += sc * (nz * w[0] - nx * w[2]);
+        u[2] += sc * (nx * w[1] - ny * w[0]);
+      }
+    }
+  }
+  free(W);
+}
+
 /*
  * One Simulator::step (fluids/Simulator.cpp:10-99) on host arrays, with the
  * same in/out contract as the GPU entry point pbf_step.  rho_out/lambda_out
@@ -492,6 +555,7 @@ int SFX(oracle_step)(const pbf_params* p, const float ulim[3], const float llim[
   }
   /* correctVelocity: XSPH with rho of the last lambda pass. */
   xsph_pass(&c, p, A, V, rho, cs, n, B);
+  if (p->vorticity_eps > 0) vorticity_pass(&c, p, A, cs, n, B);
 
   for (int k = 0; k < n; ++k) {
     size_t o = 4 * (size_t)k;

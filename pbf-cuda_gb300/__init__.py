@@ -10,10 +10,10 @@ __graft_entry__.py).
 from ._abi import (PBF_ERR_CAPACITY, PBF_ERR_CUDA, PBF_ERR_INVALID_ARG, PBF_ERR_NOT_READY, PBF_ERR_TIMEOUT,
                    PBF_OK, EXPORTED, PbfError, PbfParams, PbfStepProfile, PbfTuning, check, default_params, lib, lib_path)
 from .simulator import Ensemble, ParticleState, Simulator
-from . import adjoint, inverse, scenes
+from . import adjoint, driver, inverse, scenes
 
 __all__ = [
     "PBF_OK", "PBF_ERR_INVALID_ARG", "PBF_ERR_CAPACITY", "PBF_ERR_CUDA", "PBF_ERR_TIMEOUT",
     "PBF_ERR_NOT_READY", "EXPORTED", "PbfError", "PbfParams", "PbfStepProfile", "PbfTuning", "check", "default_params", "lib",
-    "lib_path", "Simulator", "ParticleState", "Ensemble", "adjoint", "inverse", "scenes",
+    "lib_path", "Simulator", "ParticleState", "Ensemble", "adjoint", "driver", "inverse", "scenes",
 ]

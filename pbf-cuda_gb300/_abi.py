@@ -73,6 +73,7 @@ class PbfParams(ctypes.Structure):
         ("lim_eps", ctypes.c_float),
         ("kernel_eps", ctypes.c_float),
         ("max_dp", ctypes.c_float),
+        ("vorticity_eps", ctypes.c_float),
     ]
 
     def copy(self) -> "PbfParams":

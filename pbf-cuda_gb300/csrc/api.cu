@@ -99,14 +99,14 @@ pbf_status check_params(const pbf_params* p) {
   if (p->niter < 1) return fail(PBF_ERR_INVALID_ARG, "niter must be >= 1 (got %d)", p->niter);
   const float vals[] = {p->pho0, p->g, p->h, p->dt, p->lambda_eps, p->delta_q, p->k_corr,
                         p->n_corr, p->k_boundaryDensity, p->c_XSPH, p->up[0], p->up[1],
-                        p->up[2], p->lim_eps, p->kernel_eps, p->max_dp};
+                        p->up[2], p->lim_eps, p->kernel_eps, p->max_dp, p->vorticity_eps};
   for (float v : vals)
     if (!finite_f(v)) return fail(PBF_ERR_INVALID_ARG, "params hold a non-finite value");
   if (!(p->h > 0.f)) return fail(PBF_ERR_INVALID_ARG, "h must be > 0");
   if (!(p->dt > 0.f)) return fail(PBF_ERR_INVALID_ARG, "dt must be > 0");
   if (!(p->pho0 > 0.f)) return fail(PBF_ERR_INVALID_ARG, "pho0 must be > 0");
-  if (p->max_dp < 0.f || p->lim_eps < 0.f || p->kernel_eps < 0.f)
-    return fail(PBF_ERR_INVALID_ARG, "max_dp, lim_eps and kernel_eps must be >= 0");
+  if (p->max_dp < 0.f || p->lim_eps < 0.f || p->kernel_eps < 0.f || p->vorticity_eps < 0.f)
+    return fail(PBF_ERR_INVALID_ARG, "max_dp, lim_eps, kernel_eps and vorticity_eps must be >= 0");
   return PBF_OK;
 }
 
@@ -199,6 +199,7 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
     if (p.n_corr == (float)k) c.npow = k;
   c.keps2 = p.kernel_eps * p.kernel_eps;
   c.max_dp = p.max_dp;
+  c.vort_eps = p.vorticity_eps;
   c.k_b = p.k_boundaryDensity;
   c.c_xsph = p.c_XSPH;
   c.dt = p.dt;
@@ -313,6 +314,7 @@ void pbf_params_default(pbf_params* out) {
   out->lim_eps = 1e-3f;
   out->kernel_eps = 1e-4f;
   out->max_dp = 0.1f;
+  out->vorticity_eps = 0.f;
 }
 
 const char* pbf_status_string(pbf_status s) {
@@ -530,6 +532,9 @@ pbf_status enqueue_step(const StepPlan& P, void* pos, void* npos, void* vel, voi
   PBF_CUDA(pbf::launch_xsph(c, G, (const float4*)npos, (const float4*)vel, cs, n, sol, 2 * niter,
                             (float4*)nvel, st_),
            "pbf_step: xsph");
+  if (c.vort_eps > 0.f)
+    PBF_CUDA(pbf::launch_vorticity(c, G, (const float4*)npos, cs, n, sol, (float4*)nvel, st_),
+             "pbf_step: vorticity");
   PBF_EV(P.ev[kEvEnd]);
   // the rest of the record: sorted inputs, last density, permutation, cell prefix
   PBF_TAPE(P.tape + P.tape_xs, P.sol->xs, sizeof(float4) * n);
@@ -617,8 +622,8 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   if (taping && s->params.niter > s->tape_iters)
     return fail(PBF_ERR_CAPACITY, "tape records hold %d iterations, params ask for %d (re-enable the tape)",
                 s->tape_iters, s->params.niter);
-  if (taping && s->params.k_boundaryDensity != 0.f)
-    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
+  if (taping && (s->params.k_boundaryDensity != 0.f || s->params.vorticity_eps != 0.f))
+    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0 and vorticity_eps == 0");
   if (taping && s->tape_top >= s->tape_depth)
     return fail(PBF_ERR_CAPACITY, "the tape holds %d taped steps: run pbf_backward or re-enable the tape",
                 s->tape_depth);
@@ -634,7 +639,8 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   if (st != PBF_OK) return st;
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
-  s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1);
+  s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1) +
+                     (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
   if (taping) {
@@ -652,8 +658,8 @@ pbf_status pbf_tape_enable(pbf_solver* s, int depth) {
     return PBF_OK;
   }
   s->tape_depth = 0;
-  if (s->params.k_boundaryDensity != 0.f)
-    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0");
+  if (s->params.k_boundaryDensity != 0.f || s->params.vorticity_eps != 0.f)
+    return fail(PBF_ERR_INVALID_ARG, "the reverse pass needs k_boundaryDensity == 0 and vorticity_eps == 0");
   if (depth > kMaxTapeDepth) return fail(PBF_ERR_CAPACITY, "at most %d taped steps", kMaxTapeDepth);
   const int iters = s->params.niter;
   if (iters > pbf::kMaxTapeIters) return fail(PBF_ERR_CAPACITY, "at most %d taped iterations", pbf::kMaxTapeIters);

@@ -194,5 +194,8 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   if ((e = pbf::launch_xsph(c, G, (const float4*)npos, (const float4*)vel, g.cell_start, n, s, 2 * niter,
                             (float4*)nvel, strm)) != cudaSuccess)
     return pbf::set_cuda_error(e, "pbf_step_noalloc: xsph");
+  if (c.vort_eps > 0.f &&
+      (e = pbf::launch_vorticity(c, G, (const float4*)npos, g.cell_start, n, s, (float4*)nvel, strm)) != cudaSuccess)
+    return pbf::set_cuda_error(e, "pbf_step_noalloc: vorticity");
   return PBF_OK;
 }

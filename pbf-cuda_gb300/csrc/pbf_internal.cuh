@@ -36,6 +36,7 @@ struct StepConsts {
   int npow;                // n_corr as a small positive integer, or -1
   float keps2;             // kernel_eps^2: spiky gradient is zero for |r| < kernel_eps
   float max_dp;
+  float vort_eps;          // vorticity confinement strength (0: off)
   float k_b;               // k_boundaryDensity
   float c_xsph;
   float dt, inv_dt;
@@ -265,6 +266,16 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
 // count below which every warp does (defaults; pbf_autotune can override).
 constexpr int kDefaultDenseWindow = 512;
 constexpr int kDenseAllBelow = 131072;
+
+// Vorticity confinement after XSPH, on its output NV (positions X = npos):
+// omega_i = sum_j (u_j - u_i) x g_ij and eta_i = sum_j |omega_j| g_ij over
+// the neighbours j != i with kernel_eps <= r < h, g_ij the spiky gradient
+// grad W(x_i - x_j); then u_i += dt eps (eta_i / |eta_i|) x omega_i (Macklin
+// and Mueller 2013, eqs. 15-16).  Scratch: s.xb holds omega (free after the
+// last position update).
+cudaError_t launch_vorticity(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
+                             const SolverScratch& s, float4* NV, cudaStream_t stream);
+constexpr int kVorticityLaunches = 2;
 
 // Kernel launches of one neighbour pass.
 constexpr int kLaunchesPerPass = 3;

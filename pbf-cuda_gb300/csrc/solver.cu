@@ -1186,6 +1186,98 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const f
   return run_pass<kDeltaPFinal>(a, stream);
 }
 
+// ---- vorticity confinement ---------------------------------------------------------------
+
+namespace {
+
+// Spiky gradient grad W(r) for kernel_eps <= |r| < h (else zero), r = x_i - x_j.
+__device__ __forceinline__ bool spiky_grad(const StepConsts& c, float ex, float ey, float ez, float& gx,
+                                           float& gy, float& gz) {
+  const float r2 = dist2(ex, ey, ez);
+  if (!(r2 < c.h2) || r2 < c.keps2) return false;
+  const float ir = rsqrtf(r2);
+  const float t = c.h - r2 * ir;
+  const float sc = c.spiky_coef * t * t * ir;
+  gx = sc * ex, gy = sc * ey, gz = sc * ez;
+  return true;
+}
+
+struct VortOmega {
+  const StepConsts& c;
+  const float4* __restrict__ U;
+  float4 xi, ui;
+  int i;
+  float wx = 0.f, wy = 0.f, wz = 0.f;
+  __device__ __forceinline__ void visit(float4 xj, int j) {
+    float gx, gy, gz;
+    if (j == i || !spiky_grad(c, xi.x - xj.x, xi.y - xj.y, xi.z - xj.z, gx, gy, gz)) return;
+    const float4 uj = __ldg(U + j);
+    const float dx = uj.x - ui.x, dy = uj.y - ui.y, dz = uj.z - ui.z;
+    wx += dy * gz - dz * gy;
+    wy += dz * gx - dx * gz;
+    wz += dx * gy - dy * gx;
+  }
+};
+
+struct VortEta {
+  const StepConsts& c;
+  const float4* __restrict__ W;
+  float4 xi;
+  int i;
+  float ex = 0.f, ey = 0.f, ez = 0.f;
+  __device__ __forceinline__ void visit(float4 xj, int j) {
+    float gx, gy, gz;
+    if (j == i || !spiky_grad(c, xi.x - xj.x, xi.y - xj.y, xi.z - xj.z, gx, gy, gz)) return;
+    const float m = __ldg(W + j).w;
+    ex += m * gx;
+    ey += m * gy;
+    ez += m * gz;
+  }
+};
+
+__global__ void __launch_bounds__(128)
+k_vort_omega(StepConsts c, Geometry G, const float4* __restrict__ X, const float4* __restrict__ U,
+             const uint32_t* __restrict__ cs, int n, float4* __restrict__ W) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = X[i];
+  const SceneGeom g = geom_of(c, G, i);
+  VortOmega p{c, U, xi, U[i], i};
+  visit_window(g, cs, n, cell_of(c, g, xi), X, p);
+  W[i] = make_float4(p.wx, p.wy, p.wz, sqrtf(dist2(p.wx, p.wy, p.wz)));
+}
+
+__global__ void __launch_bounds__(128)
+k_vort_force(StepConsts c, Geometry G, const float4* __restrict__ X, const float4* __restrict__ W,
+             const uint32_t* __restrict__ cs, int n, float4* __restrict__ U) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 xi = X[i];
+  const SceneGeom g = geom_of(c, G, i);
+  VortEta p{c, W, xi, i};
+  visit_window(g, cs, n, cell_of(c, g, xi), X, p);
+  const float len = sqrtf(dist2(p.ex, p.ey, p.ez));
+  if (!(len > 0.f) || !isfinite(len)) return;
+  const float nx = p.ex / len, ny = p.ey / len, nz = p.ez / len;
+  const float4 w = W[i];
+  const float s = c.dt * c.vort_eps;
+  float4 u = U[i];
+  u.x += s * (ny * w.z - nz * w.y);
+  u.y += s * (nz * w.x - nx * w.z);
+  u.z += s * (nx * w.y - ny * w.x);
+  U[i] = u;
+}
+
+}  // namespace
+
+cudaError_t launch_vorticity(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
+                             const SolverScratch& s, float4* NV, cudaStream_t stream) {
+  const int blocks = (n + 127) / 128;
+  k_vort_omega<<<blocks, 128, 0, stream>>>(c, G, X, NV, cs, n, s.xb);
+  k_vort_force<<<blocks, 128, 0, stream>>>(c, G, X, s.xb, cs, n, NV);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X, const float4* V, const uint32_t* cs,
                         int n, const SolverScratch& s, int pass, float4* NV, cudaStream_t stream) {
   cudaError_t e = launch_groups<kGroupsXsph>(c, s, X, V, n, stream);

@@ -1,0 +1,87 @@
+"""Headless scene driver: the per-frame loop of the reference's FluidSystem.
+
+FluidSystem::stepSimulate (fluids/FluidSystem.cpp:99-120) reloads the solver
+parameters, optionally sweeps the box limits sinusoidally
+(ulim + A_ulim sin(w t), llim + A_llim sin(w t), t = w (frame - start frame)),
+and calls Simulator::step once with the tic-toc buffer roles.  SceneDriver
+does the same without a window: `substeps` steps per frame (the scenes here
+use dt = 1/120 s, two per 1/60 s frame), the limits from the scene's own wall
+function or from a reference-style sweep, and optionally one particle state
+file per frame (scenes.save_state) for offline comparison.
+"""
+from __future__ import annotations
+
+import math
+from pathlib import Path
+from typing import Optional, Sequence, Tuple
+
+import torch
+
+from . import scenes as _scenes
+from .simulator import ParticleState, Simulator
+
+
+class Sweep:
+    """The reference's sinusoidal boundary sweep: limits = base + A sin(w (frame - start))."""
+
+    def __init__(self, a_ulim: Sequence[float], a_llim: Sequence[float], w: float, start_frame: int = 0):
+        self.a_ulim = tuple(float(x) for x in a_ulim)
+        self.a_llim = tuple(float(x) for x in a_llim)
+        self.w = float(w)
+        self.start = int(start_frame)
+
+    def limits(self, ulim, llim, frame: int):
+        phi = math.sin(self.w * (frame - self.start))
+        return (tuple(u + a * phi for u, a in zip(ulim, self.a_ulim)),
+                tuple(l + a * phi for l, a in zip(llim, self.a_llim)))
+
+
+class SceneDriver:
+    """Runs a scenes.Scene frame by frame on the GPU."""
+
+    def __init__(self, scene: _scenes.Scene, substeps: int = _scenes.SUBSTEPS, sweep: Optional[Sweep] = None,
+                 dump_dir=None, dump_every: int = 1):
+        self.scene = scene
+        self.substeps = int(substeps)
+        self.sweep = sweep
+        self.dump_dir = Path(dump_dir) if dump_dir is not None else None
+        self.dump_every = max(1, int(dump_every))
+        self.sim = Simulator(scene.params, scene.ulim, scene.llim, scene.n)
+        self.state = ParticleState(scene.pos, scene.vel)
+        self.frame = 0
+        self.t = 0.0
+        if self.dump_dir is not None:
+            self.dump_dir.mkdir(parents=True, exist_ok=True)
+
+    def limits(self) -> Tuple[Tuple[float, ...], Tuple[float, ...]]:
+        if self.sweep is not None:
+            return self.sweep.limits(self.scene.ulim, self.scene.llim, self.frame)
+        return self.scene.limits_at(self.t)
+
+    def step_frame(self) -> None:
+        dt = float(self.scene.params.dt)
+        for _ in range(self.substeps):
+            self.sim.setLim(*self.limits())
+            self.state.step(self.sim)
+            self.t += dt
+        self.frame += 1
+        if self.dump_dir is not None and self.frame % self.dump_every == 0:
+            self.dump(self.dump_dir / f"frame_{self.frame:06d}.bin")
+
+    def run(self, frames: int) -> None:
+        for _ in range(int(frames)):
+            self.step_frame()
+
+    def dump(self, path) -> None:
+        """The current state (positions, velocities, iids in cell order) to a state file."""
+        torch.cuda.synchronize()
+        _scenes.save_state(path, self.state.pos, self.state.vel, self.state.iid[: self.state.n])
+
+    def close(self) -> None:
+        self.sim.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
