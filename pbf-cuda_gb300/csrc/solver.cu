@@ -18,14 +18,16 @@
 //
 // Each pass is two kernels.  The sparse kernel gives every particle one
 // thread and walks its window in a compact loop (fluid at rest: ~200
-// candidates).  A warp in which some window exceeds dense_window candidates
-// (particles piled into a few cells) instead appends itself to a dense list
-// and returns; the dense kernel then gives each listed warp a block of
-// kDenseWarps warps, each walking one contiguous chunk of every lane's
-// window, and adds the chunks' partial sums in chunk order in shared memory.
-// Steps of fewer than kDenseAllBelow particles send every warp to the dense
-// kernel by default (one thread per particle would leave most SMs idle).  Both orders
-// are fixed, so results stay deterministic; they differ from the reference's
+// candidates; a window whose grouped cells -- see pbf_internal.cuh -- bring
+// it under dense_window entries is walked group by group).  A warp in which
+// some window still exceeds dense_window entries (particles piled into a few
+// cells) instead appends itself to a dense list and returns; the dense
+// kernel then gives each listed warp a block of kDenseWarps warps, each
+// walking one contiguous chunk of every lane's window, and adds the chunks'
+// partial sums in chunk order in shared memory.  Steps of fewer than
+// kDenseAllBelow particles send every warp to the dense kernel by default
+// (one thread per particle would leave most SMs idle).  Both orders are
+// fixed, so results stay deterministic; they differ from the reference's
 // sequential sums only by rounding.
 //
 // IEEE semantics follow the reference's: its kernels evaluate every
@@ -652,14 +654,20 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
   const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
   const int3 q = cell_of(a.c, g, xi);
   const int total = valid ? window_total(g, a.cs, a.n, q) : 0;
-  if (__any_sync(kFull, total > a.c.dense_window)) {
+  // a window over dense_window candidates that its grouped cells bring back
+  // under it is walked here, group by group (no masks)
+  const bool grouped = valid && total > a.c.dense_window && a.c.keps2 > 0.f;
+  const int entries = grouped ? window_total_grouped(g, a, q) : total;
+  if (__any_sync(kFull, entries > a.c.dense_window)) {
     if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(i >> 5);
     return;
   }
   if (!valid) return;
   const bool exact = exact_path(kKind, a, g, q, i);
   P p(a, g, xi, i, exact);
-  if (exact) {
+  if (grouped) {
+    visit_window_grouped(g, a, q, p, 0, entries);
+  } else if (exact) {
     visit_window(g, a.cs, a.n, q, a.X, p);  // non-neighbours matter: visit every candidate
   } else if (kKind == kLambda) {
     visit_window_masked(g, a.cs, a.n, q, a.X, p, a.masks, a.mask_stride, i);  // saves its masks
