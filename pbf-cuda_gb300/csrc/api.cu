@@ -639,7 +639,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   if (st != PBF_OK) return st;
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
-  s->last_launches = s->last_grid_launches + 1 + pbf::kLaunchesPerPass * (2 * niter + 1) +
+  s->last_launches = s->last_grid_launches + 1 + pbf::pass_launches(c, n) * (2 * niter + 1) +
                      (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;

@@ -277,8 +277,9 @@ cudaError_t launch_vorticity(const StepConsts& c, const Geometry& G, const float
                              const SolverScratch& s, float4* NV, cudaStream_t stream);
 constexpr int kVorticityLaunches = 2;
 
-// Kernel launches of one neighbour pass.
-constexpr int kLaunchesPerPass = 3;
+// Kernel launches of one neighbour pass of n particles (group build, sparse
+// kernel unless every warp goes dense, dense kernel).
+int pass_launches(const StepConsts& c, int n);
 
 // ---- reverse pass (adjoint.cu) ------------------------------------------------------
 

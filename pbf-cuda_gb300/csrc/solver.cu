@@ -1090,6 +1090,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
 template <int kWhat>
 cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const float4* X, const float4* V, int n,
                           cudaStream_t stream) {
+  if (n < kGroupCell) return cudaSuccess;  // no cell can hold kGroupCell particles
   GroupArgs a;
   a.X = X;
   a.V = V;
@@ -1145,7 +1146,8 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
 
 template <int kKind>
 cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
-  k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, 0, stream>>>(a);
+  if (!a.dense_all)  // else the sparse kernel has nothing to do
+    k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, 0, stream>>>(a);
   k_dense<kKind><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
@@ -1294,6 +1296,15 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
   a.V = V;
   a.NV = NV;
   return run_pass<kXsph>(a, stream);
+}
+
+}  // namespace pbf
+
+namespace pbf {
+
+int pass_launches(const StepConsts& c, int n) {
+  const bool all = c.dense_all >= 0 ? c.dense_all != 0 : n < kDenseAllBelow;
+  return (all ? 1 : 2) + (n < kGroupCell ? 0 : 1);
 }
 
 }  // namespace pbf
