@@ -264,6 +264,18 @@ cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
   if (e == cudaSuccess) e = alloc(&sol.grp_hash, 8 * entries);
   if (e == cudaSuccess) e = alloc(&sol.grp_max, entries);
   if (e == cudaSuccess) e = alloc(&sol.grp_acc, 3 * entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_list, entries);
+  if (e == cudaSuccess) e = alloc(&sol.grp_list_n, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_done, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_zero, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_item_off, slots);
+  if (e == cudaSuccess) e = alloc(&sol.grp_item_slot, pbf::group_items(max_particles));
+  // what the group kernels expect to find at zero
+  if (e == cudaSuccess) e = cudaMemset(sol.grp_hash, 0, sizeof(int) * 8 * entries);
+  if (e == cudaSuccess) e = cudaMemset(sol.grp_max, 0, sizeof(unsigned) * entries);
+  if (e == cudaSuccess) e = cudaMemset(sol.grp_acc, 0, sizeof(unsigned long long) * 3 * entries);
+  if (e == cudaSuccess) e = cudaMemset(sol.grp_list_n, 0, sizeof(int) * slots);
+  if (e == cudaSuccess) e = cudaMemset(sol.grp_done, 0, sizeof(int) * slots);
   return e;
 }
 
@@ -274,7 +286,8 @@ void free_all(pbf_solver* s) {
                   s->sol.lambda, s->sol.rho, s->sol.flags, s->sol.dense, s->sol.masks,
                   s->sol.cell_flags, s->sol.grp_cell, s->sol.grp_off, s->sol.grp_n, s->sol.grp_rep, s->sol.grp_cnt,
                   s->sol.grp_pos, s->sol.grp_sum, s->sol.grp_aux, s->sol.grp_id, s->sol.grp_hash,
-                  s->sol.grp_max, s->sol.grp_acc};
+                  s->sol.grp_max, s->sol.grp_acc, s->sol.grp_list, s->sol.grp_list_n, s->sol.grp_done,
+                  s->sol.grp_zero, s->sol.grp_item_off, s->sol.grp_item_slot};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -890,7 +903,8 @@ void batch_free(pbf_batch* b) {
                   b->sol.lambda, b->sol.rho, b->sol.flags, b->sol.dense, b->sol.masks,
                   b->sol.cell_flags, b->sol.grp_cell, b->sol.grp_off, b->sol.grp_n, b->sol.grp_rep, b->sol.grp_cnt,
                   b->sol.grp_pos, b->sol.grp_sum, b->sol.grp_aux, b->sol.grp_id, b->sol.grp_hash,
-                  b->sol.grp_max, b->sol.grp_acc, b->d_geom, b->d_sid};
+                  b->sol.grp_max, b->sol.grp_acc, b->sol.grp_list, b->sol.grp_list_n, b->sol.grp_done,
+                  b->sol.grp_zero, b->sol.grp_item_off, b->sol.grp_item_slot, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);

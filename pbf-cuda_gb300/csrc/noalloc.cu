@@ -85,7 +85,14 @@ constexpr size_t kOffGrpId = kOffGrpAux + align_up(16 * kEntries);
 constexpr size_t kOffGrpHash = kOffGrpId + align_up(4 * kNp);
 constexpr size_t kOffGrpMax = kOffGrpHash + align_up(4 * 8 * kNp);
 constexpr size_t kOffGrpAcc = kOffGrpMax + align_up(4 * kNp);
-constexpr size_t kNoAllocScratchBytes = kOffGrpAcc + align_up(8 * 3 * kNp);
+constexpr size_t kItems = kNp / pbf::kGroupChunk + kSlots + 1;
+constexpr size_t kOffGrpList = kOffGrpAcc + align_up(8 * 3 * kNp);
+constexpr size_t kOffGrpListN = kOffGrpList + align_up(4 * kNp);
+constexpr size_t kOffGrpDone = kOffGrpListN + align_up(4 * kSlots);
+constexpr size_t kOffGrpZero = kOffGrpDone + align_up(4 * kSlots);
+constexpr size_t kOffGrpItemOff = kOffGrpZero + align_up(4 * kSlots);
+constexpr size_t kOffGrpItemSlot = kOffGrpItemOff + align_up(4 * kSlots);
+constexpr size_t kNoAllocScratchBytes = kOffGrpItemSlot + align_up(4 * kItems);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -161,6 +168,12 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.grp_hash = (int*)(base + kOffGrpHash);
   s.grp_max = (unsigned*)(base + kOffGrpMax);
   s.grp_acc = (unsigned long long*)(base + kOffGrpAcc);
+  s.grp_list = (int*)(base + kOffGrpList);
+  s.grp_list_n = (int*)(base + kOffGrpListN);
+  s.grp_done = (int*)(base + kOffGrpDone);
+  s.grp_zero = (int*)(base + kOffGrpZero);
+  s.grp_item_off = (int*)(base + kOffGrpItemOff);
+  s.grp_item_slot = (int*)(base + kOffGrpItemSlot);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;

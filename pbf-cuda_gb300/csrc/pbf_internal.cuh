@@ -183,10 +183,17 @@ struct SolverScratch {
   float4* grp_pos;     // [max_particles] pool: the group's position
   float4* grp_sum;     // [max_particles] pool: pass sums of the group (see solver.cu)
   float4* grp_aux;     // [max_particles] pool: velocity of the group's first particle (xsph)
-  int* grp_id;         // [max_particles] group of each particle of a grouped cell
+  int* grp_id;         // [max_particles] hash entry of each particle of a grouped cell
   int* grp_hash;       // [4][2 max_particles] hash tables: owner, count, first particle, rank
-  unsigned* grp_max;   // [max_particles] pool: largest deviation of a group (fixed-point scale)
-  unsigned long long* grp_acc;  // [3 max_particles] pool: fixed-point sums
+                       // (owner, count and first are 0 between passes)
+  unsigned* grp_max;   // [max_particles] pool: largest deviation of a group (0 between passes)
+  unsigned long long* grp_acc;  // [3 max_particles] pool: fixed-point sums (0 between passes)
+  int* grp_list;       // [max_particles] pool: hash entries a slot's pass claimed
+  int* grp_list_n;     // [group_slots] entries claimed (0 between passes)
+  int* grp_done;       // [group_slots] work items finished (0 between passes)
+  int* grp_zero;       // [group_slots] every deviation of the pass's sums is zero
+  int* grp_item_off;   // [group_slots] first work item of each slot
+  int* grp_item_slot;  // [group_items] slot of each work item
 };
 
 // Bits of SolverScratch::cell_flags: the stale cell of a particle whose
@@ -216,7 +223,11 @@ constexpr int kCellSlotShift = 8;
 // reference's sum with its terms grouped: results differ from it by
 // rounding only.
 constexpr int kGroupCell = 512;
+constexpr int kGroupChunk = 8192;  // particles of a grouped cell per work item
 inline size_t group_slots(int max_particles) { return (size_t)max_particles / kGroupCell + 1; }
+inline size_t group_items(int max_particles) {
+  return (size_t)max_particles / kGroupChunk + group_slots(max_particles) + 1;
+}
 
 // Neighbour masks a particle keeps between the lambda and delta_p passes of
 // one iteration: one 32-bit mask per chunk of 32 consecutive candidates.
@@ -233,7 +244,8 @@ enum StepFlag {
   kDenseCount1 = 3,
   kGroupCount = 4,           // cells with a group slot (set by reorder)
   kGroupPool = 5,            // group pool entries handed out (set by reorder)
-  kNumFlags = 6
+  kGroupItems = 6,           // group work items (set by reorder)
+  kNumFlags = 7
 };
 
 // Entries of the dense list: one per warp of 32 consecutive particles.

@@ -727,7 +727,7 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
           float4* __restrict__ xs, float4* __restrict__ xa, uint32_t* __restrict__ iid_s,
           uint32_t* __restrict__ flags, const uint32_t* __restrict__ skeys,
           const uint32_t* __restrict__ cs, uint32_t* __restrict__ cell_flags, int* __restrict__ grp_cell,
-          int* __restrict__ grp_off) {
+          int* __restrict__ grp_off, int* __restrict__ grp_item_off, int* __restrict__ grp_item_slot) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint32_t key = skeys[k];
@@ -738,6 +738,11 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
     const uint32_t slot = atomicAdd(&flags[kGroupCount], 1u);
     grp_cell[slot] = (int)key;
     grp_off[slot] = (int)atomicAdd(&flags[kGroupPool], pop);
+    // work items of kGroupChunk particles (< n / kGroupChunk + slots of them)
+    const int items = (int)((pop + kGroupChunk - 1) / kGroupChunk);
+    const int i0 = (int)atomicAdd(&flags[kGroupItems], (uint32_t)items);
+    grp_item_off[slot] = i0;
+    for (int t = 0; t < items; ++t) grp_item_slot[i0 + t] = (int)slot;
     atomicOr(&cell_flags[key], (slot + 1u) << kCellSlotShift);
   }
   const uint32_t p = min(perm[k], (uint32_t)(n - 1));  // a permutation of [0, n): the min never binds
@@ -754,8 +759,9 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
 
 enum GroupsWhat { kGroupsPos = 0, kGroupsLambda = 1, kGroupsXsph = 2 };
 
-constexpr int kGroupThreads = 1024;  // one block per grouped cell: many loads in flight
+constexpr int kGroupThreads = 1024;
 constexpr int kGroupWarps = kGroupThreads / 32;
+constexpr int kGroupList = 4096;  // groups ranked in shared memory; more: an ordered scan
 
 struct GroupArgs {
   const float4* X;        // positions of the pass
@@ -763,21 +769,27 @@ struct GroupArgs {
   const float* rho;       // xsph: densities
   const float* lambda;    // delta_p: lambda
   const uint32_t* cs;
-  const uint32_t* count;  // number of slots (flags[kGroupCount])
+  const uint32_t* flags;  // flags[kGroupCount]: slots, flags[kGroupItems]: work items
   int n;
-  int np;                 // pool entries (the hash table parts are 2 np long)
+  int np;                 // pool entries
   const int* cell;
   const int* off;
+  const int* item_off;    // first work item of each slot
+  const int* item_slot;   // slot of each work item
+  int* done;              // per slot: work items finished (last-block-done; back to 0 after use)
   int* ng;
   int* rep;
   int* cnt;
   float4* pos;
   float4* sum;
   float4* aux;
-  int* id;
-  int* hash;
+  int* id;                // hash entry of each particle of a grouped cell
+  int* hash;              // owner (k + 1), count, first (0x7fffffff - k), rank: 2 np each; 0 = empty
+  int* list;              // pool: entries claimed per slot
+  int* list_n;            // per slot: entries claimed
   unsigned* gmax;
   unsigned long long* acc;
+  int* zero;              // per slot: every deviation is zero
 };
 
 // The key of particle j: the values that enter a pair term non-linearly.
@@ -835,273 +847,304 @@ __device__ __forceinline__ int block_scan(int flag, int* sh, int& total) {
   return sh[32 + warp] + in_warp;
 }
 
-// Fixed-point sums over the groups of slot (t0 .. t0 + ng) of the values val(k)
-// (k = cell-relative particle) minus the group's first particle's value
-// rep_val(g), C components: exact to 2^-62 of the bound max|dev| * count,
-// order-free.  Writes out(g, c, sum) for each group; false if some deviation
-// is not finite (other than between identical bits).
-// `cache` (kGroupCacheFloats floats of shared memory) holds the groups'
-// first-particle values when they fit, saving two dependent loads per particle.
-constexpr int kGroupCacheFloats = 2 * 4096;
+// A grouped cell's particles in work items of kGroupChunk; a kernel takes
+// items grid-stride and the block that finishes a slot's last item (counted
+// in done[slot], made visible by a fence) runs the slot's finishing step and
+// sets the counter back to 0.
+struct Item {
+  int slot, b, m, k0, k1, t0;
+};
 
-template <int C, class Val, class RepVal0, class Out>
-__device__ bool group_sums(const GroupArgs& a, int b, int m, int t0, int ng, Val val, RepVal0 rep_val0, Out out,
-                           int* s_flag, float* cache) {
-  const bool cached = ng * C <= kGroupCacheFloats;
-  if (threadIdx.x == 0) *s_flag = 0;
-  for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-    a.gmax[t0 + g] = 0u;
-    for (int c = 0; c < C; ++c) {
-      a.acc[3 * (t0 + g) + c] = 0ull;
-      if (cached) cache[g * C + c] = rep_val0(g, c);
-    }
-  }
-  __syncthreads();
-  auto rep_val = [&](int g, int c) { return cached ? cache[g * C + c] : rep_val0(g, c); };
-#pragma unroll 4
-  for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-    const int g = a.id[b + k];
-    float d = 0.f;
-    bool fin = true;
-    for (int c = 0; c < C; ++c) {
-      const float e = dev_from(val(k, c), rep_val(g, c));
-      fin &= isfinite(e);
-      d = fmaxf(d, fabsf(e));
-    }
-    const unsigned bits = fin ? __float_as_uint(d) : 0x7f800000u;  // +inf marks non-finite
-    const unsigned act = __activemask(), same = __match_any_sync(act, g);
-    const unsigned mx = __reduce_max_sync(same, bits);
-    if ((threadIdx.x & 31) == __ffs(same) - 1) atomicMax(&a.gmax[t0 + g], mx);
-  }
-  __syncthreads();
-  for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-    const unsigned mx = a.gmax[t0 + g];
-    if (!isfinite(__uint_as_float(mx))) atomicOr(s_flag, 1);
-    if (mx != 0u) atomicOr(s_flag, 2);
-  }
-  __syncthreads();
-  if (*s_flag & 1) return false;
-  if (!(*s_flag & 2)) {  // every member equals its group's first: all sums are 0
-    for (int g = threadIdx.x; g < ng; g += kGroupThreads)
-      for (int c = 0; c < C; ++c) out(g, c, 0.f);
-    __syncthreads();
-    return true;
-  }
-#pragma unroll 4
-  for (int k = threadIdx.x; k < m; k += kGroupThreads) {
-    const int g = a.id[b + k];
-    const float mx = __uint_as_float(a.gmax[t0 + g]);
-    int e = 0;
-    if (mx > 0.f) frexpf(mx, &e);                         // mx < 2^e
-    const int sh = 62 - e - (32 - __clz(a.cnt[t0 + g]));  // |sum| 2^sh < 2^62
-    const unsigned act = __activemask(), same = __match_any_sync(act, g);
-    for (int c = 0; c < C; ++c) {
-      // |dev| 2^sh < 2^62 is a float without overflow; the scaling is exact
-      long long q = __float2ll_rn(ldexpf(dev_from(val(k, c), rep_val(g, c)), sh));
-      if (same == act) {  // integer sums: any order gives the same result
-        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(act, q, o);
-        if ((threadIdx.x & 31) == __ffs(act) - 1) atomicAdd(&a.acc[3 * (t0 + g) + c], (unsigned long long)q);
-      } else {
-        atomicAdd(&a.acc[3 * (t0 + g) + c], (unsigned long long)q);
-      }
-    }
-  }
-  __syncthreads();
-  for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
-    const float mx = __uint_as_float(a.gmax[t0 + g]);
-    int e = 0;
-    if (mx > 0.f) frexpf(mx, &e);
-    const int sh = 62 - e - (32 - __clz(a.cnt[t0 + g]));
-    for (int c = 0; c < C; ++c)
-      out(g, c, (float)ldexp((double)(long long)a.acc[3 * (t0 + g) + c], -sh));
-  }
-  __syncthreads();
-  return true;
+__device__ __forceinline__ Item item_of(const GroupArgs& a, int item) {
+  Item it;
+  it.slot = a.item_slot[item];
+  const int cell = a.cell[it.slot];
+  it.b = (int)a.cs[cell];
+  it.m = max(min((int)a.cs[cell + 1], a.n) - it.b, 0);
+  it.k0 = (item - a.item_off[it.slot]) * kGroupChunk;
+  it.k1 = min(it.k0 + kGroupChunk, it.m);
+  it.t0 = a.off[it.slot];
+  return it;
 }
 
-// One block per slot (grid-stride).
-//   kGroupsPos / kGroupsXsph: insert every particle of the cell into the
-//     slot's hash table (2 entries per particle, in global memory: the
-//     claiming particle of an entry holds the key; integer atomics only),
-//     number the groups in order of their first particle (by counting in
-//     shared memory, or for over kGroupList groups by an ordered block scan),
-//     write rep, cnt, pos and each particle's group id; for xsph also
-//     aux = the first particle's velocity v_rep, sum.w = density and sum.xyz
-//     = sum over the group of (v_j - v_rep) in fixed point (group_sums).
-//   kGroupsLambda: for the kGroupsPos table of the same positions, sum.x =
-//     lambda_rep and sum.y = sum over the group of (lambda_j - lambda_rep).
-// A non-finite deviation in a sum: ng = -1 (the cell is visited per particle).
-// Deterministic: no result depends on which particle claimed an entry.
-constexpr int kGroupList = 4096;  // groups ranked in shared memory; more: an ordered scan
+// After a block's share of an item: whether it finished the slot's last item.
+__device__ __forceinline__ bool last_item(const GroupArgs& a, const Item& it, int* s_last) {
+  __threadfence();  // this block's writes, before the count that may let another block read them
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int items = (it.m + kGroupChunk - 1) / kGroupChunk;
+    *s_last = atomicAdd(&a.done[it.slot], 1) == items - 1;
+  }
+  __syncthreads();
+  if (*s_last) __threadfence();
+  return *s_last;
+}
 
+// Inserts the item's particles into the slot's hash table (2 entries per
+// particle of the cell, so every key finds an entry; integer atomics only),
+// kUnroll probe chains per thread in flight.  The block that finishes the
+// slot numbers the groups in order of their first particle (by counting in
+// shared memory, or for over kGroupList groups by an ordered block scan),
+// writes rep, cnt, pos (and for xsph aux = the first particle's velocity and
+// sum.w = its density), h_rank, ng, and clears the claimed entries.
 template <int kWhat>
-__global__ void __launch_bounds__(kGroupThreads) k_groups(GroupArgs a) {
+__global__ void __launch_bounds__(kGroupThreads) k_group_insert(GroupArgs a) {
   __shared__ int sh[80];
-  __shared__ int s_flag, s_ng;
-  __shared__ int s_buf[2 * kGroupList];  // the build's claimed entries and their first
-                                         // particles, then group_sums' cache
-  int* s_list = s_buf;                   // hash entries claimed (any order)
-  int* s_first = s_buf + kGroupList;     // their first particles
-  const uint32_t slots = *a.count;
-  for (uint32_t slot = blockIdx.x; slot < slots; slot += gridDim.x) {
-    const int cell = a.cell[slot];
-    const int b = (int)a.cs[cell];
-    const int m = max(min((int)a.cs[cell + 1], a.n) - b, 0);
-    const int t0 = a.off[slot];
-    if constexpr (kWhat == kGroupsLambda) {
-      const int ng = a.ng[slot];
-      if (ng <= 0) continue;
-      const bool ok = group_sums<1>(
-          a, b, m, t0, ng, [&](int k, int) { return a.lambda[b + k]; },
-          [&](int g, int) { return a.lambda[a.rep[t0 + g]]; },
-          [&](int g, int, float v) { a.sum[t0 + g] = make_float4(a.lambda[a.rep[t0 + g]], v, 0.f, 0.f); },
-          &s_flag, reinterpret_cast<float*>(s_buf));
-      if (!ok && threadIdx.x == 0) a.ng[slot] = -1;
-      __syncthreads();
-    } else {
-      if (m == 0) {
-        if (threadIdx.x == 0) a.ng[slot] = -1;
-        continue;
+  __shared__ int s_last;
+  __shared__ int s_buf[2 * kGroupList];
+  const int items = (int)a.flags[kGroupItems];
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const Item it = item_of(a, item);
+    const int H = 2 * it.m;
+    int* h_owner = a.hash + 2 * it.t0;
+    int* h_cnt = h_owner + 2 * a.np;
+    int* h_first = h_owner + 4 * a.np;
+    int* h_rank = h_owner + 6 * a.np;
+    int* list = a.list + it.t0;
+    constexpr int kUnroll = 4;
+    for (int k0 = it.k0 + threadIdx.x; k0 < it.k1; k0 += kUnroll * kGroupThreads) {
+      int found[kUnroll];
+      GroupKey<kWhat> key[kUnroll];
+      int h[kUnroll], o[kUnroll];
+#pragma unroll
+      for (int u = 0; u < kUnroll; ++u) {
+        const int k = min(k0 + u * kGroupThreads, it.k1 - 1);
+        key[u] = GroupKey<kWhat>(a, it.b + k);
+        h[u] = (int)(key[u].hash() % (uint32_t)H);
       }
-      const int H = 2 * m;
-      int* h_owner = a.hash + 2 * t0;
-      int* h_cnt = h_owner + 2 * a.np;
-      int* h_first = h_owner + 4 * a.np;
-      int* h_rank = h_owner + 6 * a.np;
-      for (int h = threadIdx.x; h < H; h += kGroupThreads) {
-        h_owner[h] = -1;
-        h_cnt[h] = 0;
-        h_first[h] = INT_MAX;
-      }
-      if (threadIdx.x == 0) s_ng = 0;
-      __syncthreads();
-      // kUnroll particles per thread per round: their loads are independent,
-      // so several probe chains are in flight at once
-      constexpr int kUnroll = 4;
-      for (int k0 = threadIdx.x; k0 < m; k0 += kUnroll * kGroupThreads) {
-        int found[kUnroll];
-        GroupKey<kWhat> key[kUnroll];
-        int h[kUnroll], o[kUnroll];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-          const int k = min(k0 + u * kGroupThreads, m - 1);
-          key[u] = GroupKey<kWhat>(a, b + k);
-          h[u] = (int)(key[u].hash() % (uint32_t)H);
-        }
+      for (int u = 0; u < kUnroll; ++u) o[u] = *(volatile int*)&h_owner[h[u]] - 1;
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) o[u] = *(volatile int*)&h_owner[h[u]];
+      for (int u = 0; u < kUnroll; ++u)  // the common case: the first entry holds the key
+        found[u] = o[u] >= 0 && GroupKey<kWhat>(a, it.b + o[u]) == key[u] ? h[u] : -1;
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u)  // the common case: the first entry holds the key
-          found[u] = o[u] >= 0 && GroupKey<kWhat>(a, b + o[u]) == key[u] ? h[u] : -1;
-#pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-          const int k = k0 + u * kGroupThreads;
-          if (k < m && found[u] < 0) {
-            int hh = h[u];
-            for (int probe = 0; probe < H; ++probe, hh = hh + 1 == H ? 0 : hh + 1) {
-              int ow = *(volatile int*)&h_owner[hh];
+      for (int u = 0; u < kUnroll; ++u) {
+        const int k = k0 + u * kGroupThreads;
+        if (k < it.k1 && found[u] < 0) {
+          int hh = h[u];
+          for (int probe = 0; probe < H; ++probe, hh = hh + 1 == H ? 0 : hh + 1) {
+            int ow = *(volatile int*)&h_owner[hh] - 1;
+            if (ow < 0) {
+              ow = atomicCAS(&h_owner[hh], 0, k + 1) - 1;
               if (ow < 0) {
-                ow = atomicCAS(&h_owner[hh], -1, k);
-                if (ow < 0) {
-                  found[u] = hh;  // claimed: a new group
-                  const int e = atomicAdd(&s_ng, 1);
-                  if (e < kGroupList) s_list[e] = hh;
-                  break;
-                }
-              }
-              if (GroupKey<kWhat>(a, b + ow) == key[u]) {
-                found[u] = hh;
+                found[u] = hh;  // claimed: a new group
+                list[atomicAdd(&a.list_n[it.slot], 1)] = hh;
                 break;
               }
             }
-            // H = 2m entries for at most m keys: a probe always ends
-          }
-          if (k < m) {
-            const unsigned act = __activemask(), same = __match_any_sync(act, found[u]);
-            if ((threadIdx.x & 31) == __ffs(same) - 1) {
-              atomicAdd(&h_cnt[found[u]], __popc(same));
-              atomicMin(&h_first[found[u]], k);  // the lowest lane holds the lowest k
+            if (GroupKey<kWhat>(a, it.b + ow) == key[u]) {
+              found[u] = hh;
+              break;
             }
-            a.id[b + k] = found[u];
           }
+          // H = 2m entries for at most m keys: a probe always ends
         }
+        if (k < it.k1) {
+          const unsigned act = __activemask(), same = __match_any_sync(act, found[u]);
+          if ((threadIdx.x & 31) == __ffs(same) - 1) {
+            atomicAdd(&h_cnt[found[u]], __popc(same));
+            atomicMax(&h_first[found[u]], 0x7fffffff - k);  // the lowest lane holds the lowest k
+          }
+          a.id[it.b + k] = found[u];
+        }
+      }
+    }
+    if (!last_item(a, it, &s_last)) continue;
+    // ---- the slot's last item is in: number the groups ----
+    // read through L2: other blocks wrote these
+    int ng = __ldcg(&a.list_n[it.slot]);
+    int* s_list = s_buf;
+    int* s_first = s_buf + kGroupList;
+    if (ng <= kGroupList) {
+      for (int e = threadIdx.x; e < ng; e += kGroupThreads) {
+        const int hh = __ldcg(&list[e]);
+        s_list[e] = hh;
+        s_first[e] = 0x7fffffff - __ldcg(&h_first[hh]);
       }
       __syncthreads();
-      // groups in order of their first particle: few groups are ranked by
-      // counting in shared memory, many by an ordered scan over the particles
-      int ng = s_ng;
-      if (ng <= kGroupList) {
-        for (int e = threadIdx.x; e < ng; e += kGroupThreads) s_first[e] = h_first[s_list[e]];
-        __syncthreads();
-        for (int e = threadIdx.x; e < ng; e += kGroupThreads) {
-          const int f = s_first[e], h = s_list[e];
-          int r = 0;
-          for (int u = 0; u < ng; ++u) r += s_first[u] < f;
-          h_rank[h] = r;
-          a.rep[t0 + r] = b + f;
-          a.cnt[t0 + r] = h_cnt[h];
-          a.pos[t0 + r] = a.X[b + f];
-          if constexpr (kWhat == kGroupsXsph) a.aux[t0 + r] = a.V[b + f];
+      for (int e = threadIdx.x; e < ng; e += kGroupThreads) {
+        const int f = s_first[e], hh = s_list[e];
+        int r = 0;
+        for (int u = 0; u < ng; ++u) r += s_first[u] < f;
+        h_rank[hh] = r;
+        a.rep[it.t0 + r] = it.b + f;
+        a.cnt[it.t0 + r] = __ldcg(&h_cnt[hh]);
+        a.pos[it.t0 + r] = a.X[it.b + f];
+        if constexpr (kWhat == kGroupsXsph) {
+          a.aux[it.t0 + r] = a.V[it.b + f];
+          a.sum[it.t0 + r].w = a.rho[it.b + f];
         }
       }
-      if (ng > kGroupList) ng = 0;
-      for (int k0 = 0; s_ng > kGroupList && k0 < m; k0 += kGroupThreads) {
+    } else {
+      ng = 0;
+      for (int k0 = 0; k0 < it.m; k0 += kGroupThreads) {
         const int k = k0 + threadIdx.x;
-        const int h = k < m ? a.id[b + k] : 0;
-        const bool first = k < m && h_first[h] == k;
+        const int hh = k < it.m ? __ldcg(&a.id[it.b + k]) : 0;
+        const bool first = k < it.m && 0x7fffffff - __ldcg(&h_first[hh]) == k;
         int total;
         const int r = ng + block_scan(first, sh, total);
         if (first) {
-          h_rank[h] = r;
-          a.rep[t0 + r] = b + k;
-          a.cnt[t0 + r] = h_cnt[h];
-          a.pos[t0 + r] = a.X[b + k];
-          if constexpr (kWhat == kGroupsXsph) a.aux[t0 + r] = a.V[b + k];
+          h_rank[hh] = r;
+          a.rep[it.t0 + r] = it.b + k;
+          a.cnt[it.t0 + r] = __ldcg(&h_cnt[hh]);
+          a.pos[it.t0 + r] = a.X[it.b + k];
+          if constexpr (kWhat == kGroupsXsph) {
+            a.aux[it.t0 + r] = a.V[it.b + k];
+            a.sum[it.t0 + r].w = a.rho[it.b + k];
+          }
         }
         ng += total;
       }
-      __syncthreads();
-      for (int k = threadIdx.x; k < m; k += kGroupThreads) a.id[b + k] = h_rank[a.id[b + k]];
-      __syncthreads();
-      int ngw = ng;
-      if constexpr (kWhat == kGroupsXsph) {
-        const bool ok = group_sums<3>(
-            a, b, m, t0, ng,
-            [&](int k, int c) { const float4 v = a.V[b + k]; return c == 0 ? v.x : (c == 1 ? v.y : v.z); },
-            [&](int g, int c) { const float4 v = a.aux[t0 + g]; return c == 0 ? v.x : (c == 1 ? v.y : v.z); },
-            [&](int g, int c, float v) {
-              float4& s4 = a.sum[t0 + g];
-              if (c == 0) s4.x = v;
-              if (c == 1) s4.y = v;
-              if (c == 2) {
-                s4.z = v;
-                s4.w = a.rho[a.rep[t0 + g]];
-              }
-            },
-            &s_flag, reinterpret_cast<float*>(s_buf));
-        if (!ok) ngw = -1;
-      }
-      if (threadIdx.x == 0) a.ng[slot] = ngw;
-      __syncthreads();
     }
+    __syncthreads();
+    // clear the claimed entries for the next pass (h_rank stays: the sums read it)
+    const int claimed = __ldcg(&a.list_n[it.slot]);
+    for (int e = threadIdx.x; e < claimed; e += kGroupThreads) {
+      const int hh = __ldcg(&list[e]);
+      h_owner[hh] = 0;
+      h_cnt[hh] = 0;
+      h_first[hh] = 0;
+    }
+    if (threadIdx.x == 0) {
+      a.ng[it.slot] = ng;
+      a.list_n[it.slot] = 0;
+      a.done[it.slot] = 0;
+    }
+    __syncthreads();
+  }
+}
+
+// Deviation of particle j (cell-relative k) from its group's first particle,
+// component c: lambda (kGroupsLambda) or velocity (kGroupsXsph).
+template <int kWhat>
+__device__ __forceinline__ float group_dev(const GroupArgs& a, const Item& it, int k, int g, int c) {
+  if constexpr (kWhat == kGroupsLambda) {
+    return dev_from(a.lambda[it.b + k], a.lambda[a.rep[it.t0 + g]]);
+  } else {
+    const float4 v = a.V[it.b + k], r = a.aux[it.t0 + g];
+    return c == 0 ? dev_from(v.x, r.x) : (c == 1 ? dev_from(v.y, r.y) : dev_from(v.z, r.z));
+  }
+}
+
+// Fixed-point sums over each group of (value - the group's first particle's
+// value), two kernels.  k_group_devmax: the largest |deviation| per group
+// (atomicMax on the float bits; +inf marks a non-finite deviation); the last
+// block of a slot sets ng = -1 on a non-finite one and zero[slot] when every
+// deviation is 0.  k_group_devsum: each deviation scaled by 2^sh, sh from the
+// group's bound max|dev| * count < 2^62, added as a 64-bit integer (order-
+// free, exact to 2^-62 of the bound); the last block writes the sums
+// (lambda: sum = (lambda_rep, sum dev); xsph: sum.xyz) and clears gmax / acc.
+template <int kWhat>
+__global__ void __launch_bounds__(kGroupThreads) k_group_devmax(GroupArgs a) {
+  constexpr int C = kWhat == kGroupsLambda ? 1 : 3;
+  __shared__ int s_last, s_flag;
+  const int items = (int)a.flags[kGroupItems];
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const Item it = item_of(a, item);
+    const int* h_rank = a.hash + 2 * it.t0 + 6 * a.np;
+    const bool grouped = a.ng[it.slot] > 0;
+    for (int k = it.k0 + threadIdx.x; grouped && k < it.k1; k += kGroupThreads) {
+      const int g = h_rank[a.id[it.b + k]];
+      float d = 0.f;
+      bool fin = true;
+      for (int c = 0; c < C; ++c) {
+        const float e = group_dev<kWhat>(a, it, k, g, c);
+        fin &= isfinite(e);
+        d = fmaxf(d, fabsf(e));
+      }
+      const unsigned bits = fin ? __float_as_uint(d) : 0x7f800000u;
+      const unsigned act = __activemask(), same = __match_any_sync(act, g);
+      const unsigned mx = __reduce_max_sync(same, bits);
+      if ((threadIdx.x & 31) == __ffs(same) - 1 && mx) atomicMax(&a.gmax[it.t0 + g], mx);
+    }
+    if (!last_item(a, it, &s_last)) continue;
+    const int ng = a.ng[it.slot];
+    if (threadIdx.x == 0) s_flag = 0;
+    __syncthreads();
+    for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+      const unsigned mx = __ldcg(&a.gmax[it.t0 + g]);
+      if (!isfinite(__uint_as_float(mx))) atomicOr(&s_flag, 1);
+      if (mx) atomicOr(&s_flag, 2);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (s_flag & 1) a.ng[it.slot] = -1;
+      a.zero[it.slot] = !(s_flag & 2);
+      a.done[it.slot] = 0;
+    }
+    if (s_flag & 1)  // ungrouped: clear the bounds now (devsum skips the slot)
+      for (int g = threadIdx.x; g < ng; g += kGroupThreads) a.gmax[it.t0 + g] = 0u;
+    __syncthreads();
   }
 }
 
 template <int kWhat>
-cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const float4* X, const float4* V, int n,
-                          cudaStream_t stream) {
-  if (n < kGroupCell) return cudaSuccess;  // no cell can hold kGroupCell particles
+__global__ void __launch_bounds__(kGroupThreads) k_group_devsum(GroupArgs a) {
+  constexpr int C = kWhat == kGroupsLambda ? 1 : 3;
+  __shared__ int s_last;
+  const int items = (int)a.flags[kGroupItems];
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const Item it = item_of(a, item);
+    const int* h_rank = a.hash + 2 * it.t0 + 6 * a.np;
+    const bool add = a.ng[it.slot] > 0 && !a.zero[it.slot];
+    for (int k = it.k0 + threadIdx.x; add && k < it.k1; k += kGroupThreads) {
+      const int g = h_rank[a.id[it.b + k]];
+      const float mx = __uint_as_float(a.gmax[it.t0 + g]);
+      int e = 0;
+      if (mx > 0.f) frexpf(mx, &e);                            // mx < 2^e
+      const int sh = 62 - e - (32 - __clz(a.cnt[it.t0 + g]));  // |sum| 2^sh < 2^62
+      const unsigned act = __activemask(), same = __match_any_sync(act, g);
+      for (int c = 0; c < C; ++c) {
+        // |dev| 2^sh < 2^62 is a float without overflow; the scaling is exact
+        long long q = __float2ll_rn(ldexpf(group_dev<kWhat>(a, it, k, g, c), sh));
+        if (same == 0xffffffffu) {  // a full warp of one group; integer sums: any order, same result
+          for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+          if ((threadIdx.x & 31) == 0 && q) atomicAdd(&a.acc[3 * (it.t0 + g) + c], (unsigned long long)q);
+        } else if (q) {
+          atomicAdd(&a.acc[3 * (it.t0 + g) + c], (unsigned long long)q);
+        }
+      }
+    }
+    if (!last_item(a, it, &s_last)) continue;
+    const int ng = a.ng[it.slot];
+    for (int g = threadIdx.x; g < ng; g += kGroupThreads) {
+      const float mx = __uint_as_float(a.gmax[it.t0 + g]);  // from the previous kernel
+      int e = 0;
+      if (mx > 0.f) frexpf(mx, &e);
+      const int sh = 62 - e - (32 - __clz(a.cnt[it.t0 + g]));
+      float s3[3];
+      for (int c = 0; c < C; ++c) {
+        s3[c] = (float)ldexp((double)(long long)__ldcg(&a.acc[3 * (it.t0 + g) + c]), -sh);
+        a.acc[3 * (it.t0 + g) + c] = 0ull;
+      }
+      a.gmax[it.t0 + g] = 0u;
+      if constexpr (kWhat == kGroupsLambda) {
+        a.sum[it.t0 + g] = make_float4(a.lambda[a.rep[it.t0 + g]], s3[0], 0.f, 0.f);
+      } else {
+        float4& s4 = a.sum[it.t0 + g];
+        s4.x = s3[0], s4.y = s3[1], s4.z = s3[2];
+      }
+    }
+    if (threadIdx.x == 0) a.done[it.slot] = 0;
+    __syncthreads();
+  }
+}
+
+GroupArgs group_args(const SolverScratch& s, const float4* X, const float4* V, int n) {
   GroupArgs a;
   a.X = X;
   a.V = V;
   a.rho = s.rho;
   a.lambda = s.lambda;
   a.cs = s.cell_start;
-  a.count = s.flags + kGroupCount;
+  a.flags = s.flags;
   a.n = n;
   a.np = s.grp_pool;
   a.cell = s.grp_cell;
   a.off = s.grp_off;
+  a.item_off = s.grp_item_off;
+  a.item_slot = s.grp_item_slot;
+  a.done = s.grp_done;
   a.ng = s.grp_n;
   a.rep = s.grp_rep;
   a.cnt = s.grp_cnt;
@@ -1110,9 +1153,27 @@ cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const flo
   a.aux = s.grp_aux;
   a.id = s.grp_id;
   a.hash = s.grp_hash;
+  a.list = s.grp_list;
+  a.list_n = s.grp_list_n;
   a.gmax = s.grp_max;
   a.acc = s.grp_acc;
-  k_groups<kWhat><<<c.dense_grid, kGroupThreads, 0, stream>>>(a);
+  a.zero = s.grp_zero;
+  return a;
+}
+
+// kGroupsPos: the lambda pass's groups.  kGroupsLambda: their lambda sums for
+// delta_p.  kGroupsXsph: the (position, density) groups and velocity sums.
+template <int kWhat>
+cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const float4* X, const float4* V, int n,
+                          cudaStream_t stream) {
+  if (n < kGroupCell) return cudaSuccess;  // no cell can hold kGroupCell particles
+  const GroupArgs a = group_args(s, X, V, n);
+  const int grid = c.dense_grid;
+  if constexpr (kWhat != kGroupsLambda) k_group_insert<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
+  if constexpr (kWhat != kGroupsPos) {
+    k_group_devmax<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
+    k_group_devsum<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
+  }
   return cudaGetLastError();
 }
 
@@ -1161,7 +1222,7 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
   if (e != cudaSuccess) return e;
   k_reorder<<<(n + 255) / 256, 256, 0, stream>>>(perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
                                                   s.flags, s.keys_sorted, s.cell_start, s.cell_flags,
-                                                  s.grp_cell, s.grp_off);
+                                                  s.grp_cell, s.grp_off, s.grp_item_off, s.grp_item_slot);
   return cudaGetLastError();
 }
 
