@@ -653,7 +653,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
   s->last_launches = s->last_grid_launches + 1 + pbf::pass_launches(c, n) * (2 * niter + 1) +
-                     (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
+                     pbf::group_launches(n, niter) + (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
   if (taping) {

@@ -22,7 +22,8 @@
 // be made before any stream capture.
 //
 // The array is shared by every call and keeps the last call's contents; the
-// step clears what must start at zero (the per-cell counters) itself.  Calls
+// step clears what must start at zero (the per-cell counters and the group
+// tables' hash entries, sums and counters) itself.  Calls
 // whose work overlaps on the GPU (different streams, different host threads)
 // race on the array: serialise them.
 //
@@ -177,6 +178,12 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;
+  // the group tables' hash entries, bounds, fixed-point sums and per-slot
+  // counters must be zero when a step starts (every pass leaves them so);
+  // cleared here so that no call depends on what an earlier one left
+  if ((e = cudaMemsetAsync(base + kOffGrpHash, 0, kOffGrpList - kOffGrpHash, strm)) != cudaSuccess ||
+      (e = cudaMemsetAsync(base + kOffGrpListN, 0, kOffGrpZero - kOffGrpListN, strm)) != cudaSuccess)
+    return pbf::set_cuda_error(e, "pbf_step_noalloc: clear");
   const uint32_t* perm = nullptr;
   // build_grid clears the per-cell counters itself (cudaMemsetAsync, no allocation)
   const pbf::Geometry G{nullptr, nullptr};

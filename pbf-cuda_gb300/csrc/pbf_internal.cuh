@@ -289,9 +289,11 @@ cudaError_t launch_vorticity(const StepConsts& c, const Geometry& G, const float
                              const SolverScratch& s, float4* NV, cudaStream_t stream);
 constexpr int kVorticityLaunches = 2;
 
-// Kernel launches of one neighbour pass of n particles (group build, sparse
-// kernel unless every warp goes dense, dense kernel).
+// Kernel launches of one neighbour pass of n particles (sparse kernel unless
+// every warp goes dense, dense kernel).
 int pass_launches(const StepConsts& c, int n);
+// Group-table launches of one step of n particles at niter iterations.
+int group_launches(int n, int niter);
 
 // ---- reverse pass (adjoint.cu) ------------------------------------------------------
 

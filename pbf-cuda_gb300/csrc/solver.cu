@@ -1365,7 +1365,10 @@ namespace pbf {
 
 int pass_launches(const StepConsts& c, int n) {
   const bool all = c.dense_all >= 0 ? c.dense_all != 0 : n < kDenseAllBelow;
-  return (all ? 1 : 2) + (n < kGroupCell ? 0 : 1);
+  return all ? 1 : 2;
 }
+
+// launch_groups: 1 launch before each lambda pass, 2 before each delta_p pass, 3 before xsph.
+int group_launches(int n, int niter) { return n < kGroupCell ? 0 : 3 * niter + 3; }
 
 }  // namespace pbf
