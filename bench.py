@@ -584,7 +584,7 @@ def main(argv=None):
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
-    ap.add_argument("--cpu-steps", type=int, default=3,
+    ap.add_argument("--cpu-steps", type=int, default=20,
                     help="most steps the CPU baseline times (0: no CPU baseline, for profiling runs)")
     ap.add_argument("--cpu-warmup-steps", type=int, default=3, help="most warm-up steps of the reference arm")
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
