@@ -567,6 +567,103 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_ssf(args):
+    """frames/s of the screen-space fluid render (include/pbf_ssf.h): the 1M
+    particles of the large sweep's lattice at 1600 x 1200 with the reference's
+    renderer settings (2 bilateral passes, kernel_r 10, sigma_r 6, sigma_z 0.1,
+    Fresnel shading), camera 11.7 units off the lattice.  A step = one render:
+    clear, depth + thickness splat, resolve, 2 smoothing passes, normals,
+    shading.  e2e: host positions copied in, the colour image copied back."""
+    import torch
+
+    pkg = load_pkg()
+    from oracle import oracle
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    scene = pkg.scenes.large_sweep(seed=0)
+    pos_y = torch.from_numpy(scene.pos).cuda()
+    pos = pkg.ssf.z_up(pos_y).contiguous()
+    n = pos.shape[0]
+    p = pkg.ssf_default_params(1600, 1200)
+    pkg.ssf.look_at(p, (3.2, -14.0, 6.0), (3.2, -3.2, 1.6))
+    r = pkg.SSFRenderer(p)
+    color = torch.zeros((p.height, p.width, 4), device="cuda")
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    warm = max(3, args.warmup)
+    for _ in range(warm):
+        r.render(pos, color=color)
+    r.profile_enable(True)
+    r.render(pos, color=color)
+    prof = r.profile()
+    r.profile_enable(False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = []
+    clocks = ClockSampler(torch.cuda.current_device())
+    for _ in range(args.steps):
+        flush.fill_(1.0)  # L2 flushed before every timed render, outside the events
+        e0.record(stream)
+        r.render(pos, color=color)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    clk = clocks.stop()
+    ms = statistics.mean(times)
+    # e2e: pinned host positions in, the colour image out, every frame
+    host_pos = pos.cpu().pin_memory()
+    host_img = torch.empty(color.shape, dtype=torch.float32).pin_memory()
+    dev_pos = torch.empty_like(pos)
+    e2e_frames = min(args.steps, 20)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(e2e_frames):
+        dev_pos.copy_(host_pos, non_blocking=True)
+        r.render(dev_pos, color=color)
+        host_img.copy_(color, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / e2e_frames
+    # CPU baseline: the float oracle renders one frame of the same workload
+    cpu_line = None
+    if args.cpu_steps > 0:
+        host = pos.cpu().numpy()
+        a = time.perf_counter()
+        o = oracle.ssf_render(p, host, prec="f32")
+        cpu_s = time.perf_counter() - a
+        cpu_line = {"value": 1.0 / cpu_s, "unit": "frames/s", "cores": oracle.threads(), "kind": "port",
+                    "sample": f"one frame of the same workload ({n} particles, 1600x1200, {o['fragments']} "
+                              f"fragments; splat on one thread, smoothing/normals/shading on all), "
+                              f"{cpu_s:.1f} s"}
+    phases = {k: round(prof[k], 4) for k in ("splat_ms", "smooth_ms", "normal_ms", "shade_ms", "total_ms")}
+    dominant = max(("splat_ms", "smooth_ms", "normal_ms", "shade_ms"), key=lambda k: prof[k])
+    npix = p.width * p.height
+    # algorithmic bytes: splat reads the positions and does one 4 B + one 8 B
+    # read-modify-write per fragment; a smoothing pass reads and writes one float per pixel
+    alg = {"splat_ms": 16 * n + 24 * prof["fragments"] + 28 * npix, "smooth_ms": 8 * npix * p.smooth_niter,
+           "normal_ms": 20 * npix, "shade_ms": 40 * npix}
+    peak, peak_kind = measured_peaks()
+    achieved = alg[dominant] / (prof[dominant] / 1e3) / 1e9
+    line = {
+        "metric": "SSF frames/s at 1M particles, 1600x1200", "value": 1e3 / ms, "unit": "frames/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": warm, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"SSF render: {n} particles (128x64x128 lattice, z-up) at 1600x1200, "
+                               f"2 bilateral passes (kernel_r 10), Fresnel shading, camera (3.2,-14,6)->(3.2,-3.2,1.6)",
+                   "particles": n, "l2": "flushed before every timed render (512 MB write, outside the events)"},
+        "phases_ms": phases, "fragments": prof["fragments"], "gpu_launches": prof["launches"] * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dominant.replace("_ms", ""), "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": alg[dominant], "traffic": None},
+        "e2e": {"value": 1e3 / e2e_ms, "unit": "frames/s", "h2d_bytes_per_step": int(host_pos.numel() * 4),
+                "d2h_bytes_per_step": int(host_img.numel() * 4), "steps": e2e_frames, "ms_per_step": e2e_ms},
+        "cpu_baseline": cpu_line,
+        "clocks": clk,
+    }
+    r.close()
+    print(json.dumps(line), flush=True)
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -574,9 +671,10 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=120, help="untimed steps (default: 60 frames x 2 steps)")
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--scene", default="large_sweep", choices=("large_sweep", "double_dam", "dam_break", "clustered"))
-    ap.add_argument("--workload", choices=("step", "ensemble", "adjoint"), default="step",
+    ap.add_argument("--workload", choices=("step", "ensemble", "adjoint", "ssf"), default="step",
                     help="step: particle-updates/s of one scene; ensemble: scene-steps/s of 256 scenes; "
-                         "adjoint: fwd+bwd ms/frame of the inverse problem")
+                         "adjoint: fwd+bwd ms/frame of the inverse problem; "
+                         "ssf: frames/s of the screen-space fluid render of 1M particles at 1600x1200")
     ap.add_argument("--frames", type=int, default=60, help="frames of the inverse problem (adjoint workload)")
     ap.add_argument("--evals", type=int, default=5, help="timed gradient evaluations (adjoint workload)")
     ap.add_argument("--scenes", type=int, default=256)
@@ -595,6 +693,8 @@ def main(argv=None):
         run_ensemble(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "ssf":
+        run_ssf(args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -1,7 +1,7 @@
 """Build recipe for the CPU oracle (test infrastructure).
 
-Compiles oracle/pbf_oracle.c twice (float port + FP64 oracle) into one shared
-library, oracle/_build/liboracle.so, with gcc and OpenMP.  Portable C: the same
+Compiles oracle/pbf_oracle.c and oracle/ssf_oracle.c twice each (float port +
+FP64 oracle) into one shared library, oracle/_build/liboracle.so, with gcc and OpenMP.  Portable C: the same
 recipe builds on x86_64 and aarch64 hosts.
 
     python oracle/build_oracle.py
@@ -15,6 +15,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "pbf_oracle.c"
+SSF_SRC = HERE / "ssf_oracle.c"
 OUT_DIR = HERE / "_build"
 LIB = OUT_DIR / "liboracle.so"
 CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unknown-pragmas"]
@@ -22,18 +23,19 @@ CFLAGS = ["-O2", "-fPIC", "-std=gnu11", "-fopenmp", "-ffp-contract=off", "-Wall"
 
 def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile the oracle library if it is missing or older than its sources."""
-    deps = [SRC, HERE.parent / "include" / "pbf.h", Path(__file__)]
+    deps = [SRC, SSF_SRC, HERE.parent / "include" / "pbf.h", HERE.parent / "include" / "pbf_ssf.h", Path(__file__)]
     if LIB.exists() and not force and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     OUT_DIR.mkdir(parents=True, exist_ok=True)
     objs = []
-    for tag, defs in (("f32", []), ("f64", ["-DORACLE_F64"])):
-        obj = OUT_DIR / f"pbf_oracle_{tag}.o"
-        cmd = ["gcc", *CFLAGS, *defs, "-c", str(SRC), "-o", str(obj)]
-        if verbose:
-            print(" ".join(cmd))
-        subprocess.run(cmd, check=True)
-        objs.append(str(obj))
+    for src in (SRC, SSF_SRC):
+        for tag, defs in (("f32", []), ("f64", ["-DORACLE_F64"])):
+            obj = OUT_DIR / f"{src.stem}_{tag}.o"
+            cmd = ["gcc", *CFLAGS, *defs, "-c", str(src), "-o", str(obj)]
+            if verbose:
+                print(" ".join(cmd))
+            subprocess.run(cmd, check=True)
+            objs.append(str(obj))
     tmp = LIB.with_suffix(f".so.tmp{os.getpid()}")
     subprocess.run(["gcc", "-shared", "-fopenmp", "-o", str(tmp), *objs, "-lm"], check=True)
     os.replace(tmp, LIB)

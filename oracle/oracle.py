@@ -245,3 +245,117 @@ def density_grid_backward(pos, lo, hi, dims, h, g_grid):
         dq = g[:, None] * (-3.0 * coef * w * w) * 2.0
         out[s:s + 2048, :3] = (dq[:, :, None] * r).sum(0)
     return out
+
+
+# ---- screen-space fluid renderer (oracle/ssf_oracle.c) ------------------------------------
+
+class OracleSsfParams(ctypes.Structure):
+    """Field-for-field mirror of ``pbf_ssf_params`` (include/pbf_ssf.h)."""
+
+    _fields_ = [
+        ("width", ctypes.c_int), ("height", ctypes.c_int),
+        ("view", ctypes.c_float * 16), ("proj", ctypes.c_float * 16),
+        ("p_n", ctypes.c_float), ("p_f", ctypes.c_float), ("p_t", ctypes.c_float), ("p_r", ctypes.c_float),
+        ("radius", ctypes.c_float),
+        ("smooth_niter", ctypes.c_int), ("kernel_r", ctypes.c_int),
+        ("sigma_r", ctypes.c_float), ("sigma_z", ctypes.c_float),
+        ("keep_edge", ctypes.c_int), ("blur_option", ctypes.c_int), ("shading_option", ctypes.c_int),
+        ("r0", ctypes.c_float), ("sky", ctypes.c_float * 3),
+    ]
+
+
+def to_oracle_ssf_params(p) -> OracleSsfParams:
+    """Copy any object with pbf_ssf_params' field names into an OracleSsfParams."""
+    out = OracleSsfParams()
+    for name, ctype in OracleSsfParams._fields_:
+        v = getattr(p, name)
+        if hasattr(ctype, "_length_"):
+            arr = getattr(out, name)
+            for k in range(ctype._length_):
+                arr[k] = float(v[k])
+        else:
+            setattr(out, name, v)
+    return out
+
+
+def ssf_render(params, pos, sky=None, color=None, prec: str = "f32"):
+    """The reference's SSF render (fluids/SSFRenderer.cpp:113-146) on host arrays.
+
+    pos: (n, 4) float32 positions; sky: optional (6, S, S, 3) float32 cube map;
+    color: optional (H, W, 4) float32 image the shading writes into (a copy is
+    returned).  Returns a dict of (H, W[, 4]) float32 images depth_raw, depth,
+    thick, normal_D, color, and the fragment count."""
+    L = lib()
+    fn = getattr(L, f"oracle_ssf_render_{prec}")
+    f32p = ctypes.POINTER(ctypes.c_float)
+    fn.argtypes = [ctypes.POINTER(OracleSsfParams), f32p, ctypes.c_int, f32p, ctypes.c_int, f32p, f32p, f32p, f32p,
+                   f32p]
+    fn.restype = ctypes.c_longlong
+    op = to_oracle_ssf_params(params)
+    W, H = op.width, op.height
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    n = pos.shape[0]
+    if n:
+        assert pos.shape == (n, 4)
+    out = {k: np.zeros((H, W), np.float32) for k in ("depth_raw", "depth", "thick")}
+    out["normal_D"] = np.zeros((H, W, 4), np.float32)
+    out["color"] = (np.zeros((H, W, 4), np.float32) if color is None
+                    else np.ascontiguousarray(color, dtype=np.float32).copy())
+    if sky is not None:
+        sky = np.ascontiguousarray(sky, dtype=np.float32)
+        assert sky.ndim == 4 and sky.shape[0] == 6 and sky.shape[1] == sky.shape[2] and sky.shape[3] == 3
+    null = f32p()
+    frags = fn(ctypes.byref(op), _ptr(pos, ctypes.c_float) if n else null, n,
+               _ptr(sky, ctypes.c_float) if sky is not None else null, 0 if sky is None else sky.shape[1],
+               _ptr(out["depth_raw"], ctypes.c_float), _ptr(out["depth"], ctypes.c_float),
+               _ptr(out["thick"], ctypes.c_float), _ptr(out["normal_D"], ctypes.c_float),
+               _ptr(out["color"], ctypes.c_float))
+    if frags < 0:
+        raise ValueError(f"oracle_ssf_render_{prec} rejected its arguments")
+    out["fragments"] = int(frags)
+    return out
+
+
+def ssf_smooth(params, raw, prec: str = "f32"):
+    """smooth_niter smoothing passes from a splatted depth image (H, W)."""
+    f32p = ctypes.POINTER(ctypes.c_float)
+    fn = getattr(lib(), f"oracle_ssf_smooth_{prec}")
+    fn.argtypes = [ctypes.POINTER(OracleSsfParams), f32p, f32p]
+    fn.restype = ctypes.c_int
+    raw = np.ascontiguousarray(raw, dtype=np.float32)
+    out = np.zeros_like(raw)
+    if fn(ctypes.byref(to_oracle_ssf_params(params)), _ptr(raw, ctypes.c_float), _ptr(out, ctypes.c_float)) != 0:
+        raise ValueError("oracle_ssf_smooth rejected its arguments")
+    return out
+
+
+def ssf_normals(params, depth, prec: str = "f32"):
+    """Normal restoration of a depth image (H, W) -> (H, W, 4)."""
+    f32p = ctypes.POINTER(ctypes.c_float)
+    fn = getattr(lib(), f"oracle_ssf_normals_{prec}")
+    fn.argtypes = [ctypes.POINTER(OracleSsfParams), f32p, f32p]
+    fn.restype = ctypes.c_int
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    out = np.zeros(depth.shape + (4,), np.float32)
+    if fn(ctypes.byref(to_oracle_ssf_params(params)), _ptr(depth, ctypes.c_float), _ptr(out, ctypes.c_float)) != 0:
+        raise ValueError("oracle_ssf_normals rejected its arguments")
+    return out
+
+
+def ssf_shade(params, depth, normal_D, thick, color, sky=None, prec: str = "f32"):
+    """Shading of given images; returns a shaded copy of color (H, W, 4)."""
+    f32p = ctypes.POINTER(ctypes.c_float)
+    fn = getattr(lib(), f"oracle_ssf_shade_{prec}")
+    fn.argtypes = [ctypes.POINTER(OracleSsfParams), f32p, f32p, f32p, f32p, ctypes.c_int, f32p]
+    fn.restype = ctypes.c_int
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    nd = np.ascontiguousarray(normal_D, dtype=np.float32)
+    th = np.ascontiguousarray(thick, dtype=np.float32)
+    out = np.ascontiguousarray(color, dtype=np.float32).copy()
+    sk = None if sky is None else np.ascontiguousarray(sky, dtype=np.float32)
+    rc = fn(ctypes.byref(to_oracle_ssf_params(params)), _ptr(depth, ctypes.c_float), _ptr(nd, ctypes.c_float),
+            _ptr(th, ctypes.c_float), _ptr(sk, ctypes.c_float) if sk is not None else f32p(),
+            0 if sk is None else sk.shape[1], _ptr(out, ctypes.c_float))
+    if rc != 0:
+        raise ValueError("oracle_ssf_shade rejected its arguments")
+    return out

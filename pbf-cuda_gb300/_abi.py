@@ -52,6 +52,21 @@ EXPORTED = (
     "pbf_step_noalloc",
 )
 
+# Every symbol include/pbf_ssf.h declares, in declaration order.
+EXPORTED_SSF = (
+    "pbf_ssf_params_default",
+    "pbf_ssf_look_at",
+    "pbf_ssf_create",
+    "pbf_ssf_destroy",
+    "pbf_ssf_set_params",
+    "pbf_ssf_get_params",
+    "pbf_ssf_set_sky",
+    "pbf_ssf_render",
+    "pbf_ssf_images",
+    "pbf_ssf_profile_enable",
+    "pbf_ssf_profile_read",
+)
+
 
 class PbfParams(ctypes.Structure):
     """Mirror of ``pbf_params``; field names follow the reference's GUIParams
@@ -121,6 +136,40 @@ class PbfTuning(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class PbfSsfParams(ctypes.Structure):
+    """Mirror of ``pbf_ssf_params`` (include/pbf_ssf.h); renderer fields follow
+    the reference's GUIParams renderer fields (fluids/GUIParams.h:19-38)."""
+
+    _fields_ = [
+        ("width", ctypes.c_int), ("height", ctypes.c_int),
+        ("view", ctypes.c_float * 16), ("proj", ctypes.c_float * 16),
+        ("p_n", ctypes.c_float), ("p_f", ctypes.c_float), ("p_t", ctypes.c_float), ("p_r", ctypes.c_float),
+        ("radius", ctypes.c_float),
+        ("smooth_niter", ctypes.c_int), ("kernel_r", ctypes.c_int),
+        ("sigma_r", ctypes.c_float), ("sigma_z", ctypes.c_float),
+        ("keep_edge", ctypes.c_int), ("blur_option", ctypes.c_int), ("shading_option", ctypes.c_int),
+        ("r0", ctypes.c_float), ("sky", ctypes.c_float * 3),
+    ]
+
+    def copy(self) -> "PbfSsfParams":
+        out = PbfSsfParams()
+        ctypes.pointer(out)[0] = self
+        return out
+
+
+class PbfSsfProfile(ctypes.Structure):
+    """Mirror of ``pbf_ssf_profile``."""
+
+    _fields_ = [
+        ("splat_ms", ctypes.c_float), ("smooth_ms", ctypes.c_float), ("normal_ms", ctypes.c_float),
+        ("shade_ms", ctypes.c_float), ("total_ms", ctypes.c_float), ("launches", ctypes.c_int),
+        ("fragments", ctypes.c_longlong),
+    ]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
 class PbfError(RuntimeError):
     """A pbf_* call returned a status other than PBF_OK."""
 
@@ -169,6 +218,17 @@ def _declare(L) -> None:
         "pbf_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]),
         "pbf_batch_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, vp, vp]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
+        "pbf_ssf_params_default": (None, [P(PbfSsfParams)]),
+        "pbf_ssf_look_at": (ctypes.c_int, [P(PbfSsfParams), f3, f3, ctypes.c_float]),
+        "pbf_ssf_create": (ctypes.c_int, [P(PbfSsfParams), P(vp)]),
+        "pbf_ssf_destroy": (None, [vp]),
+        "pbf_ssf_set_params": (ctypes.c_int, [vp, P(PbfSsfParams)]),
+        "pbf_ssf_get_params": (ctypes.c_int, [vp, P(PbfSsfParams)]),
+        "pbf_ssf_set_sky": (ctypes.c_int, [vp, f3, ctypes.c_int]),
+        "pbf_ssf_render": (ctypes.c_int, [vp, vp, ctypes.c_int, vp, vp]),
+        "pbf_ssf_images": (ctypes.c_int, [vp, vp, vp, vp, vp]),
+        "pbf_ssf_profile_enable": (ctypes.c_int, [vp, ctypes.c_int]),
+        "pbf_ssf_profile_read": (ctypes.c_int, [vp, P(PbfSsfProfile)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

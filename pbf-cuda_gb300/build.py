@@ -22,7 +22,7 @@ CSRC = HERE / "csrc"
 BUILD_DIR = HERE / "_build"
 LIB_DIR = HERE / "lib"
 LIB = LIB_DIR / "libpbf.so"
-SOURCES = ["api.cu", "grid.cu", "solver.cu", "adjoint.cu", "noalloc.cu"]
+SOURCES = ["api.cu", "grid.cu", "solver.cu", "adjoint.cu", "noalloc.cu", "ssf.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = [
     *ARCH,
@@ -44,8 +44,8 @@ def nvcc() -> str:
 
 
 def _deps() -> list[Path]:
-    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + [HERE.parent / "include" / "pbf.h",
-                                                                     Path(__file__)]
+    return (sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cuh")) + sorted((HERE.parent / "include").glob("*.h")) +
+            [Path(__file__)])
 
 
 def _compile(src: str, ptxas_v: bool, defines=(), build_dir=None) -> tuple[str, str]:
