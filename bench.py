@@ -567,6 +567,11 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def covered_pixels(renderer) -> int:
+    """Pixels of the last render with fluid depth (the ones smoothing filters)."""
+    return int((renderer.images()["depth"] < 99).sum().item())
+
+
 def run_ssf(args):
     """frames/s of the screen-space fluid render (include/pbf_ssf.h): the 1M
     particles of the large sweep's lattice at 1600 x 1200 with the reference's
@@ -638,9 +643,12 @@ def run_ssf(args):
     phases = {k: round(prof[k], 4) for k in ("splat_ms", "smooth_ms", "normal_ms", "shade_ms", "total_ms")}
     dominant = max(("splat_ms", "smooth_ms", "normal_ms", "shade_ms"), key=lambda k: prof[k])
     npix = p.width * p.height
-    # algorithmic bytes: splat reads the positions and does one 4 B + one 8 B
-    # read-modify-write per fragment; a smoothing pass reads and writes one float per pixel
-    alg = {"splat_ms": 16 * n + 24 * prof["fragments"] + 28 * npix, "smooth_ms": 8 * npix * p.smooth_niter,
+    # algorithmic HBM bytes: the splat reads the positions and leaves two images
+    # (4 B depth key + 8 B fixed-point thickness per pixel; its per-fragment
+    # atomics resolve in L2, where the 23 MB images stay); clear and resolve
+    # write / read those images and write depth_a, depth_b, thickness; a
+    # smoothing pass reads and writes one float per pixel
+    alg = {"splat_ms": 16 * n + 12 * npix + 12 * npix + 24 * npix, "smooth_ms": 8 * npix * p.smooth_niter,
            "normal_ms": 20 * npix, "shade_ms": 40 * npix}
     peak, peak_kind = measured_peaks()
     achieved = alg[dominant] / (prof[dominant] / 1e3) / 1e9
@@ -652,6 +660,9 @@ def run_ssf(args):
                                f"2 bilateral passes (kernel_r 10), Fresnel shading, camera (3.2,-14,6)->(3.2,-3.2,1.6)",
                    "particles": n, "l2": "flushed before every timed render (512 MB write, outside the events)"},
         "phases_ms": phases, "fragments": prof["fragments"], "gpu_launches": prof["launches"] * args.steps,
+        "fragments_per_s": prof["fragments"] / (prof["splat_ms"] / 1e3),
+        "bilateral_taps_per_s": (2 * p.kernel_r + 1) ** 2 * covered_pixels(r) * p.smooth_niter
+                                / (prof["smooth_ms"] / 1e3),
         "roofline": {"bound": "hbm", "kernel": dominant.replace("_ms", ""), "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg[dominant], "traffic": None},

@@ -10,7 +10,8 @@
  * Compiled twice (oracle/build_oracle.py), like pbf_oracle.c:
  *   ORACLE_F64 -> oracle_ssf_*_f64: every quantity in double (the FP64 oracle);
  *   otherwise  -> oracle_ssf_*_f32: float, each operation rounded on its own
- *                 (-ffp-contract=off) in the order of the shader source, which
+ *                 (-ffp-contract=off; fused multiply-adds only where written as
+ *                 fmaf) in the order of the shader source, which
  *                 is also the order of the CUDA kernels' explicitly rounded
  *                 operations.  So the splats (depth, thickness) agree with the
  *                 GPU bit for bit, and so do the normals and the shading options
@@ -55,6 +56,7 @@ typedef double real;
 #define RMAX(a, b) fmax((a), (b))
 #define RMIN(a, b) fmin((a), (b))
 #define RINF HUGE_VAL
+#define RFMA(a, b, c) fma((a), (b), (c))
 #else
 typedef float real;
 #define SFX(name) name##_f32
@@ -66,6 +68,7 @@ typedef float real;
 #define RMAX(a, b) fmaxf((a), (b))
 #define RMIN(a, b) fminf((a), (b))
 #define RINF HUGE_VALF
+#define RFMA(a, b, c) fmaf((a), (b), (c))
 #endif
 
 #define CLEAR_DEPTH ((real)100)     /* glClearTexImage(d_depth_a/b, 100), SSFRenderer.cpp:159-162 */
@@ -175,6 +178,7 @@ static long long splat(const ssf_consts* c, const float* pos, int n, real* depth
     real size = c->r * c->p_n * (real)H / (-vz * c->p_t);
     if (!(size < RINF)) continue;
     size = RMAX(size, (real)1);
+    const real s2 = (real)2 / size;
     const real lox = xw - (real)0.5f * size, loy = yw - (real)0.5f * size;
     const real fx0 = RCEIL(lox - (real)0.5f), fx1 = RCEIL(lox + size - (real)0.5f) - (real)1;
     const real fy0 = RCEIL(loy - (real)0.5f), fy1 = RCEIL(loy + size - (real)0.5f) - (real)1;
@@ -182,14 +186,14 @@ static long long splat(const ssf_consts* c, const float* pos, int n, real* depth
     const int y0 = (int)RMAX(fy0, (real)0), y1 = (int)RMIN(fy1, (real)(H - 1));
     for (int py = y0; py <= y1; ++py)
       for (int px = x0; px <= x1; ++px) {
-        /* gl_PointCoord (upper-left origin); x = 2 s - 1, y = 2 t - 1 */
-        const real s = (real)0.5f + ((real)px + (real)0.5f - xw) / size;
-        const real t = (real)0.5f - ((real)py + (real)0.5f - yw) / size;
-        const real x = (real)2 * s - (real)1, y = (real)2 * t - (real)1;
-        const real pho = x * x + y * y;
+        /* gl_PointCoord (upper-left origin), one reciprocal of the point size per
+         * sprite: x = 2 s - 1 = (px + 1/2 - xw) 2 / size, y = 2 t - 1 = (yw - py - 1/2) 2 / size */
+        const real x = ((real)px + (real)0.5f - xw) * s2;
+        const real y = (yw - ((real)py + (real)0.5f)) * s2;
+        const real pho = RFMA(x, x, y * y);
         if (pho > 1) continue; /* discard */
         const real z = RSQRT((real)1 - pho);
-        const real d = -(vz + z * c->r); /* -nviewPos.z, nviewPos = viewPos + (x, y, z) r */
+        const real d = -RFMA(z, c->r, vz); /* -nviewPos.z, nviewPos = viewPos + (x, y, z) r */
         const real th = (real)2 * c->r * z;
         const size_t k = (size_t)py * W + px;
         if (d < depth[k]) depth[k] = d;

@@ -14,9 +14,11 @@
 //                 2 r z in 64-bit fixed point (2^-32 per unit): both independent
 //                 of the order fragments arrive in, so renders are deterministic.
 //                 The vertex and fragment arithmetic is written with explicitly
-//                 rounded operations (no contraction into fused multiply-adds) in
-//                 the order of the shader source, so the float oracle, compiled
-//                 the same way, reproduces depth and thickness bit for bit.
+//                 rounded operations (fused multiply-adds only where written
+//                 out) in the order of the shader source, so the float oracle,
+//                 written the same way, reproduces depth and thickness bit for
+//                 bit.  gl_PointCoord takes one reciprocal of the point size per
+//                 sprite (GL leaves its precision to the implementation).
 //   k_ssf_smooth  32 x 16 output pixels per 256-thread block, the source tile
 //                 and its kernel_r halo staged in shared memory with the spatial
 //                 weights; taps summed in the shader's order (dx outer, dy inner).
@@ -87,8 +89,8 @@ __device__ __forceinline__ float depth_of_key(uint32_t k) {
 // One particle's sprite: the vertex shader (SSFget_depth.v.glsl:15-24) and
 // the point's window-space square, clipped to the image.
 struct Sprite {
-  float xw, yw, size, vz;
-  int x0, x1, y0, y1;  // inclusive pixel ranges; empty when x0 > x1
+  float xw, yw, s2, vz;  // s2 = 2 / gl_PointSize
+  int x0, x1, y0, y1;    // inclusive pixel ranges; empty when x0 > x1
 };
 
 __device__ __forceinline__ bool make_sprite(const SsfConsts& c, float4 p, Sprite& s) {
@@ -105,12 +107,13 @@ __device__ __forceinline__ bool make_sprite(const SsfConsts& c, float4 p, Sprite
   // gl_PointSize = r * p_n * s_h / (-viewPos.z * p_t), at least one pixel
   const float size = fd(fm(fm(c.r, c.p_n), (float)c.H), fm(-vz, c.p_t));
   if (!(size < INFINITY)) return false;
-  s.size = fmaxf(size, 1.f);
+  const float sz = fmaxf(size, 1.f);
+  s.s2 = fd(2.f, sz);
   s.vz = vz;
   // pixels whose centres lie in [xw - size/2, xw + size/2)
-  const float lox = fs(s.xw, fm(0.5f, s.size)), loy = fs(s.yw, fm(0.5f, s.size));
-  const float fx0 = ceilf(fs(lox, 0.5f)), fx1 = ceilf(fs(fa(lox, s.size), 0.5f)) - 1.f;
-  const float fy0 = ceilf(fs(loy, 0.5f)), fy1 = ceilf(fs(fa(loy, s.size), 0.5f)) - 1.f;
+  const float lox = fs(s.xw, fm(0.5f, sz)), loy = fs(s.yw, fm(0.5f, sz));
+  const float fx0 = ceilf(fs(lox, 0.5f)), fx1 = ceilf(fs(fa(lox, sz), 0.5f)) - 1.f;
+  const float fy0 = ceilf(fs(loy, 0.5f)), fy1 = ceilf(fs(fa(loy, sz), 0.5f)) - 1.f;
   s.x0 = (int)fmaxf(fx0, 0.f);
   s.x1 = (int)fminf(fx1, (float)(c.W - 1));
   s.y0 = (int)fmaxf(fy0, 0.f);
@@ -135,33 +138,35 @@ __global__ void __launch_bounds__(256) k_ssf_splat(SsfConsts c, const float4* __
   Sprite me = {};
   const bool ok = i < n && make_sprite(c, pos[i], me);
   unsigned frags = 0;
+  // thickness 2 r z in fixed point: z (2 r 2^32), the same value as (2 r z) 2^32
+  const float qscale = fm(fm(2.f, c.r), kThickScale);
   unsigned todo = __ballot_sync(0xffffffffu, ok);
   while (todo) {
     const int src = __ffs(todo) - 1;
     todo &= todo - 1u;
     const float xw = __shfl_sync(0xffffffffu, me.xw, src), yw = __shfl_sync(0xffffffffu, me.yw, src);
-    const float size = __shfl_sync(0xffffffffu, me.size, src), vz = __shfl_sync(0xffffffffu, me.vz, src);
+    const float s2 = __shfl_sync(0xffffffffu, me.s2, src), vz = __shfl_sync(0xffffffffu, me.vz, src);
     const int x0 = __shfl_sync(0xffffffffu, me.x0, src), x1 = __shfl_sync(0xffffffffu, me.x1, src);
     const int y0 = __shfl_sync(0xffffffffu, me.y0, src), y1 = __shfl_sync(0xffffffffu, me.y1, src);
-    const int w = x1 - x0 + 1;  // 1 .. W
-    const long long total = (long long)w * (y1 - y0 + 1);
+    const int w = x1 - x0 + 1;                 // 1 .. W
+    const int total = w * (y1 - y0 + 1);       // <= W H < 2^31
     // fragment f = row * w + col, lanes strided by 32 (row, col stepped incrementally)
     int row = lane / w, col = lane - (lane / w) * w;
     const int drow = 32 / w, dcol = 32 - drow * w;
-    for (long long f = lane; f < total; f += 32) {
+    for (int f = lane; f < total; f += 32) {
       const int px = x0 + col, py = y0 + row;
-      // gl_PointCoord (upper-left origin) and the fragment shader (SSFget_depth.f.glsl:21-37)
-      const float s = fa(0.5f, fd(fs(fa((float)px, 0.5f), xw), size));
-      const float t = fs(0.5f, fd(fs(fa((float)py, 0.5f), yw), size));
-      const float x = fs(fm(2.f, s), 1.f), y = fs(fm(2.f, t), 1.f);
-      const float pho = fa(fm(x, x), fm(y, y));
+      // the fragment shader (SSFget_depth.f.glsl:21-37) at gl_PointCoord (upper-left
+      // origin): x = 2 s - 1 = (px + 1/2 - xw) 2 / size, y = 2 t - 1 = (yw - py - 1/2) 2 / size
+      const float x = fm(fs(fa((float)px, 0.5f), xw), s2);
+      const float y = fm(fs(yw, fa((float)py, 0.5f)), s2);
+      const float pho = __fmaf_rn(x, x, fm(y, y));
       if (!(pho > 1.f)) {
         const float z = __fsqrt_rn(fs(1.f, pho));
-        const float depth = -fa(vz, fm(z, c.r));          // -nviewPos.z
-        const float thick = fm(fm(2.f, c.r), z);          // 2 r dot((x, y, z), (0, 0, 1)) (SSFget_thick.f.glsl:24-25)
+        const float depth = -__fmaf_rn(z, c.r, vz);  // -nviewPos.z, nviewPos = viewPos + (x, y, z) r
         const size_t k = (size_t)py * c.W + px;
         atomicMin(zkey + k, depth_key(depth));
-        const long long q = __float2ll_rn(fm(thick, kThickScale));
+        // 2 r dot((x, y, z), (0, 0, 1)) (SSFget_thick.f.glsl:24-25)
+        const long long q = __float2ll_rn(fm(z, qscale));
         if (q) atomicAdd(tfx + k, (unsigned long long)q);
         ++frags;
       }
@@ -193,8 +198,9 @@ __global__ void __launch_bounds__(256) k_ssf_resolve(int npix, const uint32_t* _
 }
 
 // One smoothing pass (SSFsmooth_depth.f.glsl:26-75): dst keeps its content where
-// the source depth is background (> 99).  Taps in the shader's order, each
-// operation rounded on its own as the float oracle does; only expf differs.
+// the source depth is background (> 99).  Taps in the shader's order; the
+// range weight through exp2f and fused multiply-adds (within 1e-5 of the float
+// oracle's expf and separate roundings).
 __global__ void __launch_bounds__(kSmoothTileW * kSmoothThreadsY)
 k_ssf_smooth(SsfConsts c, const float* __restrict__ src, float* __restrict__ dst) {
   constexpr int kTW = kSmoothTileW + 2 * kMaxKernelR, kTH = kSmoothTileH + 2 * kMaxKernelR;
@@ -227,14 +233,16 @@ k_ssf_smooth(SsfConsts c, const float* __restrict__ src, float* __restrict__ dst
     if (z > kBackground) continue;
     float sum = 0.f, wsum = 0.f;
     if (c.blur_option == 0) {
+      // g = exp(-((s - z) blur_z)^2) = 2^-((s - z) blur_z sqrt(log2 e))^2
+      const float bz = c.blur_z * 1.2011224087864498f;
       for (int dx = -R; dx <= R; ++dx) {
         const float* wrow = wsp + (dx + R) * K + R;
         for (int dy = -R; dy <= R; ++dy) {
           const float s = center[dy * tw + dx];
-          const float r2 = fm(fs(s, z), c.blur_z);
-          const float wg = fm(wrow[dy], expf(fm(-r2, r2)));
-          sum = fa(sum, fm(s, wg));
-          wsum = fa(wsum, wg);
+          const float r2 = (s - z) * bz;
+          const float wg = wrow[dy] * exp2f(-r2 * r2);
+          sum = fmaf(s, wg, sum);
+          wsum += wg;
         }
       }
     } else {
@@ -242,8 +250,8 @@ k_ssf_smooth(SsfConsts c, const float* __restrict__ src, float* __restrict__ dst
         const float* wrow = wsp + (dx + R) * K + R;
         for (int dy = -R; dy <= R; ++dy) {
           const float w = wrow[dy];
-          sum = fa(sum, fm(center[dy * tw + dx], w));
-          wsum = fa(wsum, w);
+          sum = fmaf(center[dy * tw + dx], w, sum);
+          wsum += w;
         }
       }
     }

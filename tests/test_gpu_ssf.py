@@ -7,13 +7,13 @@ Bars, stage by stage, each stage fed the GPU's own input image:
     sprites at the near plane, odd image sizes, 1M particles at 1600 x 1200);
   * smoothing (bilateral and gaussian, 1-3 passes, kernel_r 0-20): the same
     background pixels, covered pixels within 1e-5 |z| of the float oracle
-    (the two differ only through expf);
+    (the GPU weighs by exp2f with fused multiply-adds, the oracle by expf);
   * normals (keep_edge 0 and 1): bit-exact;
   * shading: bit-exact for the options without exp (normal, Fresnel, reflect,
     refract), within 2e-6 for the others; the same pixels drawn;
   * end to end (the reference's settings): thickness bit-exact, depth within
     1e-5 |z|, 99.5% of normals and colours within 1e-3 of the float oracle
-    (median differences <= 2e-4 and 1e-4);
+    (median differences <= 5e-4 and 2e-4);
   * determinism: two renders bitwise identical.
 """
 from __future__ import annotations
@@ -177,17 +177,18 @@ def test_end_to_end_reference_settings(pbf, oracle, cuda):
     bg = o["depth"] >= 99
     assert np.array_equal(g["depth"] >= 99, bg)
     assert (np.abs(g["depth"][~bg] - o["depth"][~bg]) <= 1e-5 * o["depth"][~bg]).all()
-    # The smoothed depths differ by ~1e-7 relative (expf).  Normals amplify
+    # The smoothed depths differ by ~1e-7 relative (exp2f vs expf, fused
+    # multiply-adds).  Normals amplify
     # depth differences by ~1 / (c_x z) ~ 80 at 320 x 240 (n_x ~ dzdx / (c_x z)),
     # so their median difference is ~5e-5; and such differences can flip a
     # discrete choice (the one-sided difference at a ridge, a checker cell) at
     # a few pixels.  The stage tests above hold every stage exact on the GPU's
     # own inputs.
     dn = np.abs(g["normal_D"][..., :3] - o["normal_D"][..., :3]).max(-1)
-    assert (dn[~bg] <= 1e-3).mean() >= 0.995 and np.median(dn[~bg]) <= 2e-4
+    assert (dn[~bg] <= 1e-3).mean() >= 0.995 and np.median(dn[~bg]) <= 5e-4
     assert np.array_equal(g["color"][..., 3], o["color"][..., 3])
     dc = np.abs(g["color"] - o["color"]).max(-1)
-    assert (dc[~bg] <= 1e-3).mean() >= 0.995 and np.median(dc[~bg]) <= 1e-4
+    assert (dc[~bg] <= 1e-3).mean() >= 0.995 and np.median(dc[~bg]) <= 2e-4
 
 
 def test_deterministic_under_heavy_overlap(pbf, cuda):
