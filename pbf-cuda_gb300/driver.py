@@ -7,7 +7,9 @@ and calls Simulator::step once with the tic-toc buffer roles.  SceneDriver
 does the same without a window: `substeps` steps per frame (the scenes here
 use dt = 1/120 s, two per 1/60 s frame), the limits from the scene's own wall
 function or from a reference-style sweep, and optionally one particle state
-file per frame (scenes.save_state) for offline comparison.
+file per frame (scenes.save_state) for offline comparison and one rendered
+image per frame (the SSF surface, ssf.SSFRenderer, as Renderer::render draws
+after each simulated frame, fluids/FluidSystem.cpp:119).
 """
 from __future__ import annotations
 
@@ -18,6 +20,7 @@ from typing import Optional, Sequence, Tuple
 import torch
 
 from . import scenes as _scenes
+from . import ssf as _ssf
 from .simulator import ParticleState, Simulator
 
 
@@ -40,7 +43,8 @@ class SceneDriver:
     """Runs a scenes.Scene frame by frame on the GPU."""
 
     def __init__(self, scene: _scenes.Scene, substeps: int = _scenes.SUBSTEPS, sweep: Optional[Sweep] = None,
-                 dump_dir=None, dump_every: int = 1):
+                 dump_dir=None, dump_every: int = 1, render_dir=None,
+                 renderer: Optional["_ssf.SSFRenderer"] = None, y_up: bool = True):
         self.scene = scene
         self.substeps = int(substeps)
         self.sweep = sweep
@@ -52,6 +56,15 @@ class SceneDriver:
         self.t = 0.0
         if self.dump_dir is not None:
             self.dump_dir.mkdir(parents=True, exist_ok=True)
+        # rendered frames: renderer (its camera and settings) or the reference's defaults
+        self.render_dir = Path(render_dir) if render_dir is not None else None
+        self.renderer = renderer
+        self.y_up = bool(y_up)
+        self.last_image = None
+        if self.render_dir is not None:
+            self.render_dir.mkdir(parents=True, exist_ok=True)
+            if self.renderer is None:
+                self.renderer = _ssf.SSFRenderer()
 
     def limits(self) -> Tuple[Tuple[float, ...], Tuple[float, ...]]:
         if self.sweep is not None:
@@ -67,6 +80,14 @@ class SceneDriver:
         self.frame += 1
         if self.dump_dir is not None and self.frame % self.dump_every == 0:
             self.dump(self.dump_dir / f"frame_{self.frame:06d}.bin")
+        if self.render_dir is not None and self.frame % self.dump_every == 0:
+            _ssf.write_ppm(self.render_dir / f"frame_{self.frame:06d}.ppm", self.render())
+
+    def render(self) -> torch.Tensor:
+        """The SSF image of the current state (positions turned z-up when the scene is y-up)."""
+        pos = self.state.pos
+        self.last_image = self.renderer.render(_ssf.z_up(pos) if self.y_up else pos.contiguous())
+        return self.last_image
 
     def run(self, frames: int) -> None:
         for _ in range(int(frames)):
@@ -79,6 +100,8 @@ class SceneDriver:
 
     def close(self) -> None:
         self.sim.close()
+        if self.renderer is not None:
+            self.renderer.close()
 
     def __enter__(self):
         return self

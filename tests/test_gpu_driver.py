@@ -32,3 +32,26 @@ def test_driver_matches_manual_steps_and_dumps(pbf, cuda, tmp_path):
         torch.cuda.synchronize()
         np.testing.assert_array_equal(st.pos.cpu().numpy(), got)
         np.testing.assert_array_equal(st.iid[: st.n].cpu().numpy().astype(np.uint32), iid3)
+
+
+def test_driver_renders_frames(pbf, oracle, cuda, tmp_path):
+    """One SSF image per frame; the last one equals the oracle's splat of the
+    same state bit for bit (no smoothing, so the raw depth reaches shading)."""
+    import torch
+
+    sc = pbf.scenes.dam_break(seed=1)
+    p = pbf.ssf_default_params(160, 120)
+    pbf.ssf.look_at(p, (2.6, -3.2, 1.8), (0.5, -0.5, 0.5))
+    p.smooth_niter = 0
+    r = pbf.SSFRenderer(p)
+    with pbf.driver.SceneDriver(sc, substeps=2, render_dir=tmp_path, renderer=r) as drv:
+        drv.run(2)
+        torch.cuda.synchronize()
+        state = drv.state.pos.cpu().numpy()
+        depth = r.images()["depth"].cpu().numpy()
+    files = sorted(tmp_path.glob("frame_*.ppm"))
+    assert [f.name for f in files] == ["frame_000001.ppm", "frame_000002.ppm"]
+    assert files[-1].read_bytes().startswith(b"P6 160 120 255\n")
+    zup = np.stack([state[:, 0], -state[:, 2], state[:, 1], state[:, 3]], 1).astype(np.float32)
+    o = oracle.ssf_render(p, zup, prec="f32")
+    np.testing.assert_array_equal(depth.view(np.uint32), o["depth_raw"].view(np.uint32))
