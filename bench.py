@@ -261,7 +261,7 @@ def run_ours(args):
     sim.profile(False)
 
     # -- end to end through the public API with host buffers ------------------------
-    e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps, stream)
+    e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps or args.steps, stream)
     alt = (measure_reference_params(pkg, torch, args, stream)
            if args.params == "scene" and args.scene == "large_sweep" else None)
 
@@ -619,7 +619,7 @@ def run_ssf(args):
     host_pos = pos.cpu().pin_memory()
     host_img = torch.empty(color.shape, dtype=torch.float32).pin_memory()
     dev_pos = torch.empty_like(pos)
-    e2e_frames = min(args.steps, 20)
+    e2e_frames = args.e2e_steps or args.steps
     torch.cuda.synchronize()
     e0.record(stream)
     for _ in range(e2e_frames):
@@ -691,7 +691,8 @@ def main(argv=None):
     ap.add_argument("--scenes", type=int, default=256)
     ap.add_argument("--params", choices=("scene", "reference"), default="scene",
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
-    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="steps of the end-to-end measurement (default: the timed steps, from the same state)")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
     ap.add_argument("--cpu-steps", type=int, default=20,
                     help="most steps the CPU baseline times (0: no CPU baseline, for profiling runs)")
