@@ -254,6 +254,13 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
                         pbf_tuning* out, void* stream);
 pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, const uint32_t* iid, int steps,
                               pbf_tuning* out, void* stream);
+/* The dense-kernel choice of the following steps, set directly (e.g. a choice
+ * an earlier pbf_autotune returned): dense_window >= 32 candidates, or 0 for
+ * the default; dense_all 1 (every warp dense), 0 (by window) or -1 (the
+ * default: every warp dense below 131072 particles).  ms fields are ignored
+ * on set and 0 on get. */
+pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
+pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
 
 /*
  * One step, same contract and results as pbf_step, for callers that cannot

@@ -49,6 +49,8 @@ EXPORTED = (
     "pbf_batch_use_graphs",
     "pbf_autotune",
     "pbf_batch_autotune",
+    "pbf_set_tuning",
+    "pbf_get_tuning",
     "pbf_step_noalloc",
 )
 
@@ -217,6 +219,8 @@ def _declare(L) -> None:
         "pbf_batch_use_graphs": (ctypes.c_int, [vp, ctypes.c_int]),
         "pbf_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, ctypes.c_int, vp, vp]),
         "pbf_batch_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, vp, vp]),
+        "pbf_set_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
+        "pbf_get_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
         "pbf_ssf_params_default": (None, [P(PbfSsfParams)]),
         "pbf_ssf_look_at": (ctypes.c_int, [P(PbfSsfParams), f3, f3, ctypes.c_float]),

@@ -1134,7 +1134,7 @@ pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], 
 namespace {
 
 // Candidate dense-kernel choices, timed by pbf_autotune / pbf_batch_autotune.
-constexpr int kTuneWindows[] = {256, 512, 1024, 2048};
+constexpr int kTuneWindows[] = {64, 128, 256, 512, 1024, 2048};
 
 // Runs `steps` steps per candidate on copies of (pos, vel, iid) through
 // step(window, all, bufs...) and returns the fastest choice.
@@ -1226,6 +1226,26 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
   }
   s->tune_window = out->dense_window;
   s->tune_all = out->dense_all;
+  return PBF_OK;
+}
+
+pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
+  if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
+  if (t->dense_window != 0 && t->dense_window < 32)
+    return fail(PBF_ERR_INVALID_ARG, "dense_window must be 0 (default) or >= 32 (got %d)", t->dense_window);
+  if (t->dense_all < -1 || t->dense_all > 1)
+    return fail(PBF_ERR_INVALID_ARG, "dense_all must be -1, 0 or 1 (got %d)", t->dense_all);
+  s->tune_window = t->dense_window;
+  s->tune_all = t->dense_all;
+  return PBF_OK;
+}
+
+pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
+  if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
+  t->dense_window = s->tune_window > 0 ? s->tune_window : pbf::kDefaultDenseWindow;
+  t->dense_all = s->tune_all;
+  t->ms_per_step = 0.f;
+  t->ms_default = 0.f;
   return PBF_OK;
 }
 

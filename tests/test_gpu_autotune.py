@@ -24,7 +24,7 @@ def test_autotune_single(pbf, oracle, cuda):
     with pbf.Simulator(p, sc.ulim, sc.llim, n) as sim:
         t = sim.autotune(pos, vel, iid, steps=2)
         torch.cuda.synchronize()
-        assert t["dense_window"] in (256, 512, 1024, 2048) and t["dense_all"] in (0, 1)
+        assert t["dense_window"] in (64, 128, 256, 512, 1024, 2048) and t["dense_all"] in (0, 1)
         assert t["ms_per_step"] > 0 and t["ms_default"] > 0 and t["ms_per_step"] <= t["ms_default"]
         for a, b in zip((pos, vel, iid), keep):
             assert torch.equal(a, b)
@@ -51,7 +51,7 @@ def test_autotune_batch(pbf, oracle, cuda):
     counts = [len(s[0]) for s in scenes]
     with pbf.Ensemble(p, [s[1] for s in scenes], [(0.0, 0.0, 0.0)] * len(scenes), counts) as ens:
         t = ens.autotune(st.pos, st.vel, st.iid, steps=2)
-        assert t["dense_window"] in (256, 512, 1024, 2048) and t["dense_all"] in (0, 1)
+        assert t["dense_window"] in (64, 128, 256, 512, 1024, 2048) and t["dense_all"] in (0, 1)
         st.step(ens)
         torch.cuda.synchronize()
         got = st.pos.cpu().numpy()
