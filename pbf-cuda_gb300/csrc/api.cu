@@ -270,6 +270,9 @@ cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
   if (e == cudaSuccess) e = alloc(&sol.grp_zero, slots);
   if (e == cudaSuccess) e = alloc(&sol.grp_item_off, slots);
   if (e == cudaSuccess) e = alloc(&sol.grp_item_slot, pbf::group_items(max_particles));
+  if (e == cudaSuccess) e = alloc(&sol.work_list, (size_t)max_particles + 1);
+  if (e == cudaSuccess) e = alloc(&sol.work_follow, (size_t)max_particles + 1);
+  if (e == cudaSuccess) e = alloc(&sol.work_blocks, pbf::work_blocks_len(max_particles));
   // what the group kernels expect to find at zero
   if (e == cudaSuccess) e = cudaMemset(sol.grp_hash, 0, sizeof(int) * 8 * entries);
   if (e == cudaSuccess) e = cudaMemset(sol.grp_max, 0, sizeof(unsigned) * entries);
@@ -287,7 +290,8 @@ void free_all(pbf_solver* s) {
                   s->sol.cell_flags, s->sol.grp_cell, s->sol.grp_off, s->sol.grp_n, s->sol.grp_rep, s->sol.grp_cnt,
                   s->sol.grp_pos, s->sol.grp_sum, s->sol.grp_aux, s->sol.grp_id, s->sol.grp_hash,
                   s->sol.grp_max, s->sol.grp_acc, s->sol.grp_list, s->sol.grp_list_n, s->sol.grp_done,
-                  s->sol.grp_zero, s->sol.grp_item_off, s->sol.grp_item_slot};
+                  s->sol.grp_zero, s->sol.grp_item_off, s->sol.grp_item_slot, s->sol.work_list,
+                  s->sol.work_follow, s->sol.work_blocks};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -653,7 +657,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
   s->last_launches = s->last_grid_launches + 1 + pbf::pass_launches(c, n) * (2 * niter + 1) +
-                     pbf::group_launches(n, niter) + (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
+                     pbf::group_launches(c, n, niter) + (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
   if (taping) {
@@ -904,7 +908,8 @@ void batch_free(pbf_batch* b) {
                   b->sol.cell_flags, b->sol.grp_cell, b->sol.grp_off, b->sol.grp_n, b->sol.grp_rep, b->sol.grp_cnt,
                   b->sol.grp_pos, b->sol.grp_sum, b->sol.grp_aux, b->sol.grp_id, b->sol.grp_hash,
                   b->sol.grp_max, b->sol.grp_acc, b->sol.grp_list, b->sol.grp_list_n, b->sol.grp_done,
-                  b->sol.grp_zero, b->sol.grp_item_off, b->sol.grp_item_slot, b->d_geom, b->d_sid};
+                  b->sol.grp_zero, b->sol.grp_item_off, b->sol.grp_item_slot, b->sol.work_list,
+                  b->sol.work_follow, b->sol.work_blocks, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);

@@ -93,7 +93,10 @@ constexpr size_t kOffGrpDone = kOffGrpListN + align_up(4 * kSlots);
 constexpr size_t kOffGrpZero = kOffGrpDone + align_up(4 * kSlots);
 constexpr size_t kOffGrpItemOff = kOffGrpZero + align_up(4 * kSlots);
 constexpr size_t kOffGrpItemSlot = kOffGrpItemOff + align_up(4 * kSlots);
-constexpr size_t kNoAllocScratchBytes = kOffGrpItemSlot + align_up(4 * kItems);
+constexpr size_t kOffWorkList = kOffGrpItemSlot + align_up(4 * kItems);
+constexpr size_t kOffWorkFollow = kOffWorkList + align_up(4 * (kNp + 1));
+constexpr size_t kOffWorkBlocks = kOffWorkFollow + align_up(4 * (kNp + 1));
+constexpr size_t kNoAllocScratchBytes = kOffWorkBlocks + align_up(4 * pbf::work_blocks_len(kNoAllocMaxParticles));
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -175,6 +178,9 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.grp_zero = (int*)(base + kOffGrpZero);
   s.grp_item_off = (int*)(base + kOffGrpItemOff);
   s.grp_item_slot = (int*)(base + kOffGrpItemSlot);
+  s.work_list = (int*)(base + kOffWorkList);
+  s.work_follow = (int*)(base + kOffWorkFollow);
+  s.work_blocks = (int*)(base + kOffWorkBlocks);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;

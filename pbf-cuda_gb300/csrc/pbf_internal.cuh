@@ -194,7 +194,21 @@ struct SolverScratch {
   int* grp_zero;       // [group_slots] every deviation of the pass's sums is zero
   int* grp_item_off;   // [group_slots] first work item of each slot
   int* grp_item_slot;  // [group_items] slot of each work item
+  // work lists of the lambda and delta_p passes (see solver.cu): the
+  // particles that compute, and for each follower its group's first particle
+  int* work_list;      // [max_particles]
+  int* work_follow;    // [max_particles] -1, or the sorted slot whose results particle i takes
+  int* work_blocks;    // [work_blocks_len(max_particles)] per-block counts, then offsets
 };
+
+// Lambda and delta_p results are the same for every particle of a position
+// group (same position: same window, same candidates in the same order; a
+// co-located particle adds W(0) to rho and, at r < kernel_eps, no gradient,
+// exactly as the particle itself does), so those passes run once per group,
+// on its first particle, and copy the results to the others (the followers).
+// The computing particles are listed in cell order per iteration.
+constexpr int kWorkThreads = 1024;
+constexpr size_t work_blocks_len(int max_particles) { return (size_t)max_particles / kWorkThreads + 2; }
 
 // Bits of SolverScratch::cell_flags: the stale cell of a particle whose
 // value can poison a neighbour's sum the way the reference's IEEE arithmetic
@@ -245,7 +259,9 @@ enum StepFlag {
   kGroupCount = 4,           // cells with a group slot (set by reorder)
   kGroupPool = 5,            // group pool entries handed out (set by reorder)
   kGroupItems = 6,           // group work items (set by reorder)
-  kNumFlags = 7
+  kWorkCount = 7,            // particles on the current iteration's work list
+  kWorkDone = 8,             // blocks of the work-list count finished (0 between uses)
+  kNumFlags = 9
 };
 
 // Entries of the dense list: one per warp of 32 consecutive particles.
@@ -292,8 +308,9 @@ constexpr int kVorticityLaunches = 2;
 // Kernel launches of one neighbour pass of n particles (sparse kernel unless
 // every warp goes dense, dense kernel).
 int pass_launches(const StepConsts& c, int n);
-// Group-table launches of one step of n particles at niter iterations.
-int group_launches(int n, int niter);
+// Group-table, work-list and follower launches of one step of n particles at
+// niter iterations.
+int group_launches(const StepConsts& c, int n, int niter);
 
 // ---- reverse pass (adjoint.cu) ------------------------------------------------------
 

@@ -93,7 +93,16 @@ struct PassArgs {
   const float4* grp_pos;
   const float4* grp_sum;
   const float4* grp_aux;
+  // work list of the lambda / delta_p passes (null: every particle, in order);
+  // its length is flags[kWorkCount]
+  const int* list;
 };
+
+// The particle that thread slot t of a pass computes (t < work_count(a)).
+__device__ __forceinline__ int work_count(const PassArgs& a) {
+  return a.list ? (int)a.flags[kWorkCount] : a.n;
+}
+__device__ __forceinline__ int work_particle(const PassArgs& a, int t) { return a.list ? __ldg(a.list + t) : t; }
 
 // ---- windows ------------------------------------------------------------------------
 
@@ -648,8 +657,11 @@ template <int kKind>
 __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
   using P = typename PassOf<kKind>::type;
   if (a.dense_all) return;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool valid = i < a.n;
+  const int count = work_count(a);
+  if ((int)(blockIdx.x * blockDim.x) >= count) return;  // the whole block is past the list
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool valid = t < count;
+  const int i = valid ? work_particle(a, t) : 0;
   const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
   const int3 q = cell_of(a.c, g, xi);
@@ -659,7 +671,7 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
   const bool grouped = valid && total > a.c.dense_window && a.c.keps2 > 0.f;
   const int entries = grouped ? window_total_grouped(g, a, q) : total;
   if (__any_sync(kFull, entries > a.c.dense_window)) {
-    if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(i >> 5);
+    if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(t >> 5);
     return;
   }
   if (!valid) return;
@@ -688,10 +700,12 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
   // the warps the sparse kernel listed, or all of them
-  const uint32_t count = a.dense_all ? (uint32_t)((a.n + 31) / 32) : a.flags[a.counter];
+  const int work = work_count(a);
+  const uint32_t count = a.dense_all ? (uint32_t)((work + 31) / 32) : a.flags[a.counter];
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
-    const int i = (int)(a.dense_all ? item : a.dense[item]) * 32 + lane;
-    const bool valid = i < a.n;
+    const int t = (int)(a.dense_all ? item : a.dense[item]) * 32 + lane;
+    const bool valid = t < work;
+    const int i = valid ? work_particle(a, t) : 0;
     const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
     const int3 q = cell_of(a.c, g, xi);
@@ -845,6 +859,32 @@ __device__ __forceinline__ int block_scan(int flag, int* sh, int& total) {
   __syncthreads();
   total = sh[64];
   return sh[32 + warp] + in_warp;
+}
+
+// Exclusive prefix of `v` over the block in thread order; `total` gets the sum.
+__device__ __forceinline__ int block_scan_value(int v, int* sh, int& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  __syncthreads();
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    const int w = lane < kGroupWarps ? sh[lane] : 0;
+    int y = w;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int z = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) y += z;
+    }
+    if (lane < kGroupWarps) sh[32 + lane] = y - w;  // exclusive
+    if (lane == kGroupWarps - 1) sh[64] = y;
+  }
+  __syncthreads();
+  total = sh[64];
+  return sh[32 + warp] + x - v;
 }
 
 // A grouped cell's particles in work items of kGroupChunk; a kernel takes
@@ -1130,6 +1170,107 @@ __global__ void __launch_bounds__(kGroupThreads) k_group_devsum(GroupArgs a) {
   }
 }
 
+// ---- work lists: one computing particle per position group -----------------------------
+
+static_assert(kWorkThreads == kGroupThreads, "the work-list kernels use the group kernels' block scan");
+
+// Marks the followers of the current position groups (the group tables the
+// lambda pass of this iteration just built): follow[i] = the group's first
+// particle when particle i of a grouped cell is not that particle, else -1;
+// blocks[b] = the computing particles of block b.  The block that finishes
+// last turns blocks[] into exclusive offsets (so the list is in cell order).
+__global__ void __launch_bounds__(kWorkThreads)
+k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cell_flags,
+            const int* __restrict__ grp_n, const int* __restrict__ grp_off, const int* __restrict__ grp_id,
+            const int* __restrict__ grp_hash, const int* __restrict__ grp_rep, int np, int n,
+            int* __restrict__ follow, int* __restrict__ blocks, uint32_t* __restrict__ flags) {
+  __shared__ int sh[80];
+  __shared__ int s_last;
+  const int i = blockIdx.x * kWorkThreads + threadIdx.x;
+  int r = -1;
+  if (i < n) {
+    const uint32_t sl = cell_flags[skeys[i]] >> kCellSlotShift;
+    if (sl) {
+      const int slot = (int)sl - 1;
+      if (grp_n[slot] > 0) {
+        // the particle's hash entry -> its group's rank -> the group's first particle
+        const int t0 = grp_off[slot];
+        const int rank = grp_hash[2 * t0 + 6 * np + grp_id[i]];
+        const int rep = grp_rep[t0 + rank];
+        if (rep != i) r = rep;
+      }
+    }
+    follow[i] = r;
+  }
+  const int cnt = __syncthreads_count(i < n && r < 0);
+  if (threadIdx.x == 0) blocks[blockIdx.x] = cnt;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_last = atomicAdd(&flags[kWorkDone], 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // the last block: exclusive offsets of every block, in chunks of kWorkThreads
+  int carry = 0;
+  for (int b0 = 0; b0 < (int)gridDim.x; b0 += kWorkThreads) {
+    const int b = b0 + threadIdx.x;
+    const int v = b < (int)gridDim.x ? __ldcg(&blocks[b]) : 0;
+    int total;
+    const int ex = block_scan_value(v, sh, total);
+    if (b < (int)gridDim.x) blocks[b] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) {
+    flags[kWorkCount] = (uint32_t)carry;
+    flags[kWorkDone] = 0u;
+  }
+}
+
+// list[blocks[b] + rank] = i for the computing particles of block b, in order.
+__global__ void __launch_bounds__(kWorkThreads)
+k_work_list(const int* __restrict__ follow, const int* __restrict__ blocks, int n, int* __restrict__ list) {
+  __shared__ int sh[80];
+  const int i = blockIdx.x * kWorkThreads + threadIdx.x;
+  const bool keep = i < n && follow[i] < 0;
+  int total;
+  const int rank = block_scan(keep, sh, total);
+  if (keep) list[blocks[blockIdx.x] + rank] = i;
+}
+
+// The followers take their group's results.
+template <int kKind>
+__global__ void __launch_bounds__(256)
+k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __restrict__ X, float* __restrict__ lambda,
+         float* __restrict__ rho, float4* __restrict__ T, const float4* __restrict__ xs,
+         const uint32_t* __restrict__ iid_s, float4* __restrict__ npos, float4* __restrict__ vel,
+         float4* __restrict__ pos, uint32_t* __restrict__ iid, const uint32_t* __restrict__ skeys,
+         uint32_t* __restrict__ cell_flags, uint32_t* __restrict__ flags) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int r = follow[i];
+  if (r < 0) return;
+  if constexpr (kKind == kLambda) {
+    lambda[i] = lambda[r];
+    rho[i] = rho[r];
+  } else if constexpr (kKind == kDeltaP) {
+    const float4 t = T[r];
+    T[i] = make_float4(t.x, t.y, t.z, X[i].w);
+  } else {
+    // DeltaPPass<true>::finish with the group's final position
+    const float4 xf = npos[r];
+    const float4 x0 = xs[i];
+    npos[i] = make_float4(xf.x, xf.y, xf.z, x0.w);
+    const float4 v = make_float4((xf.x - x0.x) * c.inv_dt, (xf.y - x0.y) * c.inv_dt, (xf.z - x0.z) * c.inv_dt, 0.f);
+    vel[i] = v;
+    if (!isfinite(v.x) || !isfinite(v.y) || !isfinite(v.z)) {
+      atomicOr(&cell_flags[skeys[i]], (uint32_t)kCellVelNonFinite);
+      atomicOr(&flags[kFlagXsphExact], 1u);
+    }
+    pos[i] = x0;
+    iid[i] = iid_s[i];
+  }
+}
+
 GroupArgs group_args(const SolverScratch& s, const float4* X, const float4* V, int n) {
   GroupArgs a;
   a.X = X;
@@ -1226,20 +1367,54 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
   return cudaGetLastError();
 }
 
+namespace {
+
+// Whether the lambda / delta_p passes run on work lists (groups exist only
+// from kGroupCell particles on, and the zero gradient of co-located particles
+// needs kernel_eps > 0).
+bool use_work_list(const StepConsts& c, int n) { return n >= kGroupCell && c.keps2 > 0.f; }
+
+cudaError_t launch_work_list(const SolverScratch& s, int n, cudaStream_t stream) {
+  const int blocks = (n + kWorkThreads - 1) / kWorkThreads;
+  k_work_mark<<<blocks, kWorkThreads, 0, stream>>>(s.keys_sorted, s.cell_flags, s.grp_n, s.grp_off, s.grp_id,
+                                                   s.grp_hash, s.grp_rep, s.grp_pool, n, s.work_follow,
+                                                   s.work_blocks, s.flags);
+  k_work_list<<<blocks, kWorkThreads, 0, stream>>>(s.work_follow, s.work_blocks, n, s.work_list);
+  return cudaGetLastError();
+}
+
+template <int kKind>
+cudaError_t launch_follow(const StepConsts& c, const SolverScratch& s, const float4* X, int n, float4* T,
+                          float4* pos, float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream) {
+  k_follow<kKind><<<(n + 255) / 256, 256, 0, stream>>>(s.work_follow, n, c, X, s.lambda, s.rho, T, s.xs, s.iid_s,
+                                                       npos, vel, pos, iid, s.keys_sorted, s.cell_flags, s.flags);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
 cudaError_t launch_lambda(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                           const SolverScratch& s, int pass, cudaStream_t stream) {
   cudaError_t e = launch_groups<kGroupsPos>(c, s, X, nullptr, n, stream);
   if (e != cudaSuccess) return e;
-  return run_pass<kLambda>(base_args(c, G, X, cs, n, s, pass), stream);
+  const bool wl = use_work_list(c, n);
+  if (wl && (e = launch_work_list(s, n, stream)) != cudaSuccess) return e;
+  PassArgs a = base_args(c, G, X, cs, n, s, pass);
+  if (wl) a.list = s.work_list;
+  if ((e = run_pass<kLambda>(a, stream)) != cudaSuccess) return e;
+  return wl ? launch_follow<kLambda>(c, s, X, n, nullptr, nullptr, nullptr, nullptr, nullptr, stream) : cudaSuccess;
 }
 
 cudaError_t launch_delta_p(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                            const SolverScratch& s, int pass, float4* T, cudaStream_t stream) {
   cudaError_t e = launch_groups<kGroupsLambda>(c, s, X, nullptr, n, stream);
   if (e != cudaSuccess) return e;
+  const bool wl = use_work_list(c, n);
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.T = T;
-  return run_pass<kDeltaP>(a, stream);
+  if (wl) a.list = s.work_list;
+  if ((e = run_pass<kDeltaP>(a, stream)) != cudaSuccess) return e;
+  return wl ? launch_follow<kDeltaP>(c, s, X, n, T, nullptr, nullptr, nullptr, nullptr, stream) : cudaSuccess;
 }
 
 cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
@@ -1247,6 +1422,7 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const f
                                  float4* vel, uint32_t* iid, cudaStream_t stream) {
   cudaError_t e = launch_groups<kGroupsLambda>(c, s, X, nullptr, n, stream);
   if (e != cudaSuccess) return e;
+  const bool wl = use_work_list(c, n);
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.xs = s.xs;
   a.iid_s = s.iid_s;
@@ -1254,7 +1430,9 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const f
   a.vel = vel;
   a.pos = pos;
   a.iid = iid;
-  return run_pass<kDeltaPFinal>(a, stream);
+  if (wl) a.list = s.work_list;
+  if ((e = run_pass<kDeltaPFinal>(a, stream)) != cudaSuccess) return e;
+  return wl ? launch_follow<kDeltaPFinal>(c, s, X, n, nullptr, pos, npos, vel, iid, stream) : cudaSuccess;
 }
 
 // ---- vorticity confinement ---------------------------------------------------------------
@@ -1368,7 +1546,12 @@ int pass_launches(const StepConsts& c, int n) {
   return all ? 1 : 2;
 }
 
-// launch_groups: 1 launch before each lambda pass, 2 before each delta_p pass, 3 before xsph.
-int group_launches(int n, int niter) { return n < kGroupCell ? 0 : 3 * niter + 3; }
+// launch_groups: 1 launch before each lambda pass, 2 before each delta_p pass, 3 before xsph;
+// with work lists 2 more before each lambda pass and one follower launch after
+// each lambda and delta_p pass.
+int group_launches(const StepConsts& c, int n, int niter) {
+  if (n < kGroupCell) return 0;
+  return 3 * niter + 3 + (use_work_list(c, n) ? 4 * niter : 0);
+}
 
 }  // namespace pbf
