@@ -182,8 +182,55 @@ __device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t*
       if (y < 0 || y >= g.dims[1]) continue;
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
-      for (int j = s; j < e; ++j) p.visit(__ldg(X + j), j);
+      int j = s;
+      for (; j + 3 < e; j += 4) {  // four loads in flight
+        const float4 q0 = __ldg(X + j), q1 = __ldg(X + j + 1), q2 = __ldg(X + j + 2), q3 = __ldg(X + j + 3);
+        p.visit(q0, j);
+        p.visit(q1, j + 1);
+        p.visit(q2, j + 2);
+        p.visit(q3, j + 3);
+      }
+      for (; j < e; ++j) p.visit(__ldg(X + j), j);
     }
+  }
+}
+
+// Candidates [j0, j1) of one run, in order: with skip_misses (the pass's exact
+// rules do not need every candidate) a hit mask per chunk of 32 (four loads in
+// flight), then p.visit() on the set bits; else every candidate, four loads in
+// flight.  Same result as visiting each candidate in turn.
+template <class P>
+__device__ __forceinline__ void visit_run(const float4* __restrict__ X, int j0, int j1, P& p, bool skip_misses) {
+  if (skip_misses) {
+    for (int jb = j0; jb < j1; jb += 32) {
+      const int m = min(32, j1 - jb);
+      uint32_t mask = 0u;
+      int k = 0;
+      for (; k + 3 < m; k += 4) {
+        const float4 a = __ldg(X + jb + k), b = __ldg(X + jb + k + 1), c2 = __ldg(X + jb + k + 2),
+                     d = __ldg(X + jb + k + 3);
+        mask |= (uint32_t)p.hit(a, jb + k) << k;
+        mask |= (uint32_t)p.hit(b, jb + k + 1) << (k + 1);
+        mask |= (uint32_t)p.hit(c2, jb + k + 2) << (k + 2);
+        mask |= (uint32_t)p.hit(d, jb + k + 3) << (k + 3);
+      }
+      for (; k < m; ++k) mask |= (uint32_t)p.hit(__ldg(X + jb + k), jb + k) << k;
+      while (mask) {
+        const int b = __ffs(mask) - 1;
+        mask &= mask - 1u;
+        p.visit(__ldg(X + jb + b), jb + b);
+      }
+    }
+  } else {
+    int j = j0;
+    for (; j + 3 < j1; j += 4) {
+      const float4 q0 = __ldg(X + j), q1 = __ldg(X + j + 1), q2 = __ldg(X + j + 2), q3 = __ldg(X + j + 3);
+      p.visit(q0, j);
+      p.visit(q1, j + 1);
+      p.visit(q2, j + 2);
+      p.visit(q3, j + 3);
+    }
+    for (; j < j1; ++j) p.visit(__ldg(X + j), j);
   }
 }
 
@@ -362,11 +409,27 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
           if (ng > 0) {
             const int t0 = __ldg(a.grp_off + slot);
             const bool own = p.i >= s0 && p.i < e0;  // i is one of the cell's particles
-            for (int t = t0 + (lo - v0); t < t0 + (hi - v0); ++t)
+            int t = t0 + (lo - v0);
+            const int tend = t0 + (hi - v0);
+            constexpr int U = P::kGroupUnroll;  // groups' loads in flight (unused parts are not loaded)
+            for (; t + U - 1 < tend; t += U) {
+              float4 gp[U], gs[U], ga[U];
+              int gc[U];
+#pragma unroll
+              for (int u = 0; u < U; ++u) {
+                gp[u] = __ldg(a.grp_pos + t + u);
+                gc[u] = __ldg(a.grp_cnt + t + u);
+                gs[u] = __ldg(a.grp_sum + t + u);
+                ga[u] = __ldg(a.grp_aux + t + u);
+              }
+#pragma unroll
+              for (int u = 0; u < U; ++u) p.visit_group(gp[u], gc[u], gs[u], ga[u], own);
+            }
+            for (; t < tend; ++t)
               p.visit_group(__ldg(a.grp_pos + t), __ldg(a.grp_cnt + t), __ldg(a.grp_sum + t),
                             __ldg(a.grp_aux + t), own);
           } else {
-            for (int j = s0 + (lo - v0); j < s0 + (hi - v0); ++j) p.visit(__ldg(a.X + j), j);
+            visit_run(a.X, s0 + (lo - v0), s0 + (hi - v0), p, p.skip_misses());
           }
         }
         v0 += len;
@@ -379,6 +442,7 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
 
 struct LambdaPass {
   static constexpr int kFields = 5;
+  static constexpr int kGroupUnroll = 4;
   const StepConsts& c;
   const SceneGeom& g;
   float4 xi;
@@ -387,6 +451,8 @@ struct LambdaPass {
 
   __device__ LambdaPass(const PassArgs& a, const SceneGeom& g_, float4 xi_, int i_, bool)
       : c(a.c), g(g_), xi(xi_), i(i_) {}
+  // candidates outside the cutoff add nothing (no exact rule in this pass)
+  __device__ __forceinline__ bool skip_misses() const { return true; }
   __device__ __forceinline__ bool hit(float4 xj, int) const {
     return !(dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) >= c.h2);
   }
@@ -456,6 +522,7 @@ struct LambdaPass {
 template <bool kFinal>
 struct DeltaPPass {
   static constexpr int kFields = 4;
+  static constexpr int kGroupUnroll = 4;
   const StepConsts& c;
   const SceneGeom& g;
   const float* __restrict__ lambda;
@@ -468,6 +535,7 @@ struct DeltaPPass {
 
   __device__ DeltaPPass(const PassArgs& a, const SceneGeom& g_, float4 xi_, int i_, bool exact_)
       : c(a.c), g(g_), lambda(a.lambda), xi(xi_), i(i_), li(a.lambda[i_]), exact(exact_) {}
+  __device__ __forceinline__ bool skip_misses() const { return !exact; }
   __device__ __forceinline__ bool hit(float4 xj, int j) const {
     const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
     return !(r2 >= c.h2) && !(r2 < c.keps2) && j != i;
@@ -554,6 +622,7 @@ struct DeltaPPass {
 // reference's NaN from 0 * v / (rho_i + rho_j) outside the cutoff.
 struct XsphPass {
   static constexpr int kFields = 6;
+  static constexpr int kGroupUnroll = 2;
   const StepConsts& c;
   const float4* __restrict__ V;
   const float* __restrict__ rho;
@@ -566,6 +635,7 @@ struct XsphPass {
 
   __device__ XsphPass(const PassArgs& a, const SceneGeom&, float4 xi_, int i_, bool exact_)
       : c(a.c), V(a.V), rho(a.rho), xi(xi_), vi(a.V[i_]), ri(a.rho[i_]), i(i_), exact(exact_) {}
+  __device__ __forceinline__ bool skip_misses() const { return !exact; }
   __device__ __forceinline__ bool hit(float4 xj, int) const {
     return !(dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) >= c.h2);
   }
@@ -654,12 +724,8 @@ __device__ __forceinline__ bool exact_path(int kind, const PassArgs& a, const Sc
 // ---- kernels ------------------------------------------------------------------------
 
 template <int kKind>
-__global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
+__device__ __forceinline__ void sparse_slot(const PassArgs& a, int t, int count) {
   using P = typename PassOf<kKind>::type;
-  if (a.dense_all) return;
-  const int count = work_count(a);
-  if ((int)(blockIdx.x * blockDim.x) >= count) return;  // the whole block is past the list
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const bool valid = t < count;
   const int i = valid ? work_particle(a, t) : 0;
   const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -690,6 +756,17 @@ __global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
     visit_window_masked(g, a.cs, a.n, q, a.X, p, nullptr, 0, i);
   }
   p.finish(a);
+}
+
+// Thread slots of the work list (or of all particles) in chunks of
+// kSparseThreads, grid-stride: the grid is sized for the SMs, not for the
+// list, whose length the host does not know.
+template <int kKind>
+__global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
+  if (a.dense_all) return;
+  const int count = work_count(a);
+  for (int t0 = blockIdx.x * kSparseThreads; t0 < count; t0 += gridDim.x * kSparseThreads)
+    sparse_slot<kKind>(a, t0 + threadIdx.x, count);
 }
 
 template <int kKind>
@@ -1348,8 +1425,11 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
 
 template <int kKind>
 cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
-  if (!a.dense_all)  // else the sparse kernel has nothing to do
-    k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, 0, stream>>>(a);
+  if (!a.dense_all) {  // else the sparse kernel has nothing to do
+    // 4 x the dense grid (16 blocks per SM): about two waves of resident blocks
+    const int grid = min((a.n + kSparseThreads - 1) / kSparseThreads, 4 * a.c.dense_grid);
+    k_sparse<kKind><<<grid, kSparseThreads, 0, stream>>>(a);
+  }
   k_dense<kKind><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
