@@ -261,7 +261,8 @@ enum StepFlag {
   kGroupItems = 6,           // group work items (set by reorder)
   kWorkCount = 7,            // particles on the current iteration's work list
   kWorkDone = 8,             // blocks of the work-list count finished (0 between uses)
-  kNumFlags = 9
+  kWorkIdentity = 9,         // 1: no grouped cell this step, the passes take every particle in order
+  kNumFlags = 10
 };
 
 // Entries of the dense list: one per warp of 32 consecutive particles.

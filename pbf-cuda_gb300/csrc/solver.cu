@@ -102,7 +102,9 @@ struct PassArgs {
 __device__ __forceinline__ int work_count(const PassArgs& a) {
   return a.list ? (int)a.flags[kWorkCount] : a.n;
 }
-__device__ __forceinline__ int work_particle(const PassArgs& a, int t) { return a.list ? __ldg(a.list + t) : t; }
+__device__ __forceinline__ int work_particle(const PassArgs& a, int t) {
+  return a.list && !a.flags[kWorkIdentity] ? __ldg(a.list + t) : t;
+}
 
 // ---- windows ------------------------------------------------------------------------
 
@@ -182,15 +184,7 @@ __device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t*
       if (y < 0 || y >= g.dims[1]) continue;
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
-      int j = s;
-      for (; j + 3 < e; j += 4) {  // four loads in flight
-        const float4 q0 = __ldg(X + j), q1 = __ldg(X + j + 1), q2 = __ldg(X + j + 2), q3 = __ldg(X + j + 3);
-        p.visit(q0, j);
-        p.visit(q1, j + 1);
-        p.visit(q2, j + 2);
-        p.visit(q3, j + 3);
-      }
-      for (; j < e; ++j) p.visit(__ldg(X + j), j);
+      for (int j = s; j < e; ++j) p.visit(__ldg(X + j), j);
     }
   }
 }
@@ -442,7 +436,7 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
 
 struct LambdaPass {
   static constexpr int kFields = 5;
-  static constexpr int kGroupUnroll = 4;
+  static constexpr int kGroupUnroll = 2;
   const StepConsts& c;
   const SceneGeom& g;
   float4 xi;
@@ -522,7 +516,7 @@ struct LambdaPass {
 template <bool kFinal>
 struct DeltaPPass {
   static constexpr int kFields = 4;
-  static constexpr int kGroupUnroll = 4;
+  static constexpr int kGroupUnroll = 2;
   const StepConsts& c;
   const SceneGeom& g;
   const float* __restrict__ lambda;
@@ -758,15 +752,22 @@ __device__ __forceinline__ void sparse_slot(const PassArgs& a, int t, int count)
   p.finish(a);
 }
 
-// Thread slots of the work list (or of all particles) in chunks of
-// kSparseThreads, grid-stride: the grid is sized for the SMs, not for the
-// list, whose length the host does not know.
+// One thread slot of the work list (or of all particles) per thread; the
+// grid covers every particle, blocks past the list's end return at once.
+// PBF_SPARSE_MIN_BLOCKS (a build-time tuning macro): resident blocks per SM the
+// compiler must allow for, which caps the sparse kernels' registers.
+#ifdef PBF_SPARSE_MIN_BLOCKS
+#define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads, PBF_SPARSE_MIN_BLOCKS)
+#else
+#define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads)
+#endif
+
 template <int kKind>
-__global__ void __launch_bounds__(kSparseThreads) k_sparse(PassArgs a) {
+__global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   if (a.dense_all) return;
   const int count = work_count(a);
-  for (int t0 = blockIdx.x * kSparseThreads; t0 < count; t0 += gridDim.x * kSparseThreads)
-    sparse_slot<kKind>(a, t0 + threadIdx.x, count);
+  if ((int)(blockIdx.x * kSparseThreads) >= count) return;
+  sparse_slot<kKind>(a, blockIdx.x * kSparseThreads + threadIdx.x, count);
 }
 
 template <int kKind>
@@ -1263,6 +1264,13 @@ k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cel
             int* __restrict__ follow, int* __restrict__ blocks, uint32_t* __restrict__ flags) {
   __shared__ int sh[80];
   __shared__ int s_last;
+  if (flags[kGroupCount] == 0u) {  // no grouped cell this step: every particle computes, in order
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      flags[kWorkCount] = (uint32_t)n;
+      flags[kWorkIdentity] = 1u;
+    }
+    return;
+  }
   const int i = blockIdx.x * kWorkThreads + threadIdx.x;
   int r = -1;
   if (i < n) {
@@ -1305,8 +1313,10 @@ k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cel
 
 // list[blocks[b] + rank] = i for the computing particles of block b, in order.
 __global__ void __launch_bounds__(kWorkThreads)
-k_work_list(const int* __restrict__ follow, const int* __restrict__ blocks, int n, int* __restrict__ list) {
+k_work_list(const int* __restrict__ follow, const int* __restrict__ blocks, int n, int* __restrict__ list,
+            const uint32_t* __restrict__ flags) {
   __shared__ int sh[80];
+  if (flags[kWorkIdentity]) return;
   const int i = blockIdx.x * kWorkThreads + threadIdx.x;
   const bool keep = i < n && follow[i] < 0;
   int total;
@@ -1323,7 +1333,7 @@ k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __re
          float4* __restrict__ pos, uint32_t* __restrict__ iid, const uint32_t* __restrict__ skeys,
          uint32_t* __restrict__ cell_flags, uint32_t* __restrict__ flags) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  if (i >= n || flags[kWorkIdentity]) return;
   const int r = follow[i];
   if (r < 0) return;
   if constexpr (kKind == kLambda) {
@@ -1425,11 +1435,8 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
 
 template <int kKind>
 cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
-  if (!a.dense_all) {  // else the sparse kernel has nothing to do
-    // 4 x the dense grid (16 blocks per SM): about two waves of resident blocks
-    const int grid = min((a.n + kSparseThreads - 1) / kSparseThreads, 4 * a.c.dense_grid);
-    k_sparse<kKind><<<grid, kSparseThreads, 0, stream>>>(a);
-  }
+  if (!a.dense_all)  // else the sparse kernel has nothing to do
+    k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, 0, stream>>>(a);
   k_dense<kKind><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
@@ -1459,7 +1466,7 @@ cudaError_t launch_work_list(const SolverScratch& s, int n, cudaStream_t stream)
   k_work_mark<<<blocks, kWorkThreads, 0, stream>>>(s.keys_sorted, s.cell_flags, s.grp_n, s.grp_off, s.grp_id,
                                                    s.grp_hash, s.grp_rep, s.grp_pool, n, s.work_follow,
                                                    s.work_blocks, s.flags);
-  k_work_list<<<blocks, kWorkThreads, 0, stream>>>(s.work_follow, s.work_blocks, n, s.work_list);
+  k_work_list<<<blocks, kWorkThreads, 0, stream>>>(s.work_follow, s.work_blocks, n, s.work_list, s.flags);
   return cudaGetLastError();
 }
 
