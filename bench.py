@@ -332,7 +332,11 @@ def run_ours(args):
 
 
 def tune(sim, st, n, args):
-    """pbf_autotune on the current state (unless --no-tune); returns the choice."""
+    """pbf_autotune on the current state (unless --no-tune or --dense-window);
+    returns the choice."""
+    if args.dense_window:
+        sim.set_tuning(args.dense_window, 0)
+        return {"dense_window": args.dense_window, "dense_all": 0, "set": "--dense-window"}
     if not args.tune:
         return None
     t = sim.autotune(st.pos, st.vel, st.iid, n, steps=3)
@@ -710,6 +714,8 @@ def main(argv=None):
                     help="scene: the dam-break parameter set; reference: the reference's own defaults")
     ap.add_argument("--no-tune", dest="tune", action="store_false",
                     help="keep the default dense-kernel choice instead of pbf_autotune after the warm-up")
+    ap.add_argument("--dense-window", type=int, default=0,
+                    help="set this dense-kernel window after the warm-up instead of tuning (no trial steps)")
     ap.add_argument("--e2e-steps", type=int, default=None,
                     help="steps of the end-to-end measurement (default: the timed steps, from the same state)")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
