@@ -266,7 +266,7 @@ pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
  * One step, same contract and results as pbf_step, for callers that cannot
  * allocate device memory (no pbf_solver, so no pbf_create).  It has no
  * counterpart in the reference.  It calls no cudaMalloc or cudaFree: its
- * scratch is a fixed array of about 10.2 MB inside this library's device image,
+ * scratch is a fixed array of about 10.5 MB inside this library's device image,
  * held by every GPU that loads the library until the process exits.
  * Limits: n <= 32768 particles and a box of at most 131072 cells at cell size
  * h; larger calls return PBF_ERR_CAPACITY.  The first call on each device

@@ -9,7 +9,7 @@
 // pbf_create allocates the solver's scratch.
 //
 // How: the scratch lives in one file-scope __device__ array of fixed size,
-// kNoAllocScratchBytes (about 10.2 MB), which is part of this library's device
+// kNoAllocScratchBytes (about 10.5 MB), which is part of this library's device
 // image: every GPU that loads the library holds it until the process exits.
 // It bounds the problem to kNoAllocMaxParticles particles and
 // kNoAllocMaxCells grid cells; larger calls are rejected with

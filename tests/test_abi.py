@@ -91,6 +91,9 @@ def test_argument_errors_need_no_gpu(pbf):
     assert L.pbf_step(None, None, None, None, None, None, 1, None) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_set_params(None, ctypes.byref(p)) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_destroy(None) == pbf.PBF_OK
+    t = pbf.PbfTuning()
+    assert L.pbf_set_tuning(None, ctypes.byref(t)) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_get_tuning(None, ctypes.byref(t)) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_abi_version() == 2
     assert L.pbf_status_string(pbf.PBF_ERR_CAPACITY) == b"capacity exceeded"
     with pytest.raises(pbf.PbfError) as e:

@@ -63,3 +63,34 @@ def test_autotune_batch(pbf, oracle, cuda):
         np.testing.assert_array_equal(iid[off:off + k] - off, r["iid"])
         assert np.abs(got[off:off + k, :3] - r["npos"][:, :3]).max() <= TOL_X
         off += k
+
+
+def test_set_tuning_round_trip(pbf, oracle, cuda):
+    """pbf_set_tuning / pbf_get_tuning: the choice reads back, 0 / -1 restore the
+    defaults, out-of-range values are refused, and a step at a set window still
+    matches the FP64 oracle."""
+    import torch
+
+    sc = pbf.scenes.dam_break(seed=6)
+    p = ref_params(pbf, 3)
+    n = sc.n
+    pos = torch.from_numpy(sc.pos).cuda()
+    vel = torch.zeros_like(pos)
+    iid = torch.arange(n, dtype=torch.int32, device="cuda")
+    with pbf.Simulator(p, sc.ulim, sc.llim, n) as sim:
+        assert sim.tuning() == {"dense_window": 512, "dense_all": -1}
+        sim.set_tuning(128, 0)
+        assert sim.tuning() == {"dense_window": 128, "dense_all": 0}
+        for bad in ((16, 0), (256, 2), (256, -2)):
+            with pytest.raises(pbf.PbfError):
+                sim.set_tuning(*bad)
+        assert sim.tuning() == {"dense_window": 128, "dense_all": 0}
+        npos, nvel = torch.empty_like(pos), torch.empty_like(vel)
+        sim.step(pos, npos, vel, nvel, iid, n)
+        torch.cuda.synchronize()
+        sim.set_tuning(0, -1)
+        assert sim.tuning() == {"dense_window": 512, "dense_all": -1}
+    r = oracle.step(p, sc.ulim, sc.llim, sc.pos.astype(np.float64), np.zeros((n, 4)), np.arange(n, dtype=np.uint32),
+                    "f64")
+    np.testing.assert_array_equal(iid.cpu().numpy().astype(np.uint32), r["iid"])
+    assert np.abs(npos.cpu().numpy()[:, :3] - r["npos"][:, :3]).max() <= TOL_X
