@@ -128,3 +128,19 @@ def test_cpp_facade_compiles(tmp_path):
         }}
     """))
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", str(src)], check=True)
+
+
+def test_cpp_ssf_facade_compiles(tmp_path):
+    """The C++ SSFRenderer facade compiles against the C ABI (no GPU call made)."""
+    src = tmp_path / "ssf_facade.cpp"
+    src.write_text(textwrap.dedent(f"""
+        #include "{ROOT / 'pbf-cuda_gb300' / 'csrc' / 'SSFRenderer.hpp'}"
+        int use(pbf::SSFRenderer& r, const void* pos, void* color) {{
+          pbf_ssf_params p = pbf::SSFRenderer::defaults(320, 240);
+          r.loadParams(p);
+          r.render(pos, 10, color);
+          r.setSky(nullptr, 0);
+          return r.params().width;
+        }}
+    """))
+    subprocess.run(["g++", "-std=c++17", "-fsyntax-only", str(src)], check=True)
