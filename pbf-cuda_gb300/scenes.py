@@ -17,6 +17,10 @@ iids for a box) with seeded numpy jitter and y up:
   inverse       15,625 particles: 25x25x25 lattice (spacing 0.04) in a 2.0 x 1.0 x 1.0 box
   clustered     1,048,576 particles: a 64^3 lattice plus six collapsed clusters
                 in the large sweep's box (the grouped-cell profiling case)
+  reference_double_dam / reference_fixed_cube
+                the reference application's own sources, bit for bit: the same
+                C-runtime generator seeded 27, the same float arithmetic and
+                jitter quirk, z up, the reference's default parameters
 
 Lattice spacing d = 0.05, jitter uniform +-0.005 per coordinate, velocities 0.
 save_state / load_state keep a particle state (float4 positions, float4
@@ -127,6 +131,100 @@ def double_dam(seed: int = 0, niter: int = 4) -> Scene:
     pos = np.concatenate([a, b])
     return Scene("double_dam_32k", pos, _zeros_like(pos), (3.2, 1.6, 1.6), (0.0, 0.0, 0.0),
                  params=scene_params(niter))
+
+
+# ---- the reference application's own sources -------------------------------------------
+
+
+class MsvcRand:
+    """The C runtime rand() the reference application draws its jitter from
+    (a Windows / Visual Studio build, fluids/fluids.vcxproj): the published
+    linear congruential generator of the Microsoft C runtime, state = state *
+    214013 + 2531011 (mod 2^32), rand() = bits 16..30 of the state, RAND_MAX =
+    32767; srand(seed) sets the state."""
+
+    RAND_MAX = 32767
+
+    def __init__(self, seed: int = 1):
+        self.state = seed & 0xFFFFFFFF
+
+    def rand(self) -> int:
+        self.state = (self.state * 214013 + 2531011) & 0xFFFFFFFF
+        return (self.state >> 16) & 0x7FFF
+
+
+def _reference_cube(llim, d, ns, rng: MsvcRand, out: list) -> None:
+    """generate_cube / FixedCubeSource::initialize (fluids/DoubleDamSource.cpp:5-21,
+    fluids/FixedCubeSource.cpp:6-26) in float32 and the same order: x, y, z start
+    at llim + d / 2 and step by d (accumulated), x slowest; each particle gets
+    0.1 (sx r1, sy r2, sz r3) added, r = 1.f * rand() / RAND_MAX, the jitter
+    scaled by the start coordinate s (the reference's quirk)."""
+    f = np.float32
+    sx, sy, sz = (f(llim[a]) + f(d[a]) / f(2) for a in range(3))
+    x = sx
+    for _ in range(ns[0]):
+        y = sy
+        for _ in range(ns[1]):
+            z = sz
+            for _ in range(ns[2]):
+                r1 = f(1.0) * f(rng.rand()) / f(MsvcRand.RAND_MAX)
+                r2 = f(1.0) * f(rng.rand()) / f(MsvcRand.RAND_MAX)
+                r3 = f(1.0) * f(rng.rand()) / f(MsvcRand.RAND_MAX)
+                out.append((x + f(0.1) * (sx * r1), y + f(0.1) * (sy * r2), z + f(0.1) * (sz * r3)))
+                z = z + f(d[2])
+            y = y + f(d[1])
+        x = x + f(d[0])
+
+
+def _reference_spacing(ulim, llim, ns):
+    """m_d = (ulim - llim) / ns per axis in float32 (fluids/DoubleDamSource.h:11-21)."""
+    f = np.float32
+    return [(f(ulim[a]) - f(llim[a])) / f(ns[a]) for a in range(3)]
+
+
+def reference_double_dam() -> Scene:
+    """The reference application's default scene (fluids/FluidSystem.cpp:34-61):
+    DoubleDamSource of two 20 x 20 x 40 cubes (32,000 particles, srand(27)) in the
+    box [-2, 2] x [-2, 2] x [0, 4], z up, the reference's default solver
+    parameters (dt 0.0083, one step per frame).  Its second cube is generated
+    with the first cube's ulim (fluids/DoubleDamSource.cpp:31), which
+    generate_cube does not use.  The reference's boundary sweep, when switched
+    on, is driver.Sweep((2, 0, 0), (0, 0, 0), w=0.05) (fluids/FluidSystem.cpp:36-38)."""
+    f = np.float32
+    dd = f(1.0) / f(20)
+    d1, d2, d3 = dd * f(20), dd * f(20), dd * f(40)
+    ulim1 = (f(-1.8), f(1.8), f(3.8))
+    llim1 = (f(-1.8) + d1, f(1.8) - d2, f(3.8) - d3)
+    ulim2 = (f(1.8) - d1, f(-1.8) + d2, f(3.8))
+    llim2 = (f(1.8), f(-1.8), f(3.8) - d3)
+    ns = (20, 20, 40)
+    rng = MsvcRand(27)
+    pts: list = []
+    _reference_cube(llim1, _reference_spacing(ulim1, llim1, ns), ns, rng, pts)
+    _reference_cube(llim2, _reference_spacing(ulim2, llim2, ns), ns, rng, pts)
+    pos = np.zeros((len(pts), 4), np.float32)
+    pos[:, :3] = np.asarray(pts, np.float32)
+    return Scene("reference_double_dam_32k", pos, _zeros_like(pos), (2.0, 2.0, 4.0), (-2.0, -2.0, 0.0),
+                 params=default_params())
+
+
+def reference_fixed_cube() -> Scene:
+    """The reference's single-cube alternative (commented out in
+    fluids/FluidSystem.cpp:47-52): FixedCubeSource of 30 x 30 x 30 particles
+    below (1.8, 1.8, 3.8), srand(27), the same box and parameters as
+    reference_double_dam."""
+    f = np.float32
+    dd = f(1.0) / f(20)
+    d1 = d2 = d3 = dd * f(30)
+    ulim = (f(1.8), f(1.8), f(3.8))
+    llim = (f(1.8) - d1, f(1.8) - d2, f(3.8) - d3)
+    ns = (30, 30, 30)
+    pts: list = []
+    _reference_cube(llim, _reference_spacing(ulim, llim, ns), ns, MsvcRand(27), pts)
+    pos = np.zeros((len(pts), 4), np.float32)
+    pos[:, :3] = np.asarray(pts, np.float32)
+    return Scene("reference_fixed_cube_27k", pos, _zeros_like(pos), (2.0, 2.0, 4.0), (-2.0, -2.0, 0.0),
+                 params=default_params())
 
 
 def sweep_wall_x(t: float) -> float:

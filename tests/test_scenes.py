@@ -93,3 +93,46 @@ def test_state_file_round_trip(pbf, tmp_path):
     path.write_bytes(path.read_bytes()[:-4])
     with pytest.raises(ValueError):
         s.load_state(path)
+
+
+def test_msvc_rand_known_answers(pbf):
+    """The Microsoft C runtime's rand(): the first values after the default seed 1."""
+    r = pbf.scenes.MsvcRand(1)
+    assert [r.rand() for _ in range(10)] == [41, 18467, 6334, 26500, 19169, 15724, 11478, 29358, 26962, 24464]
+
+
+def test_reference_double_dam_layout(pbf):
+    """fluids/FluidSystem.cpp:55-61, fluids/DoubleDamSource.cpp:5-31: 2 x 20 x 20 x 40
+    particles, the first at (llim + d/2) + 0.1 (s r1, s r2, s r3) with the first
+    three draws after srand(27), the cubes' x steps negative (ulim.x < llim.x
+    for the first cube, as the reference writes it), all inside the box."""
+    sc = pbf.scenes.reference_double_dam()
+    assert sc.n == 32000 and sc.ulim == (2.0, 2.0, 4.0) and sc.llim == (-2.0, -2.0, 0.0)
+    assert list(sc.params.up) == [0.0, 0.0, 1.0] and sc.params.niter == 4
+    f = np.float32
+    r = pbf.scenes.MsvcRand(27)
+    r1, r2, r3 = (f(1.0) * f(r.rand()) / f(32767) for _ in range(3))
+    d = (f(-1.8) - (f(-1.8) + f(1.0) / f(20) * f(20))) / f(20)
+    sx = (f(-1.8) + f(1.0) / f(20) * f(20)) + d / f(2)
+    assert sc.pos[0, 0] == sx + f(0.1) * (sx * r1)
+    assert np.all(sc.pos[:, :3] > np.array(sc.llim, np.float32)) and np.all(sc.pos[:, :3] < np.array(sc.ulim, np.float32))
+    # first cube in x < 0, y > 0; second in x > 0, y < 0
+    assert np.all(sc.pos[:16000, 0] < 0) and np.all(sc.pos[:16000, 1] > 0)
+    assert np.all(sc.pos[16000:, 0] > 0) and np.all(sc.pos[16000:, 1] < 0)
+    # the reference's jitter quirk: scaled by the start coordinate, up to 0.1 * sz = 0.1825 in z
+    assert sc.pos[:, 2].max() > 3.9
+    fc = pbf.scenes.reference_fixed_cube()
+    assert fc.n == 27000 and np.all(fc.pos[:, :3] < np.array(fc.ulim, np.float32) + 0.2)
+
+
+def test_reference_double_dam_oracle_step(pbf, oracle):
+    """One step of the reference's own scene with its own parameters: the float
+    port and the FP64 oracle give the same cell order; the heavily overlapping
+    start (jitter up to 3.6 spacings in z) makes the step ill-conditioned, so
+    positions agree to ~1e-3 h, not 1e-5 h."""
+    sc = pbf.scenes.reference_double_dam()
+    iid = np.arange(sc.n, dtype=np.uint32)
+    r32 = oracle.step(sc.params, sc.ulim, sc.llim, sc.pos, sc.vel, iid, "f32")
+    r64 = oracle.step(sc.params, sc.ulim, sc.llim, sc.pos.astype(np.float64), sc.vel.astype(np.float64), iid, "f64")
+    np.testing.assert_array_equal(r32["iid"], r64["iid"])
+    assert np.abs(r32["npos"][:, :3] - r64["npos"][:, :3]).max() < 1e-3
