@@ -108,3 +108,15 @@ class SceneDriver:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def fluid_system(moving: bool = False, dump_dir=None, render_dir=None, renderer=None) -> SceneDriver:
+    """FluidSystem() (fluids/FluidSystem.cpp:8-85) without a window: the
+    reference's DoubleDamSource scene with its default parameters, one step
+    per frame (stepSimulate calls Simulator::step once, dt = 0.0083), and,
+    when `moving`, its boundary sweep ulim + (2, 0, 0) sin(0.05 frame)
+    (fluids/FluidSystem.cpp:36-38, 104-110).  The scene is z up, the
+    renderer's world, so rendered frames need no axis change."""
+    sweep = Sweep((2.0, 0.0, 0.0), (0.0, 0.0, 0.0), w=0.05) if moving else None
+    return SceneDriver(_scenes.reference_double_dam(), substeps=1, sweep=sweep, dump_dir=dump_dir,
+                       render_dir=render_dir, renderer=renderer, y_up=False)
