@@ -229,3 +229,18 @@ def test_float_and_fp64_oracles_agree_away_from_rims(pbf, oracle):
     assert np.abs(a["depth_raw"][both] - b["depth_raw"][both]).max() < 2e-6 * 6
     # a rim fragment (pho within a few ulp of 1) adds 2 r sqrt(1 - pho) <= ~5e-5 on one side only
     assert np.abs(a["thick"] - b["thick"]).max() < 1e-5 * b["thick"].max() + 1e-4
+
+
+def test_write_ppm_orientation_and_background(pbf, tmp_path):
+    """Row 0 of an image is its bottom row (GL window coordinates): the file
+    starts with the top row; pixels with alpha 0 take the background colour."""
+    img = np.zeros((2, 3, 4), np.float32)
+    img[0, :, :] = (1.0, 0.0, 0.0, 1.0)   # bottom row red
+    img[1, 0, :] = (0.0, 0.0, 1.0, 1.0)   # top-left blue, rest of the top row background
+    path = pbf.ssf.write_ppm(tmp_path / "x.ppm", img, background=(0.0, 1.0, 0.0))
+    data = path.read_bytes()
+    header = b"P6 3 2 255\n"
+    assert data.startswith(header)
+    px = np.frombuffer(data[len(header):], np.uint8).reshape(2, 3, 3)
+    assert px[0, 0].tolist() == [0, 0, 255] and px[0, 1].tolist() == [0, 255, 0]
+    assert (px[1] == [255, 0, 0]).all()
