@@ -359,3 +359,80 @@ def ssf_shade(params, depth, normal_D, thick, color, sky=None, prec: str = "f32"
     if rc != 0:
         raise ValueError("oracle_ssf_shade rejected its arguments")
     return out
+
+
+# ---- the reference's own SSF shaders on the CPU (oracle/ref_harness/ssf_ref.cpp) ----------
+
+_ssf_ref = None
+
+
+def ssf_ref_available() -> bool:
+    """Whether the reference's shaders can be built here (its sources are present)."""
+    from .ref_harness import build_ref
+
+    return build_ref.ssf_shaders_present() or build_ref.ssf_ref_path().exists()
+
+
+def _ssf_ref_lib():
+    global _ssf_ref
+    with _lock:
+        if _ssf_ref is None:
+            from .ref_harness import build_ref
+
+            path = build_ref.build_ssf_ref() if build_ref.ssf_shaders_present() else build_ref.ssf_ref_path()
+            L = ctypes.CDLL(str(path))
+            f32p = ctypes.POINTER(ctypes.c_float)
+            P = ctypes.POINTER(OracleSsfParams)
+            L.ssf_ref_splat.argtypes = [P, f32p, ctypes.c_int, f32p, f32p]
+            L.ssf_ref_splat.restype = ctypes.c_longlong
+            L.ssf_ref_smooth.argtypes = [P, f32p, f32p]
+            L.ssf_ref_normals.argtypes = [P, f32p, f32p]
+            L.ssf_ref_shade.argtypes = [P, f32p, f32p, f32p, f32p, ctypes.c_int, f32p]
+            for fn in (L.ssf_ref_smooth, L.ssf_ref_normals, L.ssf_ref_shade):
+                fn.restype = ctypes.c_int
+            _ssf_ref = L
+    return _ssf_ref
+
+
+def ssf_ref_splat(params, pos):
+    """renderDepth + renderThick run through the reference's shaders: (depth,
+    thick, fragments)."""
+    op = to_oracle_ssf_params(params)
+    pos = np.ascontiguousarray(pos, dtype=np.float32)
+    depth = np.zeros((op.height, op.width), np.float32)
+    thick = np.zeros_like(depth)
+    n = pos.shape[0]
+    f = _ssf_ref_lib().ssf_ref_splat(ctypes.byref(op), _ptr(pos, ctypes.c_float) if n else None, n,
+                                     _ptr(depth, ctypes.c_float), _ptr(thick, ctypes.c_float))
+    return depth, thick, int(f)
+
+
+def ssf_ref_smooth(params, raw):
+    op = to_oracle_ssf_params(params)
+    raw = np.ascontiguousarray(raw, dtype=np.float32)
+    out = np.zeros_like(raw)
+    _ssf_ref_lib().ssf_ref_smooth(ctypes.byref(op), _ptr(raw, ctypes.c_float), _ptr(out, ctypes.c_float))
+    return out
+
+
+def ssf_ref_normals(params, depth):
+    op = to_oracle_ssf_params(params)
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    out = np.zeros(depth.shape + (4,), np.float32)
+    _ssf_ref_lib().ssf_ref_normals(ctypes.byref(op), _ptr(depth, ctypes.c_float), _ptr(out, ctypes.c_float))
+    return out
+
+
+def ssf_ref_shade(params, depth, normal_D, thick, color, sky=None):
+    op = to_oracle_ssf_params(params)
+    depth = np.ascontiguousarray(depth, dtype=np.float32)
+    nd = np.ascontiguousarray(normal_D, dtype=np.float32)
+    th = np.ascontiguousarray(thick, dtype=np.float32)
+    out = np.ascontiguousarray(color, dtype=np.float32).copy()
+    sk = None if sky is None else np.ascontiguousarray(sky, dtype=np.float32)
+    rc = _ssf_ref_lib().ssf_ref_shade(ctypes.byref(op), _ptr(depth, ctypes.c_float), _ptr(nd, ctypes.c_float),
+                                      _ptr(th, ctypes.c_float), _ptr(sk, ctypes.c_float) if sk is not None else None,
+                                      0 if sk is None else sk.shape[1], _ptr(out, ctypes.c_float))
+    if rc != 0:
+        raise ValueError("ssf_ref_shade rejected its arguments")
+    return out

@@ -22,14 +22,20 @@
  *   previous stage's image as input, so each stage is checked on the GPU's own
  *   input (tests/test_gpu_ssf.py).
  *
- * Parity unpinned against the reference itself: its renderer is OpenGL and no
- * graphics stack exists here, so no reference output can be produced.  The
- * restatement follows the shader source line by line (cited per stage), and
- * fixes the GL implementation details the same way include/pbf_ssf.h states
- * them (exact depth minimum, fixed-point thickness, half-open sprite squares,
- * GL point clipping, 0 outside the image in smoothing, wrap-around in normal
- * restoration, shading only where the depth is below the far plane).
- * Known answers pin the rest (tests/test_ssf_oracle.py).
+ * Parity pinned against the reference's own shader code: its renderer is
+ * OpenGL and no graphics stack exists here, but its SSF shaders
+ * (fluids/shader/SSF*.glsl) are plain arithmetic, and oracle/ref_harness
+ * compiles them as C++ and runs them on the CPU with the fixed-function steps
+ * made explicit (ssf_ref.cpp).  Their outputs, recorded in
+ * tests/golden/ssf_ref_*.npz by tests/golden/make_ssf_golden.py, agree with
+ * this restatement stage by stage (tests/test_ssf_ref.py: the same fragments
+ * and pixels, splat depth within 1e-6 relative, smoothing and normals
+ * bit-identical here, shading within 1e-5).  GL implementation details are
+ * fixed the way include/pbf_ssf.h states them (exact depth minimum,
+ * fixed-point thickness, half-open sprite squares, GL point clipping, 0
+ * outside the image in smoothing, wrap-around in normal restoration, shading
+ * only where the depth is below the far plane).  Known answers check the
+ * formulas besides (tests/test_ssf_oracle.py).
  *
  * Images: row-major W x H, row 0 at the bottom; depth/thickness 1 float per
  * pixel, normal_D and colour 4.  Particles: stride-4 float (x, y, z, w).
