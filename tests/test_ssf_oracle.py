@@ -244,3 +244,16 @@ def test_write_ppm_orientation_and_background(pbf, tmp_path):
     px = np.frombuffer(data[len(header):], np.uint8).reshape(2, 3, 3)
     assert px[0, 0].tolist() == [0, 0, 255] and px[0, 1].tolist() == [0, 255, 0]
     assert (px[1] == [255, 0, 0]).all()
+
+
+def test_look_at_refuses_degenerate_cameras(pbf):
+    """Camera(pos, focus, aspect) builds up = front x ((0, 0, 1) x front): a
+    camera looking along the world's up axis, or at its own position, has no
+    up direction (the reference would produce NaNs); pbf_ssf_look_at refuses."""
+    L = pbf.lib()
+    p = pbf.ssf_default_params(64, 48)
+    f3 = lambda *v: (ctypes.c_float * 3)(*v)
+    assert L.pbf_ssf_look_at(ctypes.byref(p), f3(0, 0, 5), f3(0, 0, 0), 60.0) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_ssf_look_at(ctypes.byref(p), f3(1, 1, 1), f3(1, 1, 1), 60.0) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_ssf_look_at(ctypes.byref(p), f3(1, -5, 2), f3(0, 0, 1.5), 0.0) == pbf.PBF_ERR_INVALID_ARG
+    assert L.pbf_ssf_look_at(ctypes.byref(p), f3(1, -5, 2), f3(0, 0, 1.5), 60.0) == pbf.PBF_OK
