@@ -30,6 +30,15 @@
 // fixed, so results stay deterministic; they differ from the reference's
 // sequential sums only by rounding.
 //
+// Particles piled onto one position (a grouped cell's position group) have
+// bitwise the same window, position and, within a step, lambda: their lambda
+// and delta_p results are equal.  When a step has grouped cells, each lambda
+// pass first builds a work list (k_work_mark, k_work_list: one particle per
+// position group plus every particle outside the groups, in cell order), the
+// two passes run on that list, and k_follow copies each group's results to
+// its other members.  With no grouped cell the list is the identity and those
+// kernels return at once.
+//
 // IEEE semantics follow the reference's: its kernels evaluate every
 // candidate of the window, so a NaN distance (from a NaN position) poisons
 // the sums, a non-finite lambda_j poisons delta_p through a zero gradient,
