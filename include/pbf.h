@@ -30,6 +30,12 @@ extern "C" {
 
 #define PBF_ABI_VERSION 2
 
+/* Largest max_particles of a solver, and largest total of a batch: 2^27.
+ * The solver's per-particle tables are indexed with 32-bit integers, the
+ * largest holding 16 words per particle.  At the limit a solver holds about
+ * 37 GB of scratch (~272 B per particle) besides the caller's buffers. */
+#define PBF_MAX_PARTICLES 134217728
+
 typedef enum pbf_status {
   PBF_OK = 0,
   PBF_ERR_INVALID_ARG = 1, /* null pointer, n < 0, aliasing buffers, bad params */
@@ -81,6 +87,8 @@ int pbf_abi_version(void);
  * particles and for a cell grid of 4x the cells of [llim, ulim] at cell size
  * h (the reference allocates 4 * prod((ulim - llim) / 0.1) cells,
  * fluids/Simulator.h:13-14).  Must be called with the target device current.
+ * max_particles in [0, PBF_MAX_PARTICLES], else PBF_ERR_INVALID_ARG (< 0) or
+ * PBF_ERR_CAPACITY (above the limit), before any CUDA call.
  */
 pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float llim[3],
                       int max_particles, pbf_solver** out);
@@ -217,8 +225,9 @@ pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], 
  */
 typedef struct pbf_batch pbf_batch;
 
-/* ulim/llim: 3 * nscenes floats; counts: nscenes particle counts.  Reserves
- * 4x the cells of the initial boxes, like pbf_create. */
+/* ulim/llim: 3 * nscenes floats; counts: nscenes particle counts, summing to
+ * at most PBF_MAX_PARTICLES (else PBF_ERR_CAPACITY).  Reserves 4x the cells
+ * of the initial boxes, like pbf_create. */
 pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* ulim, const float* llim,
                             const int* counts, pbf_batch** out);
 pbf_status pbf_batch_destroy(pbf_batch* b);

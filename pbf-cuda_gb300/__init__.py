@@ -8,15 +8,16 @@ reference's interface.  The directory name has a hyphen, so load it with
 __graft_entry__.py).
 """
 from ._abi import (PBF_ERR_CAPACITY, PBF_ERR_CUDA, PBF_ERR_INVALID_ARG, PBF_ERR_NOT_READY, PBF_ERR_TIMEOUT,
-                   PBF_OK, EXPORTED, EXPORTED_SSF, PbfError, PbfParams, PbfSsfParams, PbfSsfProfile, PbfStepProfile,
-                   PbfTuning, check, default_params, lib, lib_path)
+                   PBF_MAX_PARTICLES, PBF_OK, EXPORTED, EXPORTED_SSF, PbfError, PbfParams, PbfSsfParams,
+                   PbfSsfProfile, PbfStepProfile, PbfTuning, check, default_params, lib, lib_path)
 from .simulator import Ensemble, ParticleState, Simulator
 from .ssf import SSFRenderer, ssf_default_params
 from . import adjoint, driver, inverse, scenes, ssf
 
 __all__ = [
     "PBF_OK", "PBF_ERR_INVALID_ARG", "PBF_ERR_CAPACITY", "PBF_ERR_CUDA", "PBF_ERR_TIMEOUT",
-    "PBF_ERR_NOT_READY", "EXPORTED", "EXPORTED_SSF", "PbfError", "PbfParams", "PbfSsfParams", "PbfSsfProfile",
-    "PbfStepProfile", "PbfTuning", "check", "default_params", "lib", "lib_path", "Simulator", "ParticleState",
-    "Ensemble", "SSFRenderer", "ssf_default_params", "adjoint", "driver", "inverse", "scenes", "ssf",
+    "PBF_ERR_NOT_READY", "PBF_MAX_PARTICLES", "EXPORTED", "EXPORTED_SSF", "PbfError", "PbfParams",
+    "PbfSsfParams", "PbfSsfProfile", "PbfStepProfile", "PbfTuning", "check", "default_params", "lib", "lib_path",
+    "Simulator", "ParticleState", "Ensemble", "SSFRenderer", "ssf_default_params", "adjoint", "driver", "inverse",
+    "scenes", "ssf",
 ]

@@ -19,6 +19,9 @@ PBF_ERR_CUDA = 3
 PBF_ERR_TIMEOUT = 4
 PBF_ERR_NOT_READY = 5
 
+# Largest max_particles of a solver / total of a batch (32-bit table indices).
+PBF_MAX_PARTICLES = 1 << 27
+
 # Every symbol include/pbf.h declares, in declaration order.
 EXPORTED = (
     "pbf_params_default",

@@ -18,6 +18,13 @@
 
 #include "pbf_internal.cuh"
 
+// The kernels index per-particle tables with int: the neighbour masks
+// (kMaskWords words per particle) and the group hash (8 ints per particle)
+// are the largest.
+static_assert((long long)pbf::kMaskWords * PBF_MAX_PARTICLES - 1 <= 2147483647LL,
+              "mask index overflows int at PBF_MAX_PARTICLES");
+static_assert(8LL * PBF_MAX_PARTICLES - 1 <= 2147483647LL, "group hash index overflows int at PBF_MAX_PARTICLES");
+
 // Phase boundaries recorded by pbf_step when profiling is on.
 enum { kEvStart, kEvGrid, kEvReorder, kEvXsphStart, kEvEnd, kEvFixed };
 constexpr int kMaxProfiledIters = 64;
@@ -357,6 +364,8 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   *out = nullptr;
   if (!ulim || !llim) return fail(PBF_ERR_INVALID_ARG, "limits are NULL");
   if (max_particles < 0) return fail(PBF_ERR_INVALID_ARG, "max_particles < 0");
+  if (max_particles > PBF_MAX_PARTICLES)
+    return fail(PBF_ERR_CAPACITY, "max_particles = %d exceeds %d", max_particles, PBF_MAX_PARTICLES);
   pbf_status st = check_params(params);
   if (st != PBF_OK) return st;
   int dims[3];
@@ -950,7 +959,7 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
     if (counts[k] < 0) return fail(PBF_ERR_INVALID_ARG, "counts[%d] < 0", k);
     n += counts[k];
   }
-  if (n > 2147483647LL / 2) return fail(PBF_ERR_CAPACITY, "too many particles");
+  if (n > PBF_MAX_PARTICLES) return fail(PBF_ERR_CAPACITY, "%lld particles exceed %d", n, PBF_MAX_PARTICLES);
   pbf_batch* b = new (std::nothrow) pbf_batch();
   if (!b) return fail(PBF_ERR_CAPACITY, "host allocation failed");
   b->params = *params;

@@ -57,6 +57,11 @@ def test_params_layout_matches_c(pbf, tmp_path):
         assert getattr(pbf.PbfParams, f).offset == off, f
 
 
+def test_max_particles_matches_header(pbf):
+    m = re.search(r"#define PBF_MAX_PARTICLES (\d+)", HEADER.read_text())
+    assert m and int(m.group(1)) == pbf.PBF_MAX_PARTICLES == 1 << 27
+
+
 def test_default_params_are_the_reference_defaults(pbf):
     """fluids/FluidSystem.cpp:15-25, fluids/helper.h:4-9, fluids/Simulator.cu:174."""
     p = pbf.default_params()
@@ -88,6 +93,14 @@ def test_argument_errors_need_no_gpu(pbf):
     bad = (ctypes.c_float * 3)(0, 1, 1)  # ulim.x == llim.x
     assert L.pbf_create(ctypes.byref(p), bad, l, 10, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_create(ctypes.byref(p), u, l, -1, ctypes.byref(h)) == pbf.PBF_ERR_INVALID_ARG
+    # above the 32-bit index limit: refused before any CUDA call
+    assert L.pbf_create(ctypes.byref(p), u, l, pbf.PBF_MAX_PARTICLES + 1, ctypes.byref(h)) == pbf.PBF_ERR_CAPACITY
+    assert b"exceeds" in L.pbf_last_error() and h.value is None
+    counts = (ctypes.c_int * 2)(pbf.PBF_MAX_PARTICLES // 2, pbf.PBF_MAX_PARTICLES // 2 + 1)
+    u2 = (ctypes.c_float * 6)(1, 1, 1, 1, 1, 1)
+    l2 = (ctypes.c_float * 6)(0, 0, 0, 0, 0, 0)
+    assert L.pbf_batch_create(ctypes.byref(p), 2, u2, l2, counts, ctypes.byref(h)) == pbf.PBF_ERR_CAPACITY
+    assert h.value is None
     assert L.pbf_step(None, None, None, None, None, None, 1, None) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_set_params(None, ctypes.byref(p)) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_destroy(None) == pbf.PBF_OK
