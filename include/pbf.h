@@ -206,6 +206,8 @@ pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, v
  * [lo, hi] (device grid, x slowest), and the adjoint of that map: g_grid
  * (device, one float per node) -> g_pos (device, n float4).  Both are
  * gathers.  The loss of the inverse problem; no counterpart in the reference.
+ * PBF_ERR_INVALID_ARG unless lo < hi (finite), h > 0 (finite) and dims >= 1
+ * with fewer than 2^31 nodes.
  */
 pbf_status pbf_density_grid(const void* pos, int n, const float lo[3], const float hi[3],
                             const int dims[3], float h, float* grid, void* stream);

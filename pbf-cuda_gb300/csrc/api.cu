@@ -1115,14 +1115,30 @@ pbf_status pbf_batch_use_graphs(pbf_batch* b, int on) {
 
 // ---- density grid (the inverse problem's loss) ---------------------------------------
 
+namespace {
+
+// lo < hi finite, h > 0 finite, dims >= 1 with fewer than 2^31 nodes (the
+// kernels index nodes with int).
+pbf_status check_lattice(const float lo[3], const float hi[3], const int dims[3], float h) {
+  if (!(h > 0.f) || !std::isfinite(h)) return fail(PBF_ERR_INVALID_ARG, "h must be finite and > 0");
+  for (int a = 0; a < 3; ++a)
+    if (!(lo[a] < hi[a]) || !std::isfinite(lo[a]) || !std::isfinite(hi[a]))
+      return fail(PBF_ERR_INVALID_ARG, "lo must be below hi, both finite");
+  if (dims[0] < 1 || dims[1] < 1 || dims[2] < 1) return fail(PBF_ERR_INVALID_ARG, "dims must be >= 1");
+  if ((long long)dims[0] * dims[1] * dims[2] > 2147483647LL)
+    return fail(PBF_ERR_INVALID_ARG, "dims hold 2^31 or more nodes");
+  return PBF_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 pbf_status pbf_density_grid(const void* pos, int n, const float lo[3], const float hi[3],
                             const int dims[3], float h, float* grid, void* stream) {
   if ((!pos && n > 0) || !lo || !hi || !dims || !grid || n < 0)
     return fail(PBF_ERR_INVALID_ARG, "NULL argument or n < 0");
-  if (!(h > 0.f) || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
-    return fail(PBF_ERR_INVALID_ARG, "h must be > 0 and dims >= 1");
+  if (pbf_status st = check_lattice(lo, hi, dims, h); st != PBF_OK) return st;
   PBF_CUDA(pbf::density_grid((const float4*)pos, n, lo, hi, dims, h, grid, (cudaStream_t)stream),
            "pbf_density_grid");
   return PBF_OK;
@@ -1133,8 +1149,7 @@ pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], 
                                      void* stream) {
   if ((!pos && n > 0) || !lo || !hi || !dims || !g_grid || (!g_pos && n > 0) || n < 0)
     return fail(PBF_ERR_INVALID_ARG, "NULL argument or n < 0");
-  if (!(h > 0.f) || dims[0] < 1 || dims[1] < 1 || dims[2] < 1)
-    return fail(PBF_ERR_INVALID_ARG, "h must be > 0 and dims >= 1");
+  if (pbf_status st = check_lattice(lo, hi, dims, h); st != PBF_OK) return st;
   PBF_CUDA(pbf::density_grid_backward((const float4*)pos, n, lo, hi, dims, h, g_grid, (float4*)g_pos,
                                       (cudaStream_t)stream),
            "pbf_density_grid_backward");

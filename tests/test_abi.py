@@ -101,6 +101,17 @@ def test_argument_errors_need_no_gpu(pbf):
     l2 = (ctypes.c_float * 6)(0, 0, 0, 0, 0, 0)
     assert L.pbf_batch_create(ctypes.byref(p), 2, u2, l2, counts, ctypes.byref(h)) == pbf.PBF_ERR_CAPACITY
     assert h.value is None
+    # density lattice: empty or inverted boxes, 2^31 nodes (int node indices)
+    fake = ctypes.c_void_p(256)  # never dereferenced: the checks fail first
+    lo3, hi3 = (ctypes.c_float * 3)(0, 0, 0), (ctypes.c_float * 3)(2, 1, 1)
+    for bad_lo, bad_hi, dims in (((0, 0, 0), (2, 0, 1), (4, 4, 4)), ((0, 0, 0), (2, 1, float("inf")), (4, 4, 4)),
+                                 ((0, 0, 0), (2, 1, 1), (2048, 1024, 1024)), ((0, 0, 0), (2, 1, 1), (4, 0, 4))):
+        d = (ctypes.c_int * 3)(*dims)
+        bl, bh = (ctypes.c_float * 3)(*bad_lo), (ctypes.c_float * 3)(*bad_hi)
+        assert L.pbf_density_grid(None, 0, bl, bh, d, 0.1, fake, None) == pbf.PBF_ERR_INVALID_ARG
+        assert L.pbf_density_grid_backward(None, 0, bl, bh, d, 0.1, fake, None, None) == pbf.PBF_ERR_INVALID_ARG
+    d = (ctypes.c_int * 3)(4, 4, 4)
+    assert L.pbf_density_grid(None, 0, lo3, hi3, d, 0.0, fake, None) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_step(None, None, None, None, None, None, 1, None) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_set_params(None, ctypes.byref(p)) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_destroy(None) == pbf.PBF_OK
