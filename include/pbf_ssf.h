@@ -136,6 +136,8 @@ pbf_status pbf_ssf_set_sky(pbf_ssf* s, const float* faces, int size);
  * positions pos (float4, xyz used) through the five stages on `stream`
  * (asynchronous).  color: device float4[width * height], written where the
  * fluid is drawn; may be NULL (the intermediate images are still made).
+ * PBF_ERR_INVALID_ARG if n * radius >= 2^30 (the 64-bit fixed-point
+ * thickness sum of a pixel covered by every sprite would overflow).
  */
 pbf_status pbf_ssf_render(pbf_ssf* s, const void* pos, int n, void* color, void* stream);
 

@@ -441,7 +441,8 @@ pbf_status check_ssf_params(const pbf_ssf_params* p) {
     if (!(v > 0.f) || !std::isfinite(v))
       return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf: p_n, p_f, p_t, p_r, radius, sigma_r, sigma_z must be > 0");
   if (!(p->p_f > p->p_n)) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf: p_f must exceed p_n");
-  // thickness sums are 64-bit fixed point: 2 r 2^32 per fragment stays far below 2^63
+  // thickness sums are 64-bit fixed point, 2 r 2^32 per fragment (pbf_ssf_render
+  // also bounds n * radius, so that a pixel's sum stays below 2^63)
   if (!(p->radius <= 100.f)) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf: radius must be <= 100");
   if (p->kernel_r < 0 || p->kernel_r > kMaxKernelR)
     return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf: kernel_r must be in 0..20");
@@ -722,6 +723,9 @@ pbf_status pbf_ssf_render(pbf_ssf* s, const void* pos, int n, void* color, void*
   if (!s) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf is NULL");
   if (n < 0) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf render: n < 0");
   if (n > 0 && !pos) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf render: pos is NULL");
+  // a pixel's thickness sum is at most n fragments of 2 r 2^32 each: below 2^63
+  if ((double)n * s->p.radius >= 1073741824.0)
+    return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf render: n * radius must stay below 2^30");
   if (((uintptr_t)pos & 15u) || ((uintptr_t)color & 15u))
     return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf render: pos and color must be 16-byte aligned");
   cudaStream_t st = (cudaStream_t)stream;

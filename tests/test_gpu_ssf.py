@@ -234,6 +234,14 @@ def test_errors_and_state(pbf, cuda):
         bad = torch.zeros(5, dtype=torch.float32, device="cuda")[1:].reshape(1, 4)  # 4-byte aligned
         L = pbf.lib()
         assert L.pbf_ssf_render(r._h, bad.data_ptr(), 1, None, None) == pbf.PBF_ERR_INVALID_ARG
+        # n * radius >= 2^30 could overflow a pixel's fixed-point thickness sum:
+        # refused before any launch (pos is never read)
+        q = params_for(pbf, 64, 48)
+        q.radius = 100.0
+        r.load_params(q)
+        one = torch.zeros(1, 4, dtype=torch.float32, device="cuda")
+        assert L.pbf_ssf_render(r._h, one.data_ptr(), 10_737_419, None, None) == pbf.PBF_ERR_INVALID_ARG
+        r.load_params(p)
         r.render(torch.zeros(0, 4, device="cuda"))
         torch.cuda.synchronize()
         assert (r.images()["depth"] == 100).all()
