@@ -55,3 +55,30 @@ def test_driver_renders_frames(pbf, oracle, cuda, tmp_path):
     zup = np.stack([state[:, 0], -state[:, 2], state[:, 1], state[:, 3]], 1).astype(np.float32)
     o = oracle.ssf_render(p, zup, prec="f32")
     np.testing.assert_array_equal(depth.view(np.uint32), o["depth_raw"].view(np.uint32))
+
+
+def test_fluid_system_is_the_reference_application_loop(pbf, cuda):
+    """driver.fluid_system(moving=True): the reference's DoubleDamSource scene
+    with its default parameters, one step per frame, and its sweep
+    ulim.x + 2 sin(0.05 frame) (fluids/FluidSystem.cpp:34-61, 99-120) -- the
+    same states as stepping that scene by hand."""
+    import math
+
+    import torch
+
+    with pbf.driver.fluid_system(moving=True) as drv:
+        assert drv.scene.n == 32000 and drv.substeps == 1 and not drv.y_up
+        drv.run(3)
+        torch.cuda.synchronize()
+        got = drv.state.pos.cpu().numpy()
+        got_iid = drv.state.iid[: drv.state.n].cpu().numpy()
+    sc = pbf.scenes.reference_double_dam()
+    st = pbf.ParticleState(sc.pos, sc.vel)
+    with pbf.Simulator(sc.params, sc.ulim, sc.llim, sc.n) as sim:
+        for frame in range(3):
+            phi = math.sin(0.05 * frame)
+            sim.setLim((sc.ulim[0] + 2.0 * phi, sc.ulim[1], sc.ulim[2]), sc.llim)
+            st.step(sim)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(st.pos.cpu().numpy(), got)
+        np.testing.assert_array_equal(st.iid[: st.n].cpu().numpy(), got_iid)
