@@ -120,6 +120,22 @@ def dist_info():
     return rank, world, local
 
 
+def whole_job_rate(units_per_rank: float, local_ms: float, dist=None, device: str = "cuda"):
+    """Replicas (the path does not shard): every rank processed units_per_rank
+    units in local_ms.  The job took the slowest rank's time (max over ranks)
+    and processed every rank's units: returns (units / s, max ms).  dist is
+    torch.distributed with a process group, or None for one process."""
+    world, total_ms = 1, float(local_ms)
+    if dist is not None:
+        import torch
+
+        tt = torch.tensor([total_ms], dtype=torch.float64, device=device)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+        world = dist.get_world_size()
+    return world * units_per_rank / (total_ms / 1e3), total_ms
+
+
 def make_scene(pkg, name: str, params: str):
     scene = getattr(pkg.scenes, name)(seed=0)
     if params == "reference":
@@ -255,20 +271,16 @@ def run_ours(args):
     torch.cuda.synchronize()
     clk = clocks.stop()
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(step_ms)
+    value, total_ms = whole_job_rate(n * args.steps, sum(step_ms), dist)
     if dist is not None:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
         dist.barrier()
     sim.profile(False)
 
     # -- end to end through the public API with host buffers ------------------------
-    e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps or args.steps, stream)
+    e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps or args.steps, stream, dist)
     alt = (measure_reference_params(pkg, torch, args, stream)
            if args.params == "scene" and args.scene == "large_sweep" else None)
 
-    value = world * n * args.steps / (total_ms / 1e3)
     if rank != 0:
         sim.close()
         if dist is not None:
@@ -407,10 +419,11 @@ def measure_reference_params(pkg, torch, args, stream):
                        "delta_q": round(float(p.delta_q), 6), "c_XSPH": float(p.c_XSPH)}}
 
 
-def measure_e2e(pkg, torch, sim, scene, state0, steps, stream):
+def measure_e2e(pkg, torch, sim, scene, state0, steps, stream, dist=None):
     """Same metric through Simulator.step with HOST buffers: every step copies
     pos/vel/iid host->device from pinned memory, steps, and reads npos/nvel/iid
-    back; the copies are inside the timed region."""
+    back; the copies are inside the timed region.  With several ranks the
+    whole job's rate (every replica's steps over the slowest rank's time)."""
     pos0, vel0, iid0, t = state0
     n = scene.n
     p = scene.params
@@ -427,6 +440,8 @@ def measure_e2e(pkg, torch, sim, scene, state0, steps, stream):
         d_iid.copy_(h_iid, non_blocking=True)
         sim.step(d["pos"], d["npos"], d["vel"], d["nvel"], d_iid, n)
     torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -443,8 +458,8 @@ def measure_e2e(pkg, torch, sim, scene, state0, steps, stream):
         t += p.dt
     e1.record(stream)
     torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    return {"value": n * steps / (ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+    rate, ms = whole_job_rate(n * steps, e0.elapsed_time(e1), dist)
+    return {"value": rate, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "steps": steps, "ms_per_step": ms / steps}
 
 
