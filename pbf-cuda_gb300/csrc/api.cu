@@ -614,6 +614,7 @@ extern "C" {
 
 pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
                     int n, void* stream) {
+  const pbf::NvtxRange range("pbf_step");
   if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
   if (n < 0) return fail(PBF_ERR_INVALID_ARG, "n < 0");
   if (n > s->max_particles)
@@ -723,6 +724,7 @@ pbf_status pbf_tape_enable(pbf_solver* s, int depth) {
 
 pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, void* g_pos,
                         void* g_vel, float* g_lim, void* stream) {
+  const pbf::NvtxRange range("pbf_backward");
   if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
   if (s->tape_top <= 0) return fail(PBF_ERR_NOT_READY, "no taped step to reverse");
   if (!g_npos || !g_nvel || !g_pos || !g_vel || !g_lim) return fail(PBF_ERR_INVALID_ARG, "NULL buffer");
@@ -819,6 +821,7 @@ pbf_status pbf_get_density(const pbf_solver* s, float* rho, int n, void* stream)
 
 pbf_status pbf_build_grid(pbf_solver* s, const void* xstar, int n, uint32_t* keys, uint32_t* perm,
                           uint32_t* start, uint32_t* end, int dims[3], void* stream) {
+  const pbf::NvtxRange range("pbf_build_grid");
   if (!s || !dims) return fail(PBF_ERR_INVALID_ARG, "NULL argument");
   long long cells;
   pbf_status st = grid_dims(s->ulim, s->llim, s->params.h, dims, &cells);
@@ -1059,6 +1062,7 @@ pbf_status pbf_batch_set_limits(pbf_batch* b, int scene, const float ulim[3], co
 
 pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* nvel, uint32_t* iid,
                           void* stream) {
+  const pbf::NvtxRange range("pbf_batch_step");
   if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
   const int n = b->n;
   if (n == 0) return PBF_OK;
@@ -1136,6 +1140,7 @@ extern "C" {
 
 pbf_status pbf_density_grid(const void* pos, int n, const float lo[3], const float hi[3],
                             const int dims[3], float h, float* grid, void* stream) {
+  const pbf::NvtxRange range("pbf_density_grid");
   if ((!pos && n > 0) || !lo || !hi || !dims || !grid || n < 0)
     return fail(PBF_ERR_INVALID_ARG, "NULL argument or n < 0");
   if (pbf_status st = check_lattice(lo, hi, dims, h); st != PBF_OK) return st;
@@ -1147,6 +1152,7 @@ pbf_status pbf_density_grid(const void* pos, int n, const float lo[3], const flo
 pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], const float hi[3],
                                      const int dims[3], float h, const float* g_grid, void* g_pos,
                                      void* stream) {
+  const pbf::NvtxRange range("pbf_density_grid_backward");
   if ((!pos && n > 0) || !lo || !hi || !dims || !g_grid || (!g_pos && n > 0) || n < 0)
     return fail(PBF_ERR_INVALID_ARG, "NULL argument or n < 0");
   if (pbf_status st = check_lattice(lo, hi, dims, h); st != PBF_OK) return st;
@@ -1233,6 +1239,7 @@ extern "C" {
 
 pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
                         pbf_tuning* out, void* stream) {
+  const pbf::NvtxRange range("pbf_autotune");
   if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
   if (n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
   const int depth = s->tape_depth, top = s->tape_top;
@@ -1280,6 +1287,7 @@ pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
 
 pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, const uint32_t* iid, int steps,
                               pbf_tuning* out, void* stream) {
+  const pbf::NvtxRange range("pbf_batch_autotune");
   if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
   const int w0 = b->tune_window, a0 = b->tune_all;
   const pbf_status st = autotune(

@@ -126,6 +126,7 @@ pbf_status scratch_base(unsigned char** out) {
 extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float ulim[3],
                                        const float llim[3], void* pos, void* npos, void* vel,
                                        void* nvel, uint32_t* iid, int n, void* stream) {
+  const pbf::NvtxRange range("pbf_step_noalloc");
   if (n < 0) return pbf::set_error(PBF_ERR_INVALID_ARG, "pbf_step_noalloc: n < 0");
   if (n > kNoAllocMaxParticles)
     return pbf::set_error(PBF_ERR_CAPACITY,

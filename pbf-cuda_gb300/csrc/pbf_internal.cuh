@@ -3,11 +3,23 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "../../include/pbf.h"
 
 namespace pbf {
+
+// A named NVTX range over one C-ABI call, for profilers: the kernels a call
+// launches (graph launches included) fall inside it, so `ncu --nvtx
+// --nvtx-include "pbf_step/"` captures the steps alone.  NVTX is header-only;
+// with no tool attached a push or pop is a no-op.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // fluids/helper.h:4 — the reference's truncated pi, used by its host-side
 // kernel coefficients (getPoly6 / getSpikyGrad constructors).

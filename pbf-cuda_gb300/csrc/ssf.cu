@@ -720,6 +720,7 @@ pbf_status pbf_ssf_set_sky(pbf_ssf* s, const float* faces, int size) {
 }
 
 pbf_status pbf_ssf_render(pbf_ssf* s, const void* pos, int n, void* color, void* stream) {
+  const pbf::NvtxRange range("pbf_ssf_render");
   if (!s) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf is NULL");
   if (n < 0) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf render: n < 0");
   if (n > 0 && !pos) return pbf::set_error(PBF_ERR_INVALID_ARG, "ssf render: pos is NULL");
