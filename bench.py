@@ -102,6 +102,13 @@ class ClockSampler:
         except subprocess.TimeoutExpired:
             self.proc.kill()
             out, _ = self.proc.communicate()
+        return self.summarize(out)
+
+    @staticmethod
+    def summarize(out: str):
+        """The samples (nvidia-smi CSV rows of FIELDS, no header, no units) as
+        the JSON line's clocks: median SM MHz, max SM MHz, the throttle reasons
+        seen Active at least once."""
         rows = [r.split(",") for r in out.strip().splitlines() if r.count(",") >= 8]
         if not rows:
             return None
