@@ -168,3 +168,44 @@ def test_cpp_ssf_facade_compiles(tmp_path):
         }}
     """))
     subprocess.run(["g++", "-std=c++17", "-fsyntax-only", str(src)], check=True)
+
+
+def test_cpp_facades_throw_the_library_errors(pbf, tmp_path):
+    """The C++ facades linked against libpbf.so: argument and capacity errors
+    become pbf::Error with the C status before any CUDA call; without a GPU the
+    constructor reports the CUDA error the same way (no exit, no abort)."""
+    import torch
+
+    csrc = ROOT / "pbf-cuda_gb300" / "csrc"
+    src = tmp_path / "facade_run.cpp"
+    src.write_text(textwrap.dedent(f"""
+        #include <cstdio>
+        #include "{csrc / 'Simulator.hpp'}"
+        #include "{csrc / 'SSFRenderer.hpp'}"
+        int main() {{
+          pbf_params p;
+          pbf_params_default(&p);
+          pbf_params bad = p;
+          bad.niter = 0;
+          try {{ pbf::Simulator s(bad, {{1, 1, 1}}, {{0, 0, 0}}, 10); std::puts("no-throw"); }}
+          catch (const pbf::Error& e) {{ std::printf("invalid %d %s\\n", (int)e.status, e.what()); }}
+          try {{ pbf::Simulator s(p, {{1, 1, 1}}, {{0, 0, 0}}, PBF_MAX_PARTICLES + 1); std::puts("no-throw"); }}
+          catch (const pbf::Error& e) {{ std::printf("capacity %d\\n", (int)e.status); }}
+          try {{ pbf::Simulator s(p, {{1, 1, 1}}, {{0, 0, 0}}, 10); std::puts("created"); }}
+          catch (const pbf::Error& e) {{ std::printf("cuda %d\\n", (int)e.status); }}
+          pbf_ssf_params q = pbf::SSFRenderer::defaults(64, 48);
+          q.kernel_r = 21;
+          try {{ pbf::SSFRenderer r(q); std::puts("no-throw"); }}
+          catch (const pbf::Error& e) {{ std::printf("ssf-invalid %d\\n", (int)e.status); }}
+          return 0;
+        }}
+    """))
+    libdir = pbf.lib_path().parent
+    exe = tmp_path / "facade_run"
+    subprocess.run(["g++", "-std=c++17", str(src), "-o", str(exe), f"-L{libdir}", "-lpbf", f"-Wl,-rpath,{libdir}"],
+                   check=True)
+    lines = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines()
+    assert lines[0].startswith(f"invalid {pbf.PBF_ERR_INVALID_ARG} pbf_create") and "niter" in lines[0]
+    assert lines[1] == f"capacity {pbf.PBF_ERR_CAPACITY}"
+    assert lines[2] == ("created" if torch.cuda.is_available() else f"cuda {pbf.PBF_ERR_CUDA}")
+    assert lines[3] == f"ssf-invalid {pbf.PBF_ERR_INVALID_ARG}"
