@@ -15,7 +15,6 @@ from __future__ import annotations
 
 import ctypes
 import threading
-from pathlib import Path
 
 import numpy as np
 

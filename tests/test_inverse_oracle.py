@@ -12,7 +12,6 @@ leaving the clamp) costs ~1.5e-3, and below ~1e-5 the float32 wall position
 from __future__ import annotations
 
 import numpy as np
-import pytest
 
 
 def reduced_problem(pbf, oinv, steps=6):

@@ -3,8 +3,6 @@
 properties, and agreement of the float port with the FP64 oracle."""
 from __future__ import annotations
 
-import math
-
 import numpy as np
 import pytest
 
