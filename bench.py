@@ -66,6 +66,20 @@ def algorithmic_bytes(n: int, cells: int) -> dict:
     return {"lambda": n * (20 + 8 * c), "delta_p": n * (36 + 8 * c)}
 
 
+def fp32_roofline(n: int, steps: int, total_ms: float, sms, sm_mhz, niter: int = 4) -> dict:
+    """The pair work of the step against the FP32 pipes: ~27 true neighbours per
+    particle, ~25 flops per lambda pair, ~35 per delta_p pair, ~15 per XSPH
+    pair, so 27 (60 niter + 15) algorithmic flops per particle-step (candidates
+    outside h not counted).  Peak: SMs x 128 FP32 lanes x 2 (FMA) x the SM
+    clock (nominal; none is measured), or None without an SM count and clock."""
+    flops = 27 * (60 * niter + 15) * n
+    achieved = flops * steps / (total_ms / 1e3) / 1e12
+    peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12 if sms and sm_mhz else None
+    return {"bound": "fp32", "algorithmic_flops_per_step": flops, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak if peak else None,
+            "peak_kind": "nominal: SMs x 128 lanes x 2 x max SM clock"}
+
+
 def ncu_traffic(kernel: str):
     """dram bytes per launch of ``kernel`` from the committed ncu summary, scaled
     to the full workload there (line: 'traffic_bytes_per_launch <kernel>: <bytes>')."""
@@ -335,6 +349,8 @@ def run_ours(args):
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": alg[kernel], "launch_ms": launch_ms,
                      "traffic": ncu_traffic(kernel)},
+        "fp32": fp32_roofline(n, args.steps, total_ms, torch.cuda.get_device_properties(local).multi_processor_count,
+                              (clk or {}).get("sm_max_mhz"), p.niter),
         "phases_ms": phases,
         "cpu_baseline": cpu_line,
         "e2e": e2e,

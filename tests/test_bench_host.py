@@ -42,3 +42,12 @@ def test_traffic_from_committed_summary():
     t = bench.ncu_traffic("delta_p")
     assert t is not None and 1e6 < t < 1e9
     assert bench.ncu_traffic("no_such_kernel") is None
+
+
+def test_fp32_roofline():
+    # 1M particles, 4 iterations: 27 (240 + 15) = 6,885 flops per particle-step
+    r = bench.fp32_roofline(1 << 20, 240, 240 * 2.5, 152, 2070.0, 4)
+    assert r["algorithmic_flops_per_step"] == 6885 * (1 << 20)
+    assert abs(r["achieved"] - 6885 * (1 << 20) / 2.5e-3 / 1e12) < 1e-9
+    assert abs(r["peak"] - 152 * 256 * 2070e6 / 1e12) < 1e-9 and 0 < r["frac"] < 1
+    assert bench.fp32_roofline(1000, 10, 5.0, None, None)["frac"] is None
