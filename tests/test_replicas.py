@@ -7,6 +7,7 @@ is bench.whole_job_rate; here two gloo ranks with unequal times check it.
 """
 from __future__ import annotations
 
+import datetime
 import os
 import socket
 import sys
@@ -29,7 +30,7 @@ def _rank(rank: int, world: int, port: int, times_ms, out_dir: str) -> None:
     sys.path.insert(0, str(ROOT))
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
-    dist.init_process_group("gloo", rank=rank, world_size=world)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=60))
     import bench
 
     rate, ms = bench.whole_job_rate(1000 * 240, times_ms[rank], dist, device="cpu")
