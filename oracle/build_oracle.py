@@ -42,5 +42,27 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
+SAN_FLAGS = ["-O1", "-g", "-fno-omit-frame-pointer", "-fsanitize=address,undefined"]
+
+
+def build_sanitized(out_dir: Path) -> Path:
+    """The same library built with AddressSanitizer and UndefinedBehaviorSanitizer
+    into out_dir (tests/test_oracle_sanitized.py), for a process started with
+    the sanitizer runtimes preloaded."""
+    out_dir = Path(out_dir)
+    out_dir.mkdir(parents=True, exist_ok=True)
+    flags = [f for f in CFLAGS if not f.startswith("-O")] + SAN_FLAGS
+    objs = []
+    for src in (SRC, SSF_SRC):
+        for tag, defs in (("f32", []), ("f64", ["-DORACLE_F64"])):
+            obj = out_dir / f"{src.stem}_{tag}.o"
+            subprocess.run(["gcc", *flags, *defs, "-c", str(src), "-o", str(obj)], check=True)
+            objs.append(str(obj))
+    lib = out_dir / "liboracle.so"
+    subprocess.run(["gcc", "-shared", "-fopenmp", "-fsanitize=address,undefined", "-o", str(lib), *objs, "-lm"],
+                   check=True)
+    return lib
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))
