@@ -157,9 +157,10 @@ def whole_job_rate(units_per_rank: float, local_ms: float, dist=None, device: st
 
 
 def make_scene(pkg, name: str, params: str):
+    """The workload's scene (pure Python: loads no CUDA code)."""
     scene = getattr(pkg.scenes, name)(seed=0)
     if params == "reference":
-        p = pkg.default_params()
+        p = pkg.scenes.reference_params()
         p.up[0], p.up[1], p.up[2] = 0.0, 1.0, 0.0
         p.dt = scene.params.dt
         scene.params = p
@@ -184,6 +185,12 @@ def cpu_port_rate(oracle, scene, pos, vel, iid, t0: float, budget_s: float, max_
 
 
 def run_reference(args):
+    """The reference arm: the float OpenMP port of the reference's kernels
+    (oracle/; the reference has no CPU path of its own) on all host threads.
+    It loads none of this repository's CUDA code: the scene is generated in
+    Python and the port is the oracle library.  Same workload and parameters
+    as the GPU arm; the same W warm-up steps from the lattice (time-bounded),
+    then as many of the K timed steps as fit in --cpu-budget seconds."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
@@ -192,7 +199,6 @@ def run_reference(args):
 
     scene = make_scene(pkg, args.scene, args.params)
     iid = np.arange(scene.n, dtype=np.uint32)
-    # warm-up, bounded: the CPU arm cannot afford the GPU arm's 60 warm-up frames
     pos, vel = scene.pos, scene.vel
     t = 0.0
     w_done = 0
@@ -205,13 +211,15 @@ def run_reference(args):
         w_done += 1
     rate, steps, spent = cpu_port_rate(oracle, scene, pos, vel, iid, t, args.cpu_budget, args.steps)
     cores = oracle.threads()
-    sample = (f"{scene.n} particles per step, {steps} of {args.steps} timed steps after {w_done} of "
-              f"{args.warmup} warm-up steps (time-bounded)")
+    first = w_done + 1
+    sample = (f"{scene.n} particles per step; steps {first}-{first + steps - 1} of the workload "
+              f"({steps} of {args.steps} timed steps, after {w_done} of {args.warmup} warm-up steps; time-bounded)")
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": world,
         "steps": steps, "warmup": w_done, "ms_per_step": 1e3 * spent / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": workload_config(scene, args),
+        "steps_timed": [first, first + steps - 1],
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -298,8 +306,15 @@ def run_ours(args):
 
     # -- end to end through the public API with host buffers ------------------------
     e2e = measure_e2e(pkg, torch, sim, scene, state0, args.e2e_steps or args.steps, stream, dist)
-    alt = (measure_reference_params(pkg, torch, args, stream)
-           if args.params == "scene" and args.scene == "large_sweep" else None)
+    sweep = args.scene == "large_sweep"
+    alt = measure_reference_params(pkg, torch, args, stream) if args.params == "scene" and sweep else None
+    # the workload's own window (60 warm-up frames, 120 timed frames), when
+    # the main run timed another one
+    window = (time_window(pkg, torch, args, stream, args.params, 120, 240)
+              if args.extras and sweep and (args.warmup, args.steps) != (120, 240) and rank == 0 else None)
+    ensemble = ensemble_rates(pkg, torch, args, 3, 10) if args.extras and rank == 0 else None
+    adjoint = adjoint_times(pkg, torch, args, 2, 60) if args.extras and rank == 0 else None
+    ref_gpu = measure_reference_gpu(scene, args) if args.ref_gpu and rank == 0 else None
 
     if rank != 0:
         sim.close()
@@ -358,6 +373,10 @@ def run_ours(args):
         "clocks": clk,
         "step_ms": {"min": min(step_ms), "median": statistics.median(step_ms), "max": max(step_ms)},
         "reference_params": alt,
+        "reference_gpu": ref_gpu,
+        "window_120_240": window,
+        "ensemble": ensemble,
+        "adjoint": adjoint,
     }
     print(json.dumps(line), flush=True)
     sim.close()
@@ -404,12 +423,11 @@ def gpu_rate_first_steps(pkg, torch, scene, steps, stream):
     return scene.n * steps / (total / 1e3)
 
 
-def measure_reference_params(pkg, torch, args, stream):
-    """The same workload (particles, box, moving wall, iterations, dt) with the
-    reference's own solver parameters (fluids/FluidSystem.cpp:15-25), under
-    which the fluid stays a fluid: warm-up and timed steps as the main run,
-    timed the same way (L2 flushed before every step)."""
-    scene = make_scene(pkg, args.scene, "reference")
+def time_window(pkg, torch, args, stream, params: str, warmup: int, steps: int) -> dict:
+    """The workload with the given parameter set from the lattice: `warmup`
+    untimed steps, the choice of pbf_autotune (as the main run makes it), then
+    `steps` steps timed with CUDA events, L2 flushed before every step."""
+    scene = make_scene(pkg, args.scene, params)
     p = scene.params
     st = pkg.ParticleState(scene.pos, scene.vel)
     sim = pkg.Simulator(p, scene.ulim, scene.llim, scene.n)
@@ -417,12 +435,12 @@ def measure_reference_params(pkg, torch, args, stream):
     t = 0.0
     total = 0.0
     tuning = None
-    for k in range(args.warmup + args.steps):
+    for k in range(warmup + steps):
         ulim, llim = scene.limits_at(t)
-        if k == args.warmup:
+        if k == warmup:
             torch.cuda.synchronize()
             tuning = tune(sim, st, scene.n, args)
-        if k >= args.warmup:
+        if k >= warmup:
             flush.fill_(1.0)
             torch.cuda._sleep(2_000_000)
             e0 = torch.cuda.Event(enable_timing=True)
@@ -430,15 +448,63 @@ def measure_reference_params(pkg, torch, args, stream):
             e0.record(stream)
         sim.setLim(ulim, llim)
         st.step(sim)
-        if k >= args.warmup:
+        if k >= warmup:
             e1.record(stream)
             e1.synchronize()
             total += e0.elapsed_time(e1)
         t += p.dt
     sim.close()
-    return {"value": scene.n * args.steps / (total / 1e3), "unit": UNIT, "ms_per_step": total / args.steps,
-            "tuning": tuning, "params": {"pho0": float(p.pho0), "lambda_eps": float(p.lambda_eps), "k_corr": round(float(p.k_corr), 6),
+    return {"value": scene.n * steps / (total / 1e3), "unit": UNIT, "ms_per_step": total / steps,
+            "warmup": warmup, "steps": steps, "tuning": tuning,
+            "params": {"pho0": float(p.pho0), "lambda_eps": float(p.lambda_eps), "k_corr": round(float(p.k_corr), 6),
                        "delta_q": round(float(p.delta_q), 6), "c_XSPH": float(p.c_XSPH)}}
+
+
+def measure_reference_params(pkg, torch, args, stream):
+    """The same workload (particles, box, moving wall, iterations, dt) with the
+    reference's own solver parameters (fluids/FluidSystem.cpp:15-25), under
+    which the fluid stays a fluid: warm-up and timed steps as the main run."""
+    return time_window(pkg, torch, args, stream, "reference", args.warmup, args.steps)
+
+
+def measure_reference_gpu(scene, args):
+    """The reference's own CUDA kernels rebuilt for sm_103a (oracle/ref_harness:
+    its unmodified fluids/Simulator.cu, driven with Simulator::step's host
+    sequencing, fluids/Simulator.cpp:10-99) on the same workload and steps as
+    the main run: W warm-up steps from the lattice, then the timed steps, the
+    moving wall stepped the same way; with the reference's per-phase
+    cudaDeviceSynchronize and without it.  The timed steps are bounded: a
+    3-step probe first, then as many of the K steps as fit in
+    --ref-gpu-budget seconds."""
+    try:
+        from oracle.ref_harness import ref
+    except Exception as e:  # noqa: BLE001 - reported, not raised
+        return {"unavailable": f"reference harness import failed: {e}"}
+    if not ref.available():
+        return {"unavailable": "reference kernels not built (the cubin is built where the reference sources are)"}
+    p = scene.params
+    n = scene.n
+
+    def walls(k_steps):
+        return np.array([scene.limits_at(k * p.dt)[0][0] for k in range(args.warmup + k_steps)], np.float32)
+
+    out = {"kind": "the reference's kernels rebuilt for sm_103a", "warmup": args.warmup}
+    try:
+        probe = min(3, args.steps)
+        a = time.perf_counter()
+        ms = ref.bench(p, scene.ulim, scene.llim, scene.pos, scene.vel, args.warmup, probe, walls(probe), sync=True)
+        per_call_s = time.perf_counter() - a
+        per_step_s = per_call_s / (args.warmup + probe)
+        k = max(probe, min(args.steps, int(args.ref_gpu_budget / max(per_step_s, 1e-6)) - args.warmup))
+        if k > probe:
+            ms = ref.bench(p, scene.ulim, scene.llim, scene.pos, scene.vel, args.warmup, k, walls(k), sync=True)
+        out["steps"] = k
+        out["phase_syncs"] = {"value": n * k / (ms / 1e3), "unit": UNIT, "ms_per_step": ms / k}
+        ms2 = ref.bench(p, scene.ulim, scene.llim, scene.pos, scene.vel, args.warmup, k, walls(k), sync=False)
+        out["no_syncs"] = {"value": n * k / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2 / k}
+    except Exception as e:  # noqa: BLE001
+        out["unavailable"] = f"reference harness failed: {e}"
+    return out
 
 
 def measure_e2e(pkg, torch, sim, scene, state0, steps, stream, dist=None):
@@ -485,52 +551,47 @@ def measure_e2e(pkg, torch, sim, scene, state0, steps, stream, dist=None):
             "steps": steps, "ms_per_step": ms / steps}
 
 
-def run_ensemble(args):
-    """Ensemble scenes/s: 256 independent dam-break scenes (a x b x c lattices,
-    a, b, c uniform in [12, 40], each in its own (2a d, 2b d, 2c d) box), one
-    scene-step = one scene advanced one step.  Batched (pbf_batch_step: one
-    launch per pass for all scenes, dense-kernel choices from
-    pbf_batch_autotune after the warm-up) vs one scene per launch (256
-    solvers stepped in turn), same steps, same stream, CUDA events."""
-    import torch
-
-    pkg = load_pkg()
+def ensemble_rates(pkg, torch, args, warmup: int, steps: int) -> dict:
+    """Scene-steps/s of the 256-scene ensemble (dam-break scenes, a x b x c
+    lattices with a, b, c uniform in [12, 40], each in its own (2a d, 2b d,
+    2c d) box), batched (pbf_batch_step: one launch per pass for all scenes,
+    choices from pbf_batch_autotune after the warm-up) and one scene per
+    launch (a solver per scene, stepped in turn); same steps, same stream,
+    CUDA events around the timed steps."""
     scenes = pkg.scenes.ensemble(seed=0, count=args.scenes)
     p = scenes[0].params
     if args.params == "reference":
-        q = pkg.default_params()
+        q = pkg.scenes.reference_params()
         q.up[0], q.up[1], q.up[2] = 0.0, 1.0, 0.0
         q.dt = p.dt
         p = q
     stream = torch.cuda.current_stream()
     counts = [sc.n for sc in scenes]
     pos = np.concatenate([sc.pos for sc in scenes])
-    # batched, with the dense-kernel choices autotuned on the warmed-up state
     st = pkg.ParticleState(pos, np.zeros_like(pos))
     ens = pkg.Ensemble(p, [sc.ulim for sc in scenes], [sc.llim for sc in scenes], counts)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         st.step(ens)
     tuning = ens.autotune(st.pos, st.vel, st.iid, steps=2)
     torch.cuda.synchronize()
     torch.cuda._sleep(5_000_000)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         st.step(ens)
     e1.record(stream)
     torch.cuda.synchronize()
     batched_ms = e0.elapsed_time(e1)
     ens.close()
-    # one scene per launch
     sts = [pkg.ParticleState(sc.pos, sc.vel) for sc in scenes]
     sims = [pkg.Simulator(p, sc.ulim, sc.llim, sc.n) for sc in scenes]
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         for s_, m in zip(sts, sims):
             s_.step(m)
     torch.cuda.synchronize()
     torch.cuda._sleep(5_000_000)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         for s_, m in zip(sts, sims):
             s_.step(m)
     e1.record(stream)
@@ -538,57 +599,66 @@ def run_ensemble(args):
     single_ms = e0.elapsed_time(e1)
     for m in sims:
         m.close()
-    k = len(scenes) * args.steps
+    k = len(scenes) * steps
+    return {"value": k / (batched_ms / 1e3), "unit": "scene-steps/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": batched_ms / steps, "scenes": len(scenes), "particles": sum(counts),
+            "params": args.params, "autotune": tuning,
+            "one_scene_per_launch": {"value": k / (single_ms / 1e3), "ms_per_step": single_ms / steps},
+            "batched_over_per_scene": single_ms / batched_ms}
+
+
+def run_ensemble(args):
+    """Ensemble scenes/s (see ensemble_rates): one scene-step = one scene
+    advanced one step."""
+    import torch
+
+    pkg = load_pkg()
+    r = ensemble_rates(pkg, torch, args, args.warmup, args.steps)
     line = {
-        "metric": "ensemble scenes/s", "value": k / (batched_ms / 1e3), "unit": "scene-steps/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": batched_ms / args.steps,
+        "metric": "ensemble scenes/s", "value": r["value"], "unit": "scene-steps/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{len(scenes)} dam-break scenes, a,b,c ~ U{{12..40}} (seed 0), "
-                               f"{sum(counts)} particles, {p.niter} iterations, dt=1/120 s",
-                   "params": args.params, "particles": sum(counts)},
-        "autotune": tuning,
-        "one_scene_per_launch": {"value": k / (single_ms / 1e3), "ms_per_step": single_ms / args.steps},
-        "batched_over_per_scene": single_ms / batched_ms,
+        "config": {"workload": f"{r['scenes']} dam-break scenes, a,b,c ~ U{{12..40}} (seed 0), "
+                               f"{r['particles']} particles, 4 iterations, dt=1/120 s",
+                   "params": args.params, "particles": r["particles"]},
+        "autotune": r["autotune"],
+        "one_scene_per_launch": r["one_scene_per_launch"],
+        "batched_over_per_scene": r["batched_over_per_scene"],
     }
     print(json.dumps(line), flush=True)
 
 
-def run_adjoint(args):
+def adjoint_times(pkg, torch, args, evals: int, frames: int) -> dict:
     """fwd+bwd ms/frame of the inverse problem: 15,625 particles (25^3
-    lattice) in a 2 x 1 x 1 box, 60 frames of 2 steps, the loss on a
+    lattice) in a 2 x 1 x 1 box, `frames` frames of 2 steps, the loss on a
     32 x 16 x 16 density grid, checkpoints every 10 frames.  One evaluation =
     the forward rollout + the density grid + the reverse sweep (which re-runs
-    each 10-frame segment from its checkpoint and each step once more with the
-    tape on) + the adjoint of the grid; timed with CUDA events around whole
-    evaluations.  The forward alone (the same 120 steps through pbf_step,
-    no tape) is timed beside it for the fwd+bwd / fwd ratio."""
-    import torch
-
-    pkg = load_pkg()
+    each 10-frame segment from its checkpoint with the tape on) + the adjoint
+    of the grid; timed with CUDA events around whole evaluations.  The forward
+    alone (the same steps through pbf_step, no tape) is timed beside it."""
     scene = pkg.scenes.inverse_scene()
     if args.params == "reference":
-        q = pkg.default_params()
+        q = pkg.scenes.reference_params()
         q.up[0], q.up[1], q.up[2] = 0.0, 1.0, 0.0
         q.dt = scene.params.dt
         scene.params = q
     stream = torch.cuda.current_stream()
-    ip = pkg.inverse.InverseProblem(scene, frames=args.frames, every=10)
+    ip = pkg.inverse.InverseProblem(scene, frames=frames, every=10)
     ip.make_target()
     v0 = torch.zeros((ip.n, 3), device="cuda")
-    warm = max(3, min(args.warmup, 3))
+    warm = 3
     for _ in range(warm):
         ip.loss_and_grad(v0, 0.0)
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.evals):
+    for _ in range(evals):
         L, gv, ga = ip.loss_and_grad(v0, 0.0)
     e1.record(stream)
     torch.cuda.synchronize()
-    fb_ms = e0.elapsed_time(e1) / args.evals
+    fb_ms = e0.elapsed_time(e1) / evals
     finite = bool(torch.isfinite(gv).all()) and bool(np.isfinite(ga))
     ip.close()
-    # forward alone
     sim = pkg.Simulator(scene.params, scene.ulim, scene.llim, scene.n)
     st = pkg.ParticleState(scene.pos, scene.vel)
     for _ in range(warm):
@@ -597,7 +667,7 @@ def run_adjoint(args):
     p0 = torch.from_numpy(scene.pos).cuda()
     iid0 = torch.arange(scene.n, dtype=torch.int32, device="cuda")
     e0.record(stream)
-    for _ in range(args.evals):
+    for _ in range(evals):
         st.a_pos[: st.n].copy_(p0)
         st.a_vel.zero_()
         st.iid[: st.n].copy_(iid0)
@@ -607,20 +677,32 @@ def run_adjoint(args):
             st.step(sim)
     e1.record(stream)
     torch.cuda.synchronize()
-    f_ms = e0.elapsed_time(e1) / args.evals
+    f_ms = e0.elapsed_time(e1) / evals
     sim.close()
-    frames = ip.steps // pkg.inverse.STEPS_PER_FRAME
+    nframes = ip.steps // pkg.inverse.STEPS_PER_FRAME
+    return {"value": fb_ms / nframes, "unit": "ms/frame", "evals": evals, "warmup": warm, "frames": nframes,
+            "particles": scene.n, "params": args.params, "ms_per_step": fb_ms / ip.steps,
+            "forward_ms_per_frame": f_ms / nframes, "fwd_bwd_over_fwd": fb_ms / f_ms,
+            "gradient_finite": finite}
+
+
+def run_adjoint(args):
+    """fwd+bwd ms/frame of the inverse problem (see adjoint_times)."""
+    import torch
+
+    pkg = load_pkg()
+    r = adjoint_times(pkg, torch, args, args.evals, args.frames)
     line = {
-        "metric": "fwd+bwd ms/frame", "value": fb_ms / frames, "unit": "ms/frame", "n_gpus": 1,
-        "steps": args.evals, "warmup": warm, "ms_per_step": fb_ms / ip.steps, "higher_is_better": False,
+        "metric": "fwd+bwd ms/frame", "value": r["value"], "unit": "ms/frame", "n_gpus": 1,
+        "steps": args.evals, "warmup": r["warmup"], "ms_per_step": r["ms_per_step"], "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"inverse problem: {scene.n} particles (25^3 lattice, spacing 0.04) in a 2x1x1 box, "
-                               f"{frames} frames x 2 steps, {scene.params.niter} iterations, density loss on "
+        "config": {"workload": f"inverse problem: {r['particles']} particles (25^3 lattice, spacing 0.04) in a "
+                               f"2x1x1 box, {r['frames']} frames x 2 steps, 4 iterations, density loss on "
                                f"32x16x16, checkpoints every 10 frames",
-                   "params": args.params, "particles": scene.n},
-        "forward_ms_per_frame": f_ms / frames,
-        "fwd_bwd_over_fwd": fb_ms / f_ms,
-        "gradient_finite": finite,
+                   "params": args.params, "particles": r["particles"]},
+        "forward_ms_per_frame": r["forward_ms_per_frame"],
+        "fwd_bwd_over_fwd": r["fwd_bwd_over_fwd"],
+        "gradient_finite": r["gradient_finite"],
     }
     print(json.dumps(line), flush=True)
 
@@ -758,7 +840,13 @@ def main(argv=None):
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
     ap.add_argument("--cpu-steps", type=int, default=20,
                     help="most steps the CPU baseline times (0: no CPU baseline, for profiling runs)")
-    ap.add_argument("--cpu-warmup-steps", type=int, default=3, help="most warm-up steps of the reference arm")
+    ap.add_argument("--cpu-warmup-steps", type=int, default=8, help="most warm-up steps of the reference arm")
+    ap.add_argument("--no-extras", dest="extras", action="store_false",
+                    help="skip the sub-measurements (120/240 window, ensemble, adjoint) of the step workload")
+    ap.add_argument("--no-ref-gpu", dest="ref_gpu", action="store_false",
+                    help="skip timing the reference's own kernels (rebuilt for sm_103a) beside the run")
+    ap.add_argument("--ref-gpu-budget", type=float, default=40.0,
+                    help="seconds of reference-kernel steps per variant (bounds its timed steps)")
     ap.add_argument("--cpu-warmup-budget", type=float, default=60.0)
     args = ap.parse_args(argv)
     if args.warmup < 3:

@@ -1,7 +1,10 @@
 """Build recipe of the reference harness (test infrastructure).
 
+The reference checkout is taken from the PBF_REFERENCE environment variable
+(default: /root/reference, where this build's container mounts it).
+
 build_cubin():    nvcc -cubin of the reference's unmodified kernels
-                  (/root/reference/fluids/Simulator.cu and the
+                  (<reference>/fluids/Simulator.cu and the
                   Simulator_kernel.cuh it includes) plus the wrappers in
                   ref_kernels.cu, device code only, for sm_103a
                   -> oracle/_ref/ref_kernels.cubin.  Needs the reference
@@ -28,7 +31,8 @@ HERE = Path(__file__).resolve().parent
 ROOT = HERE.parent.parent
 OUT = ROOT / "oracle" / "_ref"
 CUBIN = OUT / "ref_kernels.cubin"
-REFERENCE = Path("/root/reference")
+# the reference checkout (read-only; nothing is written there)
+REFERENCE = Path(os.environ.get("PBF_REFERENCE", "/root/reference"))
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

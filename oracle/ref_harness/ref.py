@@ -35,7 +35,7 @@ def lib():
             L.pbfref_step.argtypes = [P(OracleParams), f, f, f, f, f, f, u, ctypes.c_int, f, f, u, u, u,
                                       P(ctypes.c_int)]
             L.pbfref_bench.argtypes = [P(OracleParams), f, f, f, f, ctypes.c_int, ctypes.c_int, ctypes.c_int, f,
-                                       P(ctypes.c_double)]
+                                       ctypes.c_int, P(ctypes.c_double)]
             rc = L.pbfref_init(str(build_ref.CUBIN).encode())
             if rc != 0:
                 raise RuntimeError(f"pbfref_init: {L.pbfref_last_error().decode()}")
@@ -87,8 +87,10 @@ def step(params, ulim, llim, pos, vel, iid) -> dict:
             "ids": ids, "start": start, "end": end, "dims": tuple(dims)}
 
 
-def bench(params, ulim, llim, pos, vel, warmup: int, steps: int, ulim_x=None) -> float:
-    """Milliseconds of `steps` reference steps on device-resident state."""
+def bench(params, ulim, llim, pos, vel, warmup: int, steps: int, ulim_x=None, sync: bool = True) -> float:
+    """Milliseconds of `steps` reference steps on device-resident state, after
+    `warmup` untimed ones; ulim_x: the x-max wall of every step (warm-up
+    first); sync: keep the reference's per-phase cudaDeviceSynchronize."""
     L = lib()
     pos3, vel3 = _f3(pos), _f3(vel)
     ux = None if ulim_x is None else np.ascontiguousarray(ulim_x, np.float32)
@@ -96,7 +98,8 @@ def bench(params, ulim, llim, pos, vel, warmup: int, steps: int, ulim_x=None) ->
     op = to_oracle_params(params)
     fl = ctypes.c_float
     rc = L.pbfref_bench(ctypes.byref(op), _lim(ulim), _lim(llim), _p(pos3, fl), _p(vel3, fl), pos3.shape[0],
-                        int(warmup), int(steps), None if ux is None else _p(ux, fl), ctypes.byref(ms))
+                        int(warmup), int(steps), None if ux is None else _p(ux, fl), int(bool(sync)),
+                        ctypes.byref(ms))
     if rc != 0:
         raise RuntimeError(f"pbfref_bench: {L.pbfref_last_error().decode()}")
     return ms.value

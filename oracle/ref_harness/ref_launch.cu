@@ -335,11 +335,13 @@ int pbfref_step(const pbf_params* P, const float ulim[3], const float llim[3], f
 
 // Times `steps` reference steps after `warmup` untimed ones on device-resident
 // state (tic-toc roles as fluids/FluidSystem.cpp:112-117), with the
-// reference's per-phase device synchronisation.  ulim_x[k] is the x-max wall
-// of step k (warm-up steps first); ms_out receives the total time of the
-// timed steps (host wall clock around the synchronous steps, in ms).
+// reference's per-phase device synchronisation (sync != 0) or without it (the
+// same launches, stream-ordered).  ulim_x[k] is the x-max wall of step k
+// (warm-up steps first); ms_out receives the total time of the timed steps
+// (CUDA events around them, in ms).
 int pbfref_bench(const pbf_params* P, const float ulim[3], const float llim[3], const float* h_pos,
-                 const float* h_vel, int n, int warmup, int steps, const float* ulim_x, double* ms_out) {
+                 const float* h_vel, int n, int warmup, int steps, const float* ulim_x, int sync,
+                 double* ms_out) {
   if (!g_mod) return fail("pbfref_init not called", 1);
   const int3 dims = grid_dims(ulim, llim, P->h);
   const long long cells = (long long)dims.x * dims.y * dims.z;
@@ -368,8 +370,8 @@ int pbfref_bench(const pbf_params* P, const float ulim[3], const float llim[3], 
         RT(cudaEventRecord(e0));
       }
       float u[3] = {ulim_x ? ulim_x[k] : ulim[0], ulim[1], ulim[2]};
-      int q = tic ? ref_step_device(*P, u, llim, d, d.npos, d.pos, d.nvel, d.vel, n, true)
-                  : ref_step_device(*P, u, llim, d, d.pos, d.npos, d.vel, d.nvel, n, true);
+      int q = tic ? ref_step_device(*P, u, llim, d, d.npos, d.pos, d.nvel, d.vel, n, sync != 0)
+                  : ref_step_device(*P, u, llim, d, d.pos, d.npos, d.vel, d.nvel, n, sync != 0);
       if (q) return q;
       tic = !tic;
     }

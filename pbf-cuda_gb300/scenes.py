@@ -34,7 +34,7 @@ from typing import Callable, List, Optional, Tuple
 
 import numpy as np
 
-from ._abi import PbfParams, default_params
+from ._abi import PbfParams
 
 SPACING = 0.05
 JITTER = 0.005
@@ -58,11 +58,38 @@ def rest_density(h: float = H, spacing: float = SPACING) -> float:
     return float(np.float32(rho))
 
 
+def reference_params() -> PbfParams:
+    """The reference's solver defaults (fluids/FluidSystem.cpp:15-25; LIM_EPS,
+    KERNAL_EPS and MAX_DP from fluids/helper.h:5-9), z up as the reference's
+    advect_kernel has it: the values pbf_params_default fills in, set here
+    without the library so that building a scene (the CPU reference arm of
+    bench.py does) loads no CUDA code.  tests/test_scenes.py checks the two
+    agree field for field."""
+    p = PbfParams()
+    p.niter = 4
+    p.pho0 = 8000.0
+    p.g = 9.8
+    p.h = 0.1
+    p.dt = 0.0083
+    p.lambda_eps = 1000.0
+    p.delta_q = 0.3 * float(np.float32(0.1))  # (float)(0.3 * h), h the float 0.1
+    p.k_corr = 0.001
+    p.n_corr = 4.0
+    p.k_boundaryDensity = 0.0
+    p.c_XSPH = 0.5
+    p.up[0], p.up[1], p.up[2] = 0.0, 0.0, 1.0
+    p.lim_eps = 1e-3
+    p.kernel_eps = 1e-4
+    p.max_dp = 0.1
+    p.vorticity_eps = 0.0
+    return p
+
+
 def scene_params(niter: int = 4) -> PbfParams:
     """Solver parameters of the dam-break scenes: h = 0.1, pho0 = lattice
     density, epsilon = 100, s_corr k = 0.1 n = 4 dq = 0.2 h, XSPH c = 0.01,
     gravity 9.8 along -y, dt = 1/120 s (a 1/60 s frame in 2 steps)."""
-    p = default_params()
+    p = reference_params()
     p.niter = niter
     p.h = H
     p.pho0 = rest_density()
@@ -205,7 +232,7 @@ def reference_double_dam() -> Scene:
     pos = np.zeros((len(pts), 4), np.float32)
     pos[:, :3] = np.asarray(pts, np.float32)
     return Scene("reference_double_dam_32k", pos, _zeros_like(pos), (2.0, 2.0, 4.0), (-2.0, -2.0, 0.0),
-                 params=default_params())
+                 params=reference_params())
 
 
 def reference_fixed_cube() -> Scene:
@@ -224,7 +251,7 @@ def reference_fixed_cube() -> Scene:
     pos = np.zeros((len(pts), 4), np.float32)
     pos[:, :3] = np.asarray(pts, np.float32)
     return Scene("reference_fixed_cube_27k", pos, _zeros_like(pos), (2.0, 2.0, 4.0), (-2.0, -2.0, 0.0),
-                 params=default_params())
+                 params=reference_params())
 
 
 def sweep_wall_x(t: float) -> float:

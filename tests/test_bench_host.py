@@ -51,3 +51,24 @@ def test_fp32_roofline():
     assert abs(r["achieved"] - 6885 * (1 << 20) / 2.5e-3 / 1e12) < 1e-9
     assert abs(r["peak"] - 152 * 256 * 2070e6 / 1e12) < 1e-9 and 0 < r["frac"] < 1
     assert bench.fp32_roofline(1000, 10, 5.0, None, None)["frac"] is None
+
+
+def test_reference_arm_loads_no_product_library():
+    """bench.py --impl reference runs the CPU port only: after a small run the
+    process has not mapped libpbf.so (the product's CUDA library)."""
+    import subprocess
+
+    code = ("import sys; sys.argv = ['bench.py']; import bench; "
+            "bench.main(['--impl', 'reference', '--scene', 'dam_break', '--steps', '2', '--warmup', '3', "
+            "'--cpu-budget', '1']); "
+            "maps = open('/proc/self/maps').read(); "
+            "assert 'libpbf' not in maps, 'libpbf mapped'; print('NO_LIBPBF')")
+    r = subprocess.run([sys.executable, "-c", code], cwd=str(ROOT), capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "NO_LIBPBF" in r.stdout
+    line = [l for l in r.stdout.splitlines() if l.startswith("{")][0]
+    import json
+
+    d = json.loads(line)
+    assert d["impl"] == "reference" and d["steps"] >= 1 and d["warmup"] == 3
+    assert d["steps_timed"][0] == 4

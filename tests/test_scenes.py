@@ -136,3 +136,12 @@ def test_reference_double_dam_oracle_step(pbf, oracle):
     r64 = oracle.step(sc.params, sc.ulim, sc.llim, sc.pos.astype(np.float64), sc.vel.astype(np.float64), iid, "f64")
     np.testing.assert_array_equal(r32["iid"], r64["iid"])
     assert np.abs(r32["npos"][:, :3] - r64["npos"][:, :3]).max() < 1e-3
+
+
+def test_reference_params_match_the_library_defaults(pbf):
+    """scenes.reference_params (no library) and pbf_params_default agree bit for bit."""
+    import ctypes
+
+    a, b = pbf.scenes.reference_params(), pbf.default_params()
+    assert ctypes.string_at(ctypes.addressof(a), ctypes.sizeof(a)) == \
+        ctypes.string_at(ctypes.addressof(b), ctypes.sizeof(b))
