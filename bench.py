@@ -393,7 +393,7 @@ def tune(sim, st, n, args):
     if not args.tune:
         return None
     t = sim.autotune(st.pos, st.vel, st.iid, n, steps=3)
-    return {"dense_window": int(t["dense_window"]), "dense_all": int(t["dense_all"]),
+    return {"dense_window": int(t["dense_window"]), "dense_all": int(t["dense_all"]), "order": int(t["order"]),
             "trial_ms_per_step": round(float(t["ms_per_step"]), 4),
             "trial_ms_per_step_default": round(float(t["ms_default"]), 4)}
 

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 2
+#define PBF_ABI_VERSION 3
 
 /* Largest max_particles of a solver, and largest total of a batch: 2^27.
  * The solver's per-particle tables are indexed with 32-bit integers, the
@@ -245,31 +245,35 @@ pbf_status pbf_batch_use_graphs(pbf_batch* b, int on);
 /*
  * Autotuning (no counterpart in the reference).  Times a few choices of how
  * the neighbour passes split their work -- the window size above which a
- * warp's 32 particles take the dense kernel (a block of 8 warps splitting
- * each window), and whether every warp does -- by running `steps` steps per
+ * particle's window goes to the dense kernel (a block of 8 warps splitting
+ * the windows of 32 particles), whether every particle does, and the order in
+ * which the passes take particles (the cell order of the grid, or the cell
+ * each particle is in at that iteration) -- by running `steps` steps per
  * choice from copies of the caller's state (pos, vel, iid: device, n entries;
  * they are not modified), and keeps the fastest for the solver's following
- * steps.  The choices change the order in which window sums are added, so
- * results differ by rounding only.  The trial steps are not taped.  The cell
- * size stays h: with the reference's stale grid, another cell size would
- * change which neighbours a step sees.
+ * steps.  The window and dense choices change the order in which window sums
+ * are added, so results differ by rounding only; the particle order changes
+ * nothing (each particle's sums are the same whichever warp computes them).
+ * The trial steps are not taped.  The cell size stays h: with the reference's
+ * stale grid, another cell size would change which neighbours a step sees.
  */
 typedef struct pbf_tuning {
-  int dense_window;   /* candidates above which a warp takes the dense kernel */
-  int dense_all;      /* 1: every warp takes the dense kernel */
+  int dense_window;   /* window entries above which a particle takes the dense kernel */
+  int dense_all;      /* 1: every particle takes the dense kernel */
   float ms_per_step;  /* the chosen configuration's time per step */
   float ms_default;   /* the default configuration's time per step */
+  int order;          /* 1: current-cell order (the default); 0: grid order */
 } pbf_tuning;
 
 pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
                         pbf_tuning* out, void* stream);
 pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, const uint32_t* iid, int steps,
                               pbf_tuning* out, void* stream);
-/* The dense-kernel choice of the following steps, set directly (e.g. a choice
- * an earlier pbf_autotune returned): dense_window >= 32 candidates, or 0 for
- * the default; dense_all 1 (every warp dense), 0 (by window) or -1 (the
- * default: every warp dense below 131072 particles).  ms fields are ignored
- * on set and 0 on get. */
+/* The choices of the following steps, set directly (e.g. a choice an earlier
+ * pbf_autotune returned): dense_window >= 32 candidates, or 0 for the
+ * default; dense_all 1 (every particle dense), 0 (by window) or -1 (the
+ * default: every particle dense below 131072 particles); order 1, 0 or -1
+ * (the default, 1).  ms fields are ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
 

@@ -71,9 +71,10 @@ struct pbf_solver {
   unsigned long long* bw8;   // 2 * max_particles: packed grid cells, packed current cells
   float* wall_part;          // 6 * blocks
   const uint32_t* last_perm;
-  // dense-kernel choices (pbf_autotune); tune_window 0: the defaults
+  // dense-kernel and order choices (pbf_autotune); tune_window 0 / tune_order -1: the defaults
   int tune_window;
   int tune_all;
+  int tune_order;
 };
 
 namespace {
@@ -217,6 +218,7 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   c.dense_grid = 4 * (num_sms > 0 ? num_sms : 1);
   c.dense_window = pbf::kDefaultDenseWindow;
   c.dense_all = -1;
+  c.order = 1;
   return c;
 }
 
@@ -289,6 +291,16 @@ cudaError_t alloc_groups(pbf::SolverScratch& sol, int max_particles) {
   return e;
 }
 
+// Current-cell buckets (StepConsts::order) for up to np particles and nc - 1 cells.
+cudaError_t alloc_buckets(pbf::SolverScratch& sol, size_t np, size_t nc) {
+  cudaError_t e = alloc(&sol.bcnt, nc);
+  if (e == cudaSuccess) e = alloc(&sol.bstart, nc);
+  if (e == cudaSuccess) e = alloc(&sol.bent, np);
+  if (e == cudaSuccess) e = alloc(&sol.bucket, np);
+  if (e == cudaSuccess) e = alloc(&sol.bpart, (size_t)pbf::kMaxScanPartials);
+  return e;
+}
+
 void free_all(pbf_solver* s) {
   void* ptrs[] = {s->grid.keys_a, s->grid.keys_b, s->grid.vals_a, s->grid.vals_b,
                   s->grid.cell_count, s->grid.cell_start, s->grid.radix_counts,
@@ -298,7 +310,8 @@ void free_all(pbf_solver* s) {
                   s->sol.grp_pos, s->sol.grp_sum, s->sol.grp_aux, s->sol.grp_id, s->sol.grp_hash,
                   s->sol.grp_max, s->sol.grp_acc, s->sol.grp_list, s->sol.grp_list_n, s->sol.grp_done,
                   s->sol.grp_zero, s->sol.grp_item_off, s->sol.grp_item_slot, s->sol.work_list,
-                  s->sol.work_follow, s->sol.work_blocks};
+                  s->sol.work_follow, s->sol.work_blocks, s->sol.bcnt, s->sol.bstart, s->sol.bent,
+                  s->sol.bucket, s->sol.bpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -382,6 +395,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (!s) return fail(PBF_ERR_CAPACITY, "host allocation failed");
   std::memset(s, 0, sizeof(*s));
   s->tune_all = -1;
+  s->tune_order = -1;
   s->params = *params;
   std::memcpy(s->ulim, ulim, sizeof(s->ulim));
   std::memcpy(s->llim, llim, sizeof(s->llim));
@@ -410,6 +424,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   s->sol.mask_stride = (int)np;
   if (e == cudaSuccess) e = alloc(&s->sol.cell_flags, nc);
   if (e == cudaSuccess) e = alloc_groups(s->sol, max_particles);
+  if (e == cudaSuccess) e = alloc_buckets(s->sol, np, nc);
   if (e == cudaSuccess) s->num_sms = current_sms();
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
   s->use_graph = true;
@@ -639,6 +654,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   P.c = make_consts(s->params, s->ulim, s->llim, dims, s->num_sms);
   if (s->tune_window > 0) P.c.dense_window = s->tune_window;
   P.c.dense_all = s->tune_all;
+  if (s->tune_order >= 0) P.c.order = s->tune_order;
   P.G = pbf::Geometry{nullptr, nullptr};
   P.grid = &s->grid;
   P.sol = &s->sol;
@@ -667,7 +683,8 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
   s->last_launches = s->last_grid_launches + 1 + pbf::pass_launches(c, n) * (2 * niter + 1) +
-                     pbf::group_launches(c, n, niter) + (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
+                     pbf::group_launches(c, n, niter) + pbf::bucket_launches(c, niter) +
+                     (c.vort_eps > 0.f ? pbf::kVorticityLaunches : 0);
   if (prof) s->prof_iters = niter < kMaxProfiledIters ? niter : kMaxProfiledIters;
   s->last_n = n;
   if (taping) {
@@ -906,8 +923,9 @@ struct pbf_batch {
   bool use_graph;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
-  int tune_window = 0;  // dense-kernel choices (pbf_batch_autotune); 0: the defaults
+  int tune_window = 0;  // dense-kernel and order choices (pbf_batch_autotune); 0 / -1: the defaults
   int tune_all = -1;
+  int tune_order = -1;
 };
 
 namespace {
@@ -921,7 +939,8 @@ void batch_free(pbf_batch* b) {
                   b->sol.grp_pos, b->sol.grp_sum, b->sol.grp_aux, b->sol.grp_id, b->sol.grp_hash,
                   b->sol.grp_max, b->sol.grp_acc, b->sol.grp_list, b->sol.grp_list_n, b->sol.grp_done,
                   b->sol.grp_zero, b->sol.grp_item_off, b->sol.grp_item_slot, b->sol.work_list,
-                  b->sol.work_follow, b->sol.work_blocks, b->d_geom, b->d_sid};
+                  b->sol.work_follow, b->sol.work_blocks, b->sol.bcnt, b->sol.bstart, b->sol.bent,
+                  b->sol.bucket, b->sol.bpart, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);
@@ -1007,6 +1026,7 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
   b->sol.mask_stride = (int)np;
   if (e == cudaSuccess) e = alloc(&b->sol.cell_flags, nc);
   if (e == cudaSuccess) e = alloc_groups(b->sol, (int)np);
+  if (e == cudaSuccess) e = alloc_buckets(b->sol, np, nc);
   if (e == cudaSuccess) e = alloc(&b->d_geom, (size_t)nscenes);
   if (e == cudaSuccess) e = alloc(&b->d_sid, np);
   if (e == cudaSuccess) {
@@ -1083,6 +1103,7 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   P.c.cells = (int)cells;
   if (b->tune_window > 0) P.c.dense_window = b->tune_window;
   P.c.dense_all = b->tune_all;
+  if (b->tune_order >= 0) P.c.order = b->tune_order;
   P.G = pbf::Geometry{b->d_geom, b->d_sid};
   P.grid = &b->grid;
   P.sol = &b->sol;
@@ -1190,7 +1211,8 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   pbf_status result = PBF_OK;
   float best = -1.f, def_ms = -1.f;
-  int best_w = pbf::kDefaultDenseWindow, best_all = -1;
+  int best_w = pbf::kDefaultDenseWindow, best_all = -1, best_ord = 1;
+  for (int ord = 1; ord >= 0 && e == cudaSuccess && result == PBF_OK; --ord)
   for (int all = 0; all <= 1 && e == cudaSuccess && result == PBF_OK; ++all) {
     for (int w : kTuneWindows) {
       if (all == 1 && w != pbf::kDefaultDenseWindow) continue;  // the window plays no part then
@@ -1202,7 +1224,7 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
       float ms = 0.f;
       for (int k = -1; k < steps && result == PBF_OK; ++k) {  // one untimed step first
         if (k == 0) e = cudaEventRecord(e0, st);
-        result = step(w, all, p[cur], p[1 - cur], v[cur], v[1 - cur], id, st);
+        result = step(w, all, ord, p[cur], p[1 - cur], v[cur], v[1 - cur], id, st);
         cur = 1 - cur;
       }
       if (result != PBF_OK) break;
@@ -1211,12 +1233,14 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
       if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
       if (e != cudaSuccess) break;
       ms /= (float)steps;
-      const bool is_default = w == pbf::kDefaultDenseWindow && all == (n < pbf::kDenseAllBelow ? 1 : 0);
+      const bool is_default =
+          ord == 1 && w == pbf::kDefaultDenseWindow && all == (n < pbf::kDenseAllBelow ? 1 : 0);
       if (is_default) def_ms = ms;
       if (best < 0.f || ms < best) {
         best = ms;
         best_w = w;
         best_all = all;
+        best_ord = ord;
       }
     }
   }
@@ -1228,6 +1252,7 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
   if (e != cudaSuccess) return cuda_fail(e, "pbf_autotune");
   out->dense_window = best_w;
   out->dense_all = best_all;
+  out->order = best_ord;
   out->ms_per_step = best;
   out->ms_default = def_ms;
   return PBF_OK;
@@ -1244,12 +1269,13 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
   if (n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
   const int depth = s->tape_depth, top = s->tape_top;
   s->tape_depth = 0;  // the trial steps are not taped
-  const int w0 = s->tune_window, a0 = s->tune_all;
+  const int w0 = s->tune_window, a0 = s->tune_all, o0 = s->tune_order;
   const pbf_status st = autotune(
       n, pos, vel, iid, steps, (cudaStream_t)stream,
-      [&](int w, int all, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+      [&](int w, int all, int ord, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
         s->tune_window = w;
         s->tune_all = all;
+        s->tune_order = ord;
         return pbf_step(s, p, np, v, nv, id, n, strm);
       },
       out);
@@ -1258,10 +1284,12 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
   if (st != PBF_OK) {
     s->tune_window = w0;
     s->tune_all = a0;
+    s->tune_order = o0;
     return st;
   }
   s->tune_window = out->dense_window;
   s->tune_all = out->dense_all;
+  s->tune_order = out->order;
   return PBF_OK;
 }
 
@@ -1271,8 +1299,11 @@ pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
     return fail(PBF_ERR_INVALID_ARG, "dense_window must be 0 (default) or >= 32 (got %d)", t->dense_window);
   if (t->dense_all < -1 || t->dense_all > 1)
     return fail(PBF_ERR_INVALID_ARG, "dense_all must be -1, 0 or 1 (got %d)", t->dense_all);
+  if (t->order < -1 || t->order > 1)
+    return fail(PBF_ERR_INVALID_ARG, "order must be -1, 0 or 1 (got %d)", t->order);
   s->tune_window = t->dense_window;
   s->tune_all = t->dense_all;
+  s->tune_order = t->order;
   return PBF_OK;
 }
 
@@ -1280,6 +1311,7 @@ pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
   if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
   t->dense_window = s->tune_window > 0 ? s->tune_window : pbf::kDefaultDenseWindow;
   t->dense_all = s->tune_all;
+  t->order = s->tune_order >= 0 ? s->tune_order : 1;
   t->ms_per_step = 0.f;
   t->ms_default = 0.f;
   return PBF_OK;
@@ -1289,22 +1321,25 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
                               pbf_tuning* out, void* stream) {
   const pbf::NvtxRange range("pbf_batch_autotune");
   if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
-  const int w0 = b->tune_window, a0 = b->tune_all;
+  const int w0 = b->tune_window, a0 = b->tune_all, o0 = b->tune_order;
   const pbf_status st = autotune(
       b->n, pos, vel, iid, steps, (cudaStream_t)stream,
-      [&](int w, int all, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+      [&](int w, int all, int ord, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
         b->tune_window = w;
         b->tune_all = all;
+        b->tune_order = ord;
         return pbf_batch_step(b, p, np, v, nv, id, strm);
       },
       out);
   if (st != PBF_OK) {
     b->tune_window = w0;
     b->tune_all = a0;
+    b->tune_order = o0;
     return st;
   }
   b->tune_window = out->dense_window;
   b->tune_all = out->dense_all;
+  b->tune_order = out->order;
   return PBF_OK;
 }
 

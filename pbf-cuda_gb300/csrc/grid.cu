@@ -117,6 +117,9 @@ k_scan_down(const uint32_t* in, int len, const uint32_t* __restrict__ partials, 
   }
 }
 
+
+}  // namespace
+
 cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, int len, uint32_t* partials,
                            cudaStream_t stream) {
   const int tiles = (len + kScanTile - 1) / kScanTile;
@@ -126,6 +129,8 @@ cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, int len, uint32_t*
   k_scan_down<<<tiles, kScanThreads, 0, stream>>>(in, len, partials, out);
   return cudaGetLastError();
 }
+
+namespace {
 
 // ---- predict + hash ---------------------------------------------------------------
 

@@ -70,7 +70,7 @@ constexpr size_t kOffLambda = kOffIid + align_up(4 * kNp);
 constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
 constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
 constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
-constexpr size_t kOffMasks = kOffDense + align_up(4 * (kNp / 32 + 1));
+constexpr size_t kOffMasks = kOffDense + align_up(4 * pbf::dense_list_len(kNoAllocMaxParticles));
 constexpr size_t kOffCellFlags = kOffMasks + align_up(4 * (size_t)pbf::kMaskWords * kNp);
 constexpr size_t kSlots = (size_t)kNoAllocMaxParticles / pbf::kGroupCell + 1;
 constexpr size_t kEntries = kNp;
@@ -96,7 +96,12 @@ constexpr size_t kOffGrpItemSlot = kOffGrpItemOff + align_up(4 * kSlots);
 constexpr size_t kOffWorkList = kOffGrpItemSlot + align_up(4 * kItems);
 constexpr size_t kOffWorkFollow = kOffWorkList + align_up(4 * (kNp + 1));
 constexpr size_t kOffWorkBlocks = kOffWorkFollow + align_up(4 * (kNp + 1));
-constexpr size_t kNoAllocScratchBytes = kOffWorkBlocks + align_up(4 * pbf::work_blocks_len(kNoAllocMaxParticles));
+constexpr size_t kOffBcnt = kOffWorkBlocks + align_up(4 * pbf::work_blocks_len(kNoAllocMaxParticles));
+constexpr size_t kOffBstart = kOffBcnt + align_up(4 * kNc);
+constexpr size_t kOffBent = kOffBstart + align_up(4 * kNc);
+constexpr size_t kOffBucket = kOffBent + align_up(8 * kNp);
+constexpr size_t kOffBpart = kOffBucket + align_up(4 * kNp);
+constexpr size_t kNoAllocScratchBytes = kOffBpart + align_up(4 * (size_t)pbf::kMaxScanPartials);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -182,6 +187,11 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   s.work_list = (int*)(base + kOffWorkList);
   s.work_follow = (int*)(base + kOffWorkFollow);
   s.work_blocks = (int*)(base + kOffWorkBlocks);
+  s.bcnt = (uint32_t*)(base + kOffBcnt);
+  s.bstart = (uint32_t*)(base + kOffBstart);
+  s.bent = (uint2*)(base + kOffBent);
+  s.bucket = (int*)(base + kOffBucket);
+  s.bpart = (uint32_t*)(base + kOffBpart);
 
   cudaStream_t strm = (cudaStream_t)stream;
   cudaError_t e;

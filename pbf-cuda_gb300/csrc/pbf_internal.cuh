@@ -57,6 +57,7 @@ struct StepConsts {
   int dense_grid;          // blocks of the dense neighbour kernels (a multiple of the SM count)
   int dense_window;        // candidates above which a warp takes the dense kernel
   int dense_all;           // 1: every warp takes the dense kernel; 0: never; -1: by particle count
+  int order;               // 1: the passes take particles in current-cell order (bucketed); 0: grid order
   SceneGeom geom;          // the box of a single-scene step
 };
 
@@ -176,7 +177,7 @@ struct SolverScratch {
   float* lambda;
   float* rho;
   uint32_t* flags;     // [kNumFlags] per-step flags and dense-list counters, zeroed by reorder
-  uint32_t* dense;     // [dense_list_len(max_particles)] warps handed to the dense kernels
+  uint32_t* dense;     // [dense_list_len(max_particles)] work slots handed to the dense kernels
   uint32_t* masks;     // [kMaskWords][mask_stride] the lambda pass's neighbour masks
   int mask_stride;     // >= particles
   uint32_t* cell_flags;         // [max_cells + 1] CellFlag bits per cell, zeroed by reorder
@@ -211,6 +212,13 @@ struct SolverScratch {
   int* work_list;      // [max_particles]
   int* work_follow;    // [max_particles] -1, or the sorted slot whose results particle i takes
   int* work_blocks;    // [work_blocks_len(max_particles)] per-block counts, then offsets
+  // current-cell order (StepConsts::order): the computing particles of a pass
+  // bucketed by the cell they are in now
+  uint32_t* bcnt;      // [max_cells + 1] particles per current cell
+  uint32_t* bstart;    // [max_cells + 1] exclusive prefix of bcnt
+  uint2* bent;         // [max_particles] (current cell, rank in it) of each computing particle
+  int* bucket;         // [max_particles] the computing particles, bucket by bucket
+  uint32_t* bpart;     // [kMaxScanPartials] scan partials
 };
 
 // Lambda and delta_p results are the same for every particle of a position
@@ -274,11 +282,12 @@ enum StepFlag {
   kWorkCount = 7,            // particles on the current iteration's work list
   kWorkDone = 8,             // blocks of the work-list count finished (0 between uses)
   kWorkIdentity = 9,         // 1: no grouped cell this step, the passes take every particle in order
-  kNumFlags = 10
+  kBucketCount = 10,         // particles in the current buckets
+  kNumFlags = 11
 };
 
-// Entries of the dense list: one per warp of 32 consecutive particles.
-inline size_t dense_list_len(int max_particles) { return (size_t)max_particles / 32 + 1; }
+// Entries of the dense list: one per particle.
+constexpr size_t dense_list_len(int max_particles) { return (size_t)max_particles + 1; }
 
 // Gather pos/vel/iid into cell order and recompute x* (bit-identical to the hash).
 cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
@@ -379,6 +388,15 @@ cudaError_t density_grid_backward(const float4* pos, int n, const float lo[3], c
 cudaError_t backward(const BackwardArgs& args, const BackwardTape& tape, const uint32_t* perm,
                      const void* g_npos, const void* g_nvel, void* g_pos, void* g_vel, float* g_lim,
                      cudaStream_t stream);
+
+// Exclusive prefix of in[0, len) into out (may alias in): 3 launches,
+// partials holds kMaxScanPartials entries.
+cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, int len, uint32_t* partials, cudaStream_t stream);
+
+// Launches (and memset nodes) of one bucketing by current cell; an ordered
+// step buckets before every lambda pass and before XSPH.
+constexpr int kBucketLaunches = 6;
+inline int bucket_launches(const StepConsts& c, int niter) { return c.order ? kBucketLaunches * (niter + 1) : 0; }
 
 // Kernel launches of one build_grid call with n particles and c.cells cells.
 int grid_launches(const StepConsts& c, int n);

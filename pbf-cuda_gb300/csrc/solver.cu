@@ -102,17 +102,21 @@ struct PassArgs {
   const float4* grp_pos;
   const float4* grp_sum;
   const float4* grp_aux;
-  // work list of the lambda / delta_p passes (null: every particle, in order);
-  // its length is flags[kWorkCount]
+  // the particles the pass computes: list[0, flags[count_word]) (null: every
+  // particle, in order); the work list of the lambda / delta_p passes, or the
+  // current-cell buckets.  identity_word >= 0: a flag saying the list is the
+  // identity (every particle in order)
   const int* list;
+  int count_word;
+  int identity_word;
 };
 
 // The particle that thread slot t of a pass computes (t < work_count(a)).
 __device__ __forceinline__ int work_count(const PassArgs& a) {
-  return a.list ? (int)a.flags[kWorkCount] : a.n;
+  return a.list ? (int)a.flags[a.count_word] : a.n;
 }
 __device__ __forceinline__ int work_particle(const PassArgs& a, int t) {
-  return a.list && !a.flags[kWorkIdentity] ? __ldg(a.list + t) : t;
+  return a.list && !(a.identity_word >= 0 && a.flags[a.identity_word]) ? __ldg(a.list + t) : t;
 }
 
 // ---- windows ------------------------------------------------------------------------
@@ -739,11 +743,20 @@ __device__ __forceinline__ void sparse_slot(const PassArgs& a, int t, int count)
   // under it is walked here, group by group (no masks)
   const bool grouped = valid && total > a.c.dense_window && a.c.keps2 > 0.f;
   const int entries = grouped ? window_total_grouped(g, a, q) : total;
-  if (__any_sync(kFull, entries > a.c.dense_window)) {
-    if ((threadIdx.x & 31) == 0) a.dense[atomicAdd(&a.flags[a.counter], 1u)] = (uint32_t)(t >> 5);
-    return;
+  // a window over dense_window entries goes to the dense kernel, particle by
+  // particle (one list slot each, warp-aggregated): which kernel sums a
+  // particle's window depends on its own window only, so results do not
+  // depend on the list's order or on the particle's warp-mates
+  const bool go_dense = valid && entries > a.c.dense_window;
+  const unsigned dmask = __ballot_sync(kFull, go_dense);
+  if (dmask) {
+    const int lane = threadIdx.x & 31, leader = __ffs(dmask) - 1;
+    uint32_t base = 0u;
+    if (lane == leader) base = atomicAdd(&a.flags[a.counter], (uint32_t)__popc(dmask));
+    base = __shfl_sync(kFull, base, leader);
+    if (go_dense) a.dense[base + __popc(dmask & ((1u << lane) - 1u))] = (uint32_t)t;
   }
-  if (!valid) return;
+  if (!valid || go_dense) return;
   const bool exact = exact_path(kKind, a, g, q, i);
   P p(a, g, xi, i, exact);
   if (grouped) {
@@ -786,12 +799,14 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   static_assert(P::kFields <= kMaxFields, "partial-sum fields");
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
-  // the warps the sparse kernel listed, or all of them
+  // the slots the sparse kernel listed, or all of them, 32 per item
   const int work = work_count(a);
-  const uint32_t count = a.dense_all ? (uint32_t)((work + 31) / 32) : a.flags[a.counter];
+  const uint32_t listed = a.dense_all ? (uint32_t)work : a.flags[a.counter];
+  const uint32_t count = (listed + 31) / 32;
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
-    const int t = (int)(a.dense_all ? item : a.dense[item]) * 32 + lane;
-    const bool valid = t < work;
+    const uint32_t e = item * 32 + lane;
+    const bool valid = e < listed;
+    const int t = valid ? (int)(a.dense_all ? e : a.dense[e]) : 0;
     const int i = valid ? work_particle(a, t) : 0;
     const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
@@ -1367,6 +1382,36 @@ k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __re
   }
 }
 
+// ---- current-cell order ---------------------------------------------------------------
+
+// The pass's computing particles (its list, or every particle) by the cell
+// they are in now: count (integer atomics: the counts are exact, the rank
+// inside a cell is arbitrary), exclusive scan over cells, scatter.  Consecutive
+// particles of the resulting list mostly share a window, so a warp's lanes
+// load the same candidates and run similar loops.  A particle's result does
+// not depend on its place in the list (sparse / dense routing is per
+// particle), so the arbitrary ranks leave results bitwise reproducible.
+__global__ void __launch_bounds__(256) k_bucket_count(PassArgs a, uint32_t* __restrict__ bcnt,
+                                                      uint2* __restrict__ bent) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int count = work_count(a);
+  if (t == 0) a.flags[kBucketCount] = (uint32_t)count;
+  if (t >= count) return;
+  const int i = work_particle(a, t);
+  const SceneGeom g = geom_of(a.c, a.G, i);
+  const int3 q = cell_of(a.c, g, a.X[i]);
+  const uint32_t cell = (uint32_t)cell_index(g, q.x, q.y, q.z);
+  bent[t] = make_uint2(cell, atomicAdd(&bcnt[cell], 1u));
+}
+
+__global__ void __launch_bounds__(256) k_bucket_scatter(PassArgs a, const uint32_t* __restrict__ bstart,
+                                                        const uint2* __restrict__ bent, int* __restrict__ bucket) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= work_count(a)) return;
+  const uint2 e = bent[t];
+  bucket[bstart[e.x] + e.y] = work_particle(a, t);
+}
+
 GroupArgs group_args(const SolverScratch& s, const float4* X, const float4* V, int n) {
   GroupArgs a;
   a.X = X;
@@ -1439,7 +1484,31 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.grp_pos = s.grp_pos;
   a.grp_sum = s.grp_sum;
   a.grp_aux = s.grp_aux;
+  a.count_word = kWorkCount;
+  a.identity_word = kWorkIdentity;
   return a;
+}
+
+// Makes the pass take its computing particles in current-cell order: buckets
+// them (kBucketLaunches launches) and points the pass at the buckets.
+cudaError_t bucket_by_cell(PassArgs& a, const SolverScratch& s, int n, cudaStream_t stream) {
+  cudaError_t e = cudaMemsetAsync(s.bcnt, 0, sizeof(uint32_t) * (a.c.cells + 1), stream);
+  if (e != cudaSuccess) return e;
+  const int blocks = (n + 255) / 256;
+  k_bucket_count<<<blocks, 256, 0, stream>>>(a, s.bcnt, s.bent);
+  if ((e = exclusive_scan(s.bcnt, s.bstart, a.c.cells + 1, s.bpart, stream)) != cudaSuccess) return e;
+  k_bucket_scatter<<<blocks, 256, 0, stream>>>(a, s.bstart, s.bent, s.bucket);
+  a.list = s.bucket;
+  a.count_word = kBucketCount;
+  a.identity_word = -1;
+  return cudaGetLastError();
+}
+
+// The delta_p passes of an iteration take the lambda pass's buckets (same positions).
+void use_buckets(PassArgs& a, const SolverScratch& s) {
+  a.list = s.bucket;
+  a.count_word = kBucketCount;
+  a.identity_word = -1;
 }
 
 template <int kKind>
@@ -1497,6 +1566,7 @@ cudaError_t launch_lambda(const StepConsts& c, const Geometry& G, const float4* 
   if (wl && (e = launch_work_list(s, n, stream)) != cudaSuccess) return e;
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   if (wl) a.list = s.work_list;
+  if (c.order && (e = bucket_by_cell(a, s, n, stream)) != cudaSuccess) return e;
   if ((e = run_pass<kLambda>(a, stream)) != cudaSuccess) return e;
   return wl ? launch_follow<kLambda>(c, s, X, n, nullptr, nullptr, nullptr, nullptr, nullptr, stream) : cudaSuccess;
 }
@@ -1509,6 +1579,7 @@ cudaError_t launch_delta_p(const StepConsts& c, const Geometry& G, const float4*
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.T = T;
   if (wl) a.list = s.work_list;
+  if (c.order) use_buckets(a, s);
   if ((e = run_pass<kDeltaP>(a, stream)) != cudaSuccess) return e;
   return wl ? launch_follow<kDeltaP>(c, s, X, n, T, nullptr, nullptr, nullptr, nullptr, stream) : cudaSuccess;
 }
@@ -1527,6 +1598,7 @@ cudaError_t launch_delta_p_final(const StepConsts& c, const Geometry& G, const f
   a.pos = pos;
   a.iid = iid;
   if (wl) a.list = s.work_list;
+  if (c.order) use_buckets(a, s);
   if ((e = run_pass<kDeltaPFinal>(a, stream)) != cudaSuccess) return e;
   return wl ? launch_follow<kDeltaPFinal>(c, s, X, n, nullptr, pos, npos, vel, iid, stream) : cudaSuccess;
 }
@@ -1630,6 +1702,7 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
   PassArgs a = base_args(c, G, X, cs, n, s, pass);
   a.V = V;
   a.NV = NV;
+  if (c.order && (e = bucket_by_cell(a, s, n, stream)) != cudaSuccess) return e;
   return run_pass<kXsph>(a, stream);
 }
 
