@@ -7,9 +7,11 @@ FP32 code, so long runs are compared through statistics: per step, over the
 particles, the mean and the max of the compression part max(C_i, 0) of the
 constraint C_i = rho_i / rho0 - 1, with rho_i from the step's last lambda
 pass.  Needs a GPU and oracle/_ref/ref_kernels.cubin (built where the
-reference sources are; see oracle/ref_harness).  Usage:
+reference sources are; see oracle/ref_harness).  Cases: the 8,000-particle
+dam break and the 32,768-particle double dam break, each with the dam-break
+parameters and with the reference's own defaults.  Usage:
 
-    python tests/golden/make_stats.py [out_dir]
+    python tests/golden/make_stats.py [out_dir [case ...]]
 """
 from __future__ import annotations
 
@@ -33,17 +35,24 @@ def constraint_stats(rho: np.ndarray, rho0: float):
 
 
 SEEDS = tuple(range(32))
+# seeds of each case (lattice jitter); the 32K double dam runs fewer
+CASE_SEEDS = {"dam8k_sceneparams": SEEDS, "dam8k_refparams": SEEDS,
+              "ddam32k_sceneparams": tuple(range(8)), "ddam32k_refparams": tuple(range(8))}
 
 
 def cases(pbf, seed=0):
-    """The 8,000-particle dam break (lattice jitter from ``seed``) with the
-    dam-break parameters and with the reference's own defaults (y up)."""
-    sc = pbf.scenes.dam_break(seed=seed)
-    ref_p = pbf.default_params()
+    """The 8,000-particle dam break and the 32,768-particle double dam break
+    (lattice jitter from ``seed``), each with the dam-break parameters and with
+    the reference's own defaults (y up)."""
+    ref_p = pbf.scenes.reference_params()
     ref_p.up[0], ref_p.up[1], ref_p.up[2] = 0.0, 1.0, 0.0
+    dam = pbf.scenes.dam_break(seed=seed)
+    ddam = pbf.scenes.double_dam(seed=seed)
     return {
-        "dam8k_sceneparams": (sc.params, sc),
-        "dam8k_refparams": (ref_p, sc),
+        "dam8k_sceneparams": (dam.params, dam),
+        "dam8k_refparams": (ref_p, dam),
+        "ddam32k_sceneparams": (ddam.params, ddam),
+        "ddam32k_refparams": (ref_p, ddam),
     }
 
 
@@ -65,15 +74,17 @@ def main():
     pbf = __graft_entry__.load()
     out_dir = Path(sys.argv[1] if len(sys.argv) > 1 else Path(__file__).resolve().parent)
     out_dir.mkdir(parents=True, exist_ok=True)
-    for name in cases(pbf):
+    names = sys.argv[2:] or list(cases(pbf))
+    for name in names:
         runs = []
-        for seed in SEEDS:
+        seeds = CASE_SEEDS[name]
+        for seed in seeds:
             p, sc = cases(pbf, seed)[name]
             runs.append(run_reference(ref, p, sc))
         runs = np.stack(runs)  # (seeds, steps, [mean C+, max C+, non-finite rho])
         out = out_dir / f"stats_{name}.npz"
-        np.savez_compressed(out, stats=runs, seeds=np.array(SEEDS), steps=np.array(STEPS))
-        for k, seed in enumerate(SEEDS):
+        np.savez_compressed(out, stats=runs, seeds=np.array(seeds), steps=np.array(STEPS))
+        for k, seed in enumerate(seeds):
             print(f"{out.name} seed {seed}: time-mean of mean C+ {runs[k, :, 0].mean():.6g}, "
                   f"of max C+ {runs[k, :, 1].mean():.6g}, steps with non-finite rho "
                   f"{int(np.count_nonzero(runs[k, :, 2]))}")

@@ -10,7 +10,15 @@ bars:
     density within 1e-5 relative, for every case except the chaotic one (dam-break parameters
     at 4 iterations, where FP32 rounding alone moves particles by ~1e-2): there
     the integer outputs, the set of particles left without density, and the
-    set of non-finite velocities must match.
+    set of non-finite velocities must match, and the CUDA path's floats are
+    held to the reference's own float arithmetic as closely as the float port
+    of the reference's kernels is: the median, 90th and 99th percentile of
+    |CUDA - reference kernels| in positions, velocities and densities within
+    1e-5 h (1e-5 h / dt, 1e-5 of the largest density) + 3x the same
+    percentile of |float port - reference kernels| of the same step; the
+    maximum (one worst particle of 1,728) within the floor + 3x the larger of
+    the float port's and the FP64 oracle's maximum (the FP64 restatement is
+    itself 6x farther than the port from the reference's float results there).
 """
 from __future__ import annotations
 
@@ -98,7 +106,7 @@ def test_oracle_step_matches_reference(pbf, oracle, name, prec):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", CASES)
-def test_cuda_step_matches_reference(pbf, cuda, name):
+def test_cuda_step_matches_reference(pbf, oracle, cuda, name):
     import torch
 
     z, p = load_case(pbf, name)
@@ -116,3 +124,29 @@ def test_cuda_step_matches_reference(pbf, cuda, name):
         got["iid"] = got["iid"].astype(np.uint32)
         got["rho"] = rho.cpu().numpy()
         check_against(z, s, got, name, p, f"cuda {name} step {s}")
+        if name in CHAOTIC:
+            port = oracle.step(p, z["ulim"], z["llim"], pos, vel, iid, prec="f32")
+            fp64 = oracle.step(p, z["ulim"], z["llim"], pos, vel, iid, prec="f64")
+            check_port_relative(z, s, got, port, fp64, p, f"cuda {name} step {s}")
+
+
+def check_port_relative(z, s, got, port, fp64, p, what):
+    """Error percentiles of the CUDA path against the reference's kernels
+    within a floor + 3x those of the float port of the same step (the
+    maximum: 3x the larger of the port's and the FP64 oracle's)."""
+    rho_ref = z[f"s{s}_rho"]
+    for k, ref, floor in (("npos", z[f"s{s}_npos"], TOL_X), ("nvel", z[f"s{s}_nvel"], TOL_X / p.dt),
+                          ("rho", rho_ref, 1e-5 * float(rho_ref.max()))):
+        def cols(a):
+            return a[:, :3] if k != "rho" else np.asarray(a)[:, None]
+
+        g, q, f, r = cols(got[k]), cols(port[k]), cols(fp64[k]), cols(ref)
+        fin = np.isfinite(r).all(1)
+        np.testing.assert_array_equal(np.isfinite(g).all(1), fin, err_msg=f"{what}: {k} non-finite set")
+        e_gpu = np.abs(g[fin] - r[fin]).ravel()
+        e_port = np.abs(q[fin] - r[fin]).ravel()
+        for pct in (50, 90, 99):
+            a, b = float(np.percentile(e_gpu, pct)), float(np.percentile(e_port, pct))
+            assert a <= floor + 3 * b, (what, k, pct, a, b)
+        worst = max(float(e_port.max()), float(np.abs(f[fin] - r[fin]).max()))
+        assert float(e_gpu.max()) <= floor + 3 * worst, (what, k, "max", float(e_gpu.max()), worst)

@@ -283,7 +283,11 @@ def test_moving_wall_sequence(pbf, oracle, cuda):
 def test_large_sweep_one_step(pbf, oracle, cuda):
     """1,048,576 particles (the large-sweep lattice), scene parameters, one
     step of 4 iterations: order bit-exact vs the float port, positions finite
-    and inside the box, keys of the output order non-decreasing, deterministic."""
+    and inside the box, keys of the output order non-decreasing, deterministic;
+    and the floats as close to FP64 as the reference-order float port gets:
+    the median, 90th, 99th percentile and maximum of |x - x_fp64| within
+    1e-5 h + 3x the port's (the dam-break parameters make this step
+    ill-conditioned: the port itself is 0.3 off FP64 at its worst particle)."""
     sc = pbf.scenes.large_sweep(seed=0)
     p = sc.params
     got = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
@@ -302,6 +306,14 @@ def test_large_sweep_one_step(pbf, oracle, cuda):
     assert np.all(got["npos"][:, :3] <= np.array(sc.ulim, np.float32) - lo + 1e-6)
     again = gpu_step(pbf, p, sc.ulim, sc.llim, sc.pos, sc.vel)
     np.testing.assert_array_equal(again["npos"], got["npos"])
+    iid = np.arange(sc.n, dtype=np.uint32)
+    r64 = oracle.step(p, sc.ulim, sc.llim, sc.pos, sc.vel, iid, prec="f64")
+    r32 = oracle.step(p, sc.ulim, sc.llim, sc.pos, sc.vel, iid, prec="f32")
+    e_gpu = np.abs(got["npos"][:, :3] - r64["npos"][:, :3]).ravel()
+    e_port = np.abs(r32["npos"][:, :3] - r64["npos"][:, :3]).ravel()
+    for q in (50, 90, 99, 100):
+        a, b = float(np.percentile(e_gpu, q)), float(np.percentile(e_port, q))
+        assert a <= TOL_X + 3 * b, (q, a, b)
 
 
 def test_large_sweep_one_iteration_vs_port(pbf, oracle, cuda):

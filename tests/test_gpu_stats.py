@@ -1,6 +1,7 @@
 """Statistical parity over long runs: 300 frames (600 steps) of the 8,000-particle
-dam break, 32 jitter seeds, against the reference's own kernels
-(tests/golden/stats_*.npz, made by tests/golden/make_stats.py).
+dam break (32 jitter seeds) and of the 32,768-particle double dam break (8
+seeds), against the reference's own kernels (tests/golden/stats_*.npz, made by
+tests/golden/make_stats.py).
 
 Trajectories diverge chaotically (FP32 rounding differences grow, and the
 fluid settles into one of several layered packings), so runs are compared
@@ -44,7 +45,8 @@ def golden_path():
     sys.path.remove(str(GOLDEN))
 
 
-@pytest.mark.parametrize("name", ["dam8k_refparams", "dam8k_sceneparams"])
+@pytest.mark.parametrize("name", ["dam8k_refparams", "dam8k_sceneparams", "ddam32k_refparams",
+                                  "ddam32k_sceneparams"])
 def test_constraint_statistics_match_reference(pbf, cuda, golden_path, name):
     from make_stats import cases
 
@@ -55,7 +57,7 @@ def test_constraint_statistics_match_reference(pbf, cuda, golden_path, name):
     for col, what in ((0, "mean C+"), (1, "max C+")):
         r_seed, o_seed = ref[:, :, col].mean(1), ours[:, :, col].mean(1)
         r, o = r_seed.mean(), o_seed.mean()
-        if name == "dam8k_refparams":
+        if name.endswith("_refparams"):
             assert abs(o / r - 1) <= 0.01, (what, o, r)
         else:
             se = np.sqrt(r_seed.var(ddof=1) / len(seeds) + o_seed.var(ddof=1) / len(seeds))
