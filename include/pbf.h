@@ -278,16 +278,18 @@ pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
 
 /*
- * One step, same contract and results as pbf_step, for callers that cannot
- * allocate device memory (no pbf_solver, so no pbf_create).  It has no
- * counterpart in the reference.  It calls no cudaMalloc or cudaFree: its
- * scratch is a fixed array of about 10.5 MB inside this library's device image,
- * held by every GPU that loads the library until the process exits.
+ * One step, same contract and results as pbf_step (bit for bit, with the
+ * default tuning), for callers that cannot allocate device memory (no
+ * pbf_solver, so no pbf_create).  It has no counterpart in the reference.  It
+ * calls no cudaMalloc or cudaFree: its scratch is a fixed array of about
+ * 11.6 MB inside this library's device image, held by every GPU that loads
+ * the library until the process exits.
  * Limits: n <= 32768 particles and a box of at most 131072 cells at cell size
  * h; larger calls return PBF_ERR_CAPACITY.  The first call on each device
  * looks up the array's device address (set-up), so make it before any stream
- * capture.  Every call shares the array: calls that overlap on the GPU race,
- * so serialise them.
+ * capture; the address is looked up again when the device's context has
+ * changed since (after cudaDeviceReset, for one).  Every call shares the
+ * array: calls that overlap on the GPU race, so serialise them.
  */
 pbf_status pbf_step_noalloc(const pbf_params* params, const float ulim[3], const float llim[3],
                             void* pos, void* npos, void* vel, void* nvel, uint32_t* iid, int n,

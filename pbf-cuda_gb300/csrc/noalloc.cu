@@ -16,10 +16,13 @@
 // PBF_ERR_CAPACITY.  The caller still passes every input and output buffer.
 //
 // Host code cannot use the array's name as a device address (on the host it
-// names a stand-in object).  The device address is looked up once per device
-// with cudaGetSymbolAddress, on the first call made while that device is
-// current, and cached.  That first call therefore does set-up work and should
-// be made before any stream capture.
+// names a stand-in object).  The device address is looked up with
+// cudaGetSymbolAddress on the first call made while a device is current, and
+// cached together with that device's CUDA context; a call that finds another
+// context current on the device (after cudaDeviceReset, say, the module is
+// loaded again and the array may sit elsewhere) looks it up again.  A first
+// call therefore does set-up work and should be made before any stream
+// capture.
 //
 // The array is shared by every call and keeps the last call's contents; the
 // step clears what must start at zero (the per-cell counters and the group
@@ -29,6 +32,8 @@
 //
 // The kernels and their sequence are exactly those of pbf_step; only where the
 // scratch comes from differs.
+#include <cuda.h>  // CUcontext / CUresult: the driver call below is resolved at run time
+
 #include <mutex>
 
 #include "pbf_internal.cuh"
@@ -108,19 +113,48 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void* g_base[kMaxDevices] = {};
+CUcontext g_ctx[kMaxDevices] = {};
 
-// Device address of g_noalloc_scratch on the current device (set-up on first use).
+// The driver's cuCtxGetCurrent, found through the runtime (no link against
+// the driver library); null where it cannot be found.
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+CtxGetCurrent ctx_get_current() {
+  static const CtxGetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      f = nullptr;
+    }
+    return (CtxGetCurrent)f;
+  }();
+  return fn;
+}
+
+CUcontext current_context() {
+  CUcontext c = nullptr;
+  const CtxGetCurrent fn = ctx_get_current();
+  if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+  return c;
+}
+
+// Device address of g_noalloc_scratch on the current device: looked up on the
+// first call with this device's context current, again when another context
+// is current, and on every call when the context cannot be identified.
 pbf_status scratch_base(unsigned char** out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return pbf::set_cuda_error(e, "pbf_step_noalloc: cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return pbf::set_error(PBF_ERR_INVALID_ARG, "pbf_step_noalloc: device index out of range");
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_base[dev]) {
+  CUcontext ctx = current_context();
+  if (!g_base[dev] || !ctx || ctx != g_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return pbf::set_cuda_error(e, "pbf_step_noalloc: cudaGetSymbolAddress");
     g_base[dev] = p;
+    g_ctx[dev] = current_context();  // the lookup makes the device's context current if none was
   }
   *out = (unsigned char*)g_base[dev];
   return PBF_OK;
