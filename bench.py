@@ -272,9 +272,25 @@ def run_ours(args):
         st.step(sim)
         t += p.dt
 
+    if args.load_state:
+        # profiling: the saved state after `warmup` steps, then `steps` untimed steps
+        pos_s, vel_s, iid_s = pkg.scenes.load_state(args.load_state)
+        st = pkg.ParticleState(pos_s, vel_s, iid_s)
+        t = args.warmup * p.dt
+        for _ in range(args.steps):
+            one_step()
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_steps": args.steps, "from_step": args.warmup, "state": str(args.load_state)}))
+        sim.close()
+        return
     for _ in range(args.warmup):
         one_step()
     torch.cuda.synchronize()
+    if args.save_state:
+        pkg.scenes.save_state(args.save_state, st.pos, st.vel, st.iid[:n])
+        print(json.dumps({"saved_after_steps": args.warmup, "state": str(args.save_state)}))
+        sim.close()
+        return
     # the dense-kernel choice, tuned once on the state the timed steps start from
     # (pbf_autotune: trial steps on copies of the state, outside the timed region)
     tuning = tune(sim, st, n, args)
@@ -841,6 +857,11 @@ def main(argv=None):
     ap.add_argument("--cpu-steps", type=int, default=20,
                     help="most steps the CPU baseline times (0: no CPU baseline, for profiling runs)")
     ap.add_argument("--cpu-warmup-steps", type=int, default=8, help="most warm-up steps of the reference arm")
+    ap.add_argument("--save-state", default=None,
+                    help="profiling: after the warm-up steps, save the particle state to this file and exit")
+    ap.add_argument("--load-state", default=None,
+                    help="profiling: start from this state (saved after --warmup steps), run --steps untimed "
+                         "steps and exit (a short command for ncu)")
     ap.add_argument("--no-extras", dest="extras", action="store_false",
                     help="skip the sub-measurements (120/240 window, ensemble, adjoint) of the step workload")
     ap.add_argument("--no-ref-gpu", dest="ref_gpu", action="store_false",

@@ -57,7 +57,12 @@ namespace pbf {
 namespace {
 
 constexpr int kSparseThreads = 128;
-constexpr int kDenseWarps = 8;                  // chunks of a dense warp's windows
+// PBF_DENSE_WARPS (a build-time tuning macro): warps of a dense-kernel block,
+// i.e. the chunks each listed particle's window is split into.
+#ifndef PBF_DENSE_WARPS
+#define PBF_DENSE_WARPS 8
+#endif
+constexpr int kDenseWarps = PBF_DENSE_WARPS;   // chunks of a dense item's windows
 constexpr int kDenseThreads = 32 * kDenseWarps;
 // Below kDenseAllBelow particles one thread per particle leaves most of the
 // GPU idle: by default every warp then takes the dense kernel (8 warps per 32
