@@ -80,14 +80,17 @@ def fp32_roofline(n: int, steps: int, total_ms: float, sms, sm_mhz, niter: int =
             "peak_kind": "nominal: SMs x 128 lanes x 2 x max SM clock"}
 
 
-def ncu_traffic(kernel: str):
-    """dram bytes per launch of ``kernel`` from the committed ncu summary, scaled
-    to the full workload there (line: 'traffic_bytes_per_launch <kernel>: <bytes>')."""
-    for f in sorted((ROOT / "profiles").glob("*.md")):
-        m = re.search(rf"traffic_bytes_per_launch {kernel}: ([0-9.eE+]+)", f.read_text())
-        if m:
-            return float(m.group(1))
-    return None
+TRAFFIC_PROFILE = ROOT / "profiles" / "neighbour_passes_step16_large_sweep_1m.md"
+
+
+def ncu_traffic(kernel: str, path: Path = TRAFFIC_PROFILE):
+    """DRAM bytes per launch of ``kernel``'s pass (sparse + dense kernel, read +
+    write) on the timed regime of this workload, from the committed ncu
+    summary (line: 'traffic_bytes_per_launch <kernel>: <bytes>'), or None."""
+    if not path.exists():
+        return None
+    m = re.search(rf"traffic_bytes_per_launch {kernel}: ([0-9.eE+]+)", path.read_text())
+    return float(m.group(1)) if m else None
 
 
 class ClockSampler:
@@ -401,11 +404,12 @@ def run_ours(args):
 
 
 def tune(sim, st, n, args):
-    """pbf_autotune on the current state (unless --no-tune or --dense-window);
-    returns the choice."""
-    if args.dense_window:
-        sim.set_tuning(args.dense_window, 0)
-        return {"dense_window": args.dense_window, "dense_all": 0, "set": "--dense-window"}
+    """pbf_autotune on the current state (unless --no-tune, --dense-window or
+    --order); returns the choice."""
+    if args.dense_window or args.order is not None:
+        order = -1 if args.order is None else args.order
+        sim.set_tuning(args.dense_window, 0 if args.dense_window else -1, order)
+        return {**sim.tuning(), "set": "--dense-window / --order"}
     if not args.tune:
         return None
     t = sim.autotune(st.pos, st.vel, st.iid, n, steps=3)
@@ -851,6 +855,8 @@ def main(argv=None):
                     help="keep the default dense-kernel choice instead of pbf_autotune after the warm-up")
     ap.add_argument("--dense-window", type=int, default=0,
                     help="set this dense-kernel window after the warm-up instead of tuning (no trial steps)")
+    ap.add_argument("--order", type=int, choices=(0, 1), default=None,
+                    help="set the particle order after the warm-up instead of tuning (1: current cell, 0: grid)")
     ap.add_argument("--e2e-steps", type=int, default=None,
                     help="steps of the end-to-end measurement (default: the timed steps, from the same state)")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-port timing")
