@@ -10,7 +10,9 @@
 // predicted positions, so a pair can be one-sided when a particle crossed a
 // cell boundary during the step's iterations; each pair checks this
 // (near_cell on the packed cells), and i scatters the terms that j cannot
-// gather into fix / fixv with atomics, which small kernels then fold in.
+// gather; they are summed exactly in any order (scatter_term, k_bwd_acc) and
+// small kernels then fold them in, so the reverse pass is bitwise
+// reproducible.
 // Kernels:
 //   W(q) = a (h^2 - q)^3,  W'(q) = -3a (h^2 - q)^2,  q = |r|^2
 //   F(r) = phi(s) r,  phi = b (h - s)^2 / s,  s = |r|        (spiky gradient)
@@ -97,6 +99,121 @@ __device__ __forceinline__ void atomic_add3(float4* p, float x, float y, float z
   atomicAdd(&p->x, x);
   atomicAdd(&p->y, y);
   atomicAdd(&p->z, z);
+}
+
+// ---- exact scattered sums ------------------------------------------------------------
+//
+// A term that particle i cannot leave for j to gather is scattered to j.  Float
+// atomics would add the terms in arrival order, so the result would change
+// from run to run in its last bits; instead every term is listed (any order),
+// each target keeps its term count and its largest finite |term| per component
+// (integer atomics), k_bwd_acc then adds every listed term as a 64-bit integer
+// scaled by 2^sh, sh = 62 - e - bits(count) with the largest |term| < 2^e (so
+// no sum can overflow; integer sums do not depend on the order), and the fold
+// converts back.  Each term is rounded to 2^-sh, at most 2^-62 of the target's
+// largest term times its count: far below float rounding.  Non-finite terms
+// are tracked per component (NaN, +inf, -inf) and give the IEEE sum's NaN or
+// infinity.  Terms beyond the list's capacity go to fix / fixv with float
+// atomics (results then correct but not bitwise reproducible; sc_ctr[1]
+// counts them).
+
+__device__ __forceinline__ int scale_shift(unsigned maxbits, unsigned cnt) {
+  int e = 0;
+  const float mx = __uint_as_float(maxbits);
+  if (mx > 0.f) frexpf(mx, &e);  // mx < 2^e
+  return 62 - e - (32 - __clz(cnt));
+}
+
+__device__ __forceinline__ void note_term(const BackwardArgs& a, int comp, int j, float v) {
+  if (isfinite(v)) {
+    if (v != 0.f) atomicMax(&a.sc_max[comp * a.sc_stride + j], __float_as_uint(fabsf(v)));
+  } else {
+    const unsigned bit = isnan(v) ? 1u : (v > 0.f ? 2u : 4u);
+    atomicOr(&a.sc_nonfin[j], bit << (3 * comp));
+  }
+}
+
+// Scatters (x, y, z, w) to target j: kind 0 (fix: position adjoints xyz and
+// lambda / rho adjoint w) or kind 1 (fixv: velocity adjoints xyz).
+__device__ __forceinline__ void scatter_term(const BackwardArgs& a, int kind, int j, float x, float y, float z,
+                                             float w) {
+  const unsigned slot = atomicAdd(&a.sc_ctr[0], 1u);
+  if (slot >= (unsigned)a.sc_cap) {
+    atomicAdd(&a.sc_ctr[1], 1u);
+    float4* f = kind == 0 ? a.fix : a.fixv;
+    atomic_add3(f + j, x, y, z);
+    if (kind == 0) atomicAdd(&f[j].w, w);
+    return;
+  }
+  a.sc_key[slot] = make_int2(j, kind);
+  a.sc_val[slot] = make_float4(x, y, z, w);
+  atomicAdd(&a.sc_cnt[kind * a.sc_stride + j], 1u);
+  const int base = kind == 0 ? 0 : 4;
+  note_term(a, base, j, x);
+  note_term(a, base + 1, j, y);
+  note_term(a, base + 2, j, z);
+  if (kind == 0) note_term(a, 3, j, w);
+}
+
+// Adds every listed term into its target's fixed-point sums (grid-stride).
+__global__ void __launch_bounds__(256) k_bwd_acc(BackwardArgs a) {
+  const unsigned listed = min(a.sc_ctr[0], (unsigned)a.sc_cap);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < listed; e += gridDim.x * blockDim.x) {
+    const int2 key = a.sc_key[e];
+    const float4 v = a.sc_val[e];
+    const int j = key.x, kind = key.y, base = kind == 0 ? 0 : 4, comps = kind == 0 ? 4 : 3;
+    const unsigned cnt = a.sc_cnt[kind * a.sc_stride + j];
+    const float vs[4] = {v.x, v.y, v.z, v.w};
+    for (int c = 0; c < comps; ++c) {
+      if (!isfinite(vs[c]) || vs[c] == 0.f) continue;
+      const int comp = base + c;
+      const int sh = scale_shift(a.sc_max[comp * a.sc_stride + j], cnt);
+      const long long q = __double2ll_rn(ldexp((double)vs[c], sh));  // |q| < 2^62 / cnt
+      atomicAdd(&a.sc_acc[comp * a.sc_stride + j], (unsigned long long)q);
+    }
+  }
+}
+
+// The exact sum of component `comp` of target j's listed terms, with its
+// scratch set back to zero.
+__device__ __forceinline__ float take_sum(const BackwardArgs& a, int comp, int j, unsigned cnt, unsigned nonfin) {
+  const size_t k = (size_t)comp * a.sc_stride + j;
+  const unsigned bits = (nonfin >> (3 * comp)) & 7u;
+  const unsigned long long acc = a.sc_acc[k];
+  const unsigned mx = a.sc_max[k];
+  a.sc_acc[k] = 0ull;
+  a.sc_max[k] = 0u;
+  if (bits) {
+    if ((bits & 1u) || (bits & 6u) == 6u) return __int_as_float(0x7fffffff);
+    return (bits & 2u) ? __int_as_float(0x7f800000) : __int_as_float((int)0xff800000);
+  }
+  if (cnt == 0u || acc == 0ull) return 0.f;
+  return (float)ldexp((double)(long long)acc, -scale_shift(mx, cnt));
+}
+
+// Target i's scattered sums of `kind` (xyz, and w for fix), its scratch
+// cleared, plus what overflowed into fix / fixv (also cleared).
+__device__ __forceinline__ float4 take_scattered(const BackwardArgs& a, int kind, int i) {
+  const unsigned cnt = a.sc_cnt[kind * a.sc_stride + i];
+  a.sc_cnt[kind * a.sc_stride + i] = 0u;
+  const unsigned nonfin = a.sc_nonfin[i];
+  float4* f = kind == 0 ? a.fix : a.fixv;
+  const float4 o = f[i];
+  f[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int base = kind == 0 ? 0 : 4;
+  float4 s;
+  s.x = take_sum(a, base, i, cnt, nonfin) + o.x;
+  s.y = take_sum(a, base + 1, i, cnt, nonfin) + o.y;
+  s.z = take_sum(a, base + 2, i, cnt, nonfin) + o.z;
+  s.w = kind == 0 ? take_sum(a, 3, i, cnt, nonfin) + o.w : 0.f;
+  return s;
+}
+
+// After a fold: the list is empty again, and each target's non-finite bits
+// of the folded kind are clear.
+__device__ __forceinline__ void clear_nonfin(const BackwardArgs& a, int i, unsigned mask) {
+  const unsigned nf = a.sc_nonfin[i];
+  if (nf & mask) a.sc_nonfin[i] = nf & ~mask;
 }
 
 // L lanes share one particle (L = 1, or a whole warp for small steps, where
@@ -189,9 +306,8 @@ k_bwd_xsph(BackwardArgs a) {
       rb += tr * dr;
     } else {
       // j cannot gather nv_i's term: scatter its adjoint on j's inputs
-      atomic_add3(a.fixv + j, c.c_xsph * w * gi.x, c.c_xsph * w * gi.y, c.c_xsph * w * gi.z);
-      atomic_add3(a.fix + j, -own * dq * r.x, -own * dq * r.y, -own * dq * r.z);
-      atomicAdd(&a.fix[j].w, own * dr);
+      scatter_term(a, 1, j, c.c_xsph * w * gi.x, c.c_xsph * w * gi.y, c.c_xsph * w * gi.z, 0.f);
+      scatter_term(a, 0, j, -own * dq * r.x, -own * dq * r.y, -own * dq * r.z, own * dr);
     }
   }, lane, L);
   vb = lane_sum<L>(vb);
@@ -207,31 +323,34 @@ k_bwd_xsph(BackwardArgs a) {
   a.grho[i] = rb;
 }
 
-// Folds the scattered XSPH adjoints in and clears fix / fixv.
+// Folds the scattered XSPH adjoints in and clears their scratch.
 __global__ void __launch_bounds__(256)
 k_bwd_fix_xsph(BackwardArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) a.sc_ctr[0] = 0u;  // every listed term has been added (k_bwd_acc)
   if (i >= a.n) return;
-  const float4 f = a.fix[i], v = a.fixv[i], g = a.gx[i], g0 = a.gx0[i];
+  const float4 f = take_scattered(a, 0, i), v = take_scattered(a, 1, i);
+  clear_nonfin(a, i, 0x1fffffu);
+  const float4 g = a.gx[i], g0 = a.gx0[i];
   const float t = a.c.inv_dt;
   a.gx[i] = make_float4(g.x + f.x + v.x * t, g.y + f.y + v.y * t, g.z + f.z + v.z * t, 0.f);
   a.gx0[i] = make_float4(g0.x - v.x * t, g0.y - v.y * t, g0.z - v.z * t, 0.f);
   a.grho[i] += f.w;
-  a.fix[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-  a.fixv[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // Folds scattered position adjoints into gx_next (and, with kLambda, the w
-// part into lambdabar) and clears fix.
+// part into lambdabar) and clears their scratch.
 template <bool kLambda>
 __global__ void __launch_bounds__(256)
 k_bwd_fix(BackwardArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) a.sc_ctr[0] = 0u;
   if (i >= a.n) return;
-  const float4 f = a.fix[i], g = a.gx_next[i];
+  const float4 f = take_scattered(a, 0, i);
+  clear_nonfin(a, i, 0xfffu);
+  const float4 g = a.gx_next[i];
   a.gx_next[i] = make_float4(g.x + f.x, g.y + f.y, g.z + f.z, 0.f);
   if (kLambda) a.lbar[i] += f.w;
-  a.fix[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // ---- delta_p -----------------------------------------------------------------------
@@ -351,8 +470,7 @@ k_bwd_dp2(BackwardArgs a, const float4* __restrict__ X, const float* __restrict_
       xb.z -= lsum * Jj.z + 2.f * dsdq * r.z * fj;
     } else {
       // j cannot gather P_i's term: scatter its adjoint on lambda_j and x_j
-      atomic_add3(a.fix + j, -oi.x, -oi.y, -oi.z);
-      atomicAdd(&a.fix[j].w, fi);
+      scatter_term(a, 0, j, -oi.x, -oi.y, -oi.z, fi);
     }
   }, lane, L);
   xb = lane_sum<L>(xb);
@@ -459,7 +577,7 @@ k_bwd_lam2(BackwardArgs a, const float4* __restrict__ X) {
         sz -= Ji.z * c.inv_pho0;
       }
     }
-    if (!recip) atomic_add3(a.fix + j, sx, sy, sz);
+    if (!recip) scatter_term(a, 0, j, sx, sy, sz, 0.f);
   }, lane, L);
   xb = lane_sum<L>(xb);
   if (lane != 0) return;
@@ -600,7 +718,9 @@ cudaError_t run_backward(BackwardArgs a, const BackwardTape& t, const uint32_t* 
                          void* g_vel, float* g_lim, cudaStream_t stream) {
   const int blocks = (int)(((long long)a.n * L + kThreads - 1) / kThreads);
   const int blocks256 = (a.n + 255) / 256;
+  const int acc_blocks = a.c.dense_grid;
   k_bwd_xsph<L><<<blocks, kThreads, 0, stream>>>(a);
+  k_bwd_acc<<<acc_blocks, 256, 0, stream>>>(a);
   k_bwd_fix_xsph<<<blocks256, 256, 0, stream>>>(a);
   for (int k = t.niter - 1; k >= 0; --k) {
     const float4* X = t.X[k];
@@ -608,9 +728,11 @@ cudaError_t run_backward(BackwardArgs a, const BackwardTape& t, const uint32_t* 
     k_bwd_dp1<L><<<blocks, kThreads, 0, stream>>>(a, X, lam);  // also the packed cells of X_k
     k_bwd_wall<<<1, 32, 0, stream>>>(a.wall_part, blocks, g_lim);
     k_bwd_dp2<L><<<blocks, kThreads, 0, stream>>>(a, X, lam);
+    k_bwd_acc<<<acc_blocks, 256, 0, stream>>>(a);
     k_bwd_fix<true><<<blocks256, 256, 0, stream>>>(a);
     k_bwd_lam1<L><<<blocks, kThreads, 0, stream>>>(a, X, lam, k == t.niter - 1);
     k_bwd_lam2<L><<<blocks, kThreads, 0, stream>>>(a, X);
+    k_bwd_acc<<<acc_blocks, 256, 0, stream>>>(a);
     k_bwd_fix<false><<<blocks256, 256, 0, stream>>>(a);
     // the adjoint of X_k becomes the input of the next (earlier) iteration
     float4* tmp = a.gx;

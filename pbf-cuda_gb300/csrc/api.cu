@@ -67,6 +67,7 @@ struct pbf_solver {
     int niter;
   } tape_meta[kMaxTapeDepth];
   float4* bw4;               // 7 * max_particles: gx, gx_next, gx0, pbar, gs, fix, fixv
+  unsigned char* bw_sc;      // the reverse pass's exact-scatter scratch (scatter_bytes)
   float* bw1;                // 4 * max_particles: grho, lbar, rtot (+ spare)
   unsigned long long* bw8;   // 2 * max_particles: packed grid cells, packed current cells
   float* wall_part;          // 6 * blocks
@@ -320,12 +321,33 @@ void free_all(pbf_solver* s) {
     if (e) cudaEventDestroy(e);
   if (s->exec) cudaGraphExecDestroy(s->exec);
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
-  void* tape[] = {s->tape_mem, s->bw4, s->bw1, s->bw8, s->wall_part};
+  void* tape[] = {s->tape_mem, s->bw4, s->bw1, s->bw8, s->wall_part, s->bw_sc};
   for (void* p : tape)
     if (p) cudaFree(p);
 }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// The parts of the reverse pass's exact-scatter scratch (pbf::scatter_bytes(np) bytes at base).
+void scatter_layout(unsigned char* base, size_t np, pbf::BackwardArgs& a) {
+  const size_t cap = np * pbf::kScatterPerParticle;
+  unsigned char* p = base;
+  a.sc_val = (float4*)p;
+  p += sizeof(float4) * cap;
+  a.sc_acc = (unsigned long long*)p;
+  p += sizeof(unsigned long long) * 7 * np;
+  a.sc_key = (int2*)p;
+  p += sizeof(int2) * cap;
+  a.sc_max = (unsigned*)p;
+  p += sizeof(unsigned) * 7 * np;
+  a.sc_cnt = (unsigned*)p;
+  p += sizeof(unsigned) * 2 * np;
+  a.sc_nonfin = (unsigned*)p;
+  p += sizeof(unsigned) * np;
+  a.sc_ctr = (unsigned*)p;
+  a.sc_cap = (int)cap;
+  a.sc_stride = (int)np;
+}
 
 }  // namespace
 
@@ -715,6 +737,9 @@ pbf_status pbf_tape_enable(pbf_solver* s, int depth) {
     if (e == cudaSuccess) e = alloc(&s->bw8, np * 2);
     if (e == cudaSuccess) e = cudaMemset(s->bw4 + 5 * np, 0, sizeof(float4) * 2 * np);
     if (e == cudaSuccess) e = alloc(&s->wall_part, blocks * 6);
+    // the exact-scatter scratch starts (and is left by every fold) at zero
+    if (e == cudaSuccess) e = alloc(&s->bw_sc, pbf::scatter_bytes(np));
+    if (e == cudaSuccess) e = cudaMemset(s->bw_sc, 0, pbf::scatter_bytes(np));
     if (e != cudaSuccess) {
       cudaGetLastError();
       return cuda_fail(e, "pbf_tape_enable");
@@ -768,6 +793,7 @@ pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, v
   a.rtot = s->bw1 + 2 * np;
   a.fix = s->bw4 + 5 * np;
   a.fixv = s->bw4 + 6 * np;
+  scatter_layout(s->bw_sc, np, a);
   a.gcell = s->bw8;
   a.kcell = s->bw8 + np;
   a.wall_part = s->wall_part;

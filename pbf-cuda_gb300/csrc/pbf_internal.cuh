@@ -370,7 +370,27 @@ struct BackwardArgs {
   unsigned long long* kcell;  // packed cell of the current positions
   float4* fix;      // scattered adjoints of non-reciprocal pairs: xyz positions, w lambda / rho
   float4* fixv;     // scattered velocity adjoints of non-reciprocal pairs (XSPH)
+  // The scattered terms are summed exactly, in any order (adjoint.cu): listed,
+  // then added per target as 64-bit fixed point scaled by the target's largest
+  // term; fix / fixv above take only terms beyond the list's capacity.
+  int2* sc_key;               // [sc_cap] (target particle, 0: fix / 1: fixv)
+  float4* sc_val;             // [sc_cap] the term (fixv: w unused)
+  unsigned long long* sc_acc; // [7][sc_stride] fixed-point sums (fix xyzw, fixv xyz); 0 between folds
+  unsigned* sc_max;           // [7][sc_stride] largest finite |term| (float bits); 0 between folds
+  unsigned* sc_cnt;           // [2][sc_stride] terms per target (fix, fixv); 0 between folds
+  unsigned* sc_nonfin;        // [sc_stride] non-finite terms, 3 bits per component; 0 between folds
+  unsigned* sc_ctr;           // [2] terms listed, terms beyond the capacity; listed is 0 between folds
+  int sc_cap;
+  int sc_stride;
 };
+
+// Bytes of the reverse pass's exact-scatter scratch for up to np particles
+// (list capacity kScatterPerParticle terms per particle).
+constexpr int kScatterPerParticle = 8;
+inline size_t scatter_bytes(size_t np) {
+  const size_t cap = np * kScatterPerParticle;
+  return cap * (sizeof(int2) + sizeof(float4)) + np * (7 * 8 + 7 * 4 + 2 * 4 + 4) + 64;
+}
 
 // Poly6 density (mass 1, radius h) of the particles at the nodes of a
 // dims[0] x dims[1] x dims[2] lattice of cell centres spanning [lo, hi], and
