@@ -663,22 +663,31 @@ def adjoint_times(pkg, torch, args, evals: int, frames: int) -> dict:
         q.dt = scene.params.dt
         scene.params = q
     stream = torch.cuda.current_stream()
-    ip = pkg.inverse.InverseProblem(scene, frames=frames, every=10)
-    ip.make_target()
-    v0 = torch.zeros((ip.n, 3), device="cuda")
-    warm = 3
-    for _ in range(warm):
-        ip.loss_and_grad(v0, 0.0)
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(evals):
-        L, gv, ga = ip.loss_and_grad(v0, 0.0)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fb_ms = e0.elapsed_time(e1) / evals
-    finite = bool(torch.isfinite(gv).all()) and bool(np.isfinite(ga))
-    ip.close()
+    warm = 3
+
+    def fwd_bwd(keep):
+        ip = pkg.inverse.InverseProblem(scene, frames=frames, every=10, keep=keep)
+        ip.make_target()
+        v0 = torch.zeros((ip.n, 3), device="cuda")
+        for _ in range(warm):
+            ip.loss_and_grad(v0, 0.0)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(evals):
+            L, gv, ga = ip.loss_and_grad(v0, 0.0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / evals
+        fin = bool(torch.isfinite(gv).all()) and bool(np.isfinite(ga))
+        steps, lim = ip.steps, ip.limits(0.0)
+        ip.close()
+        return ms, fin, steps, lim
+
+    # checkpoints every 10 frames, the last 10-frame segment taped by the forward
+    fb_ms, finite, nsteps, limits = fwd_bwd(1)
+    # the whole rollout taped by the forward (no segment re-run; 10-frame checkpoints kept)
+    fb_all_ms = fwd_bwd(1 << 20)[0]
     sim = pkg.Simulator(scene.params, scene.ulim, scene.llim, scene.n)
     st = pkg.ParticleState(scene.pos, scene.vel)
     for _ in range(warm):
@@ -692,18 +701,19 @@ def adjoint_times(pkg, torch, args, evals: int, frames: int) -> dict:
         st.a_vel.zero_()
         st.iid[: st.n].copy_(iid0)
         st.tictoc = False
-        for k in range(ip.steps):
-            sim.setLim(*ip.limits(0.0)(k))
+        for k in range(nsteps):
+            sim.setLim(*limits(k))
             st.step(sim)
     e1.record(stream)
     torch.cuda.synchronize()
     f_ms = e0.elapsed_time(e1) / evals
     sim.close()
-    nframes = ip.steps // pkg.inverse.STEPS_PER_FRAME
+    nframes = nsteps // pkg.inverse.STEPS_PER_FRAME
     return {"value": fb_ms / nframes, "unit": "ms/frame", "evals": evals, "warmup": warm, "frames": nframes,
-            "particles": scene.n, "params": args.params, "ms_per_step": fb_ms / ip.steps,
+            "particles": scene.n, "params": args.params, "ms_per_step": fb_ms / nsteps,
             "forward_ms_per_frame": f_ms / nframes, "fwd_bwd_over_fwd": fb_ms / f_ms,
-            "gradient_finite": finite}
+            "gradient_finite": finite,
+            "whole_rollout_taped": {"value": fb_all_ms / nframes, "fwd_bwd_over_fwd": fb_all_ms / f_ms}}
 
 
 def run_adjoint(args):
@@ -723,6 +733,7 @@ def run_adjoint(args):
         "forward_ms_per_frame": r["forward_ms_per_frame"],
         "fwd_bwd_over_fwd": r["fwd_bwd_over_fwd"],
         "gradient_finite": r["gradient_finite"],
+        "whole_rollout_taped": r["whole_rollout_taped"],
     }
     print(json.dumps(line), flush=True)
 

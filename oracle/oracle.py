@@ -213,36 +213,53 @@ def _nodes(lo, hi, dims):
     return np.stack([gx.ravel(), gy.ravel(), gz.ravel()], 1)
 
 
+def _node_pairs(x, lo, hi, dims, h):
+    """Every (particle, node) pair closer than h: particle indices, flat node
+    indices and r = x - node.  A node within h of a particle lies within
+    h / step of its lattice coordinate u, so within ceil(h / step + 0.5) of
+    rint(u): those nodes are tested."""
+    lo = np.asarray(lo, np.float64)
+    dims = np.asarray(dims, np.int64)
+    step = (np.asarray(hi, np.float64) - lo) / dims
+    u = (x - lo) / step - 0.5  # lattice coordinate of the particle (node k sits at k)
+    base = np.rint(u).astype(np.int64)
+    reach = [int(np.ceil(h / step[a] + 0.5)) for a in range(3)]
+    offs = np.stack(np.meshgrid(*[np.arange(-r, r + 1) for r in reach], indexing="ij"), -1).reshape(-1, 3)
+    k = base[:, None, :] + offs[None, :, :]                      # (n, m, 3) node indices
+    inside = np.all((k >= 0) & (k < dims), -1)
+    node = lo + (k + 0.5) * step
+    r = x[:, None, :] - node
+    q = (r * r).sum(-1)
+    hit = inside & (q < h * h)
+    pi, mi = np.nonzero(hit)
+    kk = k[pi, mi]
+    flat = (kk[:, 0] * dims[1] + kk[:, 1]) * dims[2] + kk[:, 2]
+    return pi, flat, r[pi, mi], q[pi, mi]
+
+
 def density_grid(pos, lo, hi, dims, h):
     """FP64 poly6 density (mass 1, radius h) at the centres of the dims cells
     spanning [lo, hi] (x slowest).  The inverse problem's loss term; the
     reference has none, so this restatement is checked against finite
     differences instead."""
     x = np.asarray(pos, np.float64)[:, :3]
-    nodes = _nodes(lo, hi, dims)
     coef = 315.0 / (64.0 * np.pi * h ** 9)
-    out = np.zeros(len(nodes))
-    for s in range(0, len(x), 2048):
-        d = nodes[:, None, :] - x[None, s:s + 2048, :]
-        q = (d * d).sum(-1)
-        w = np.where(q < h * h, h * h - q, 0.0)
-        out += coef * (w ** 3).sum(1)
+    pi, flat, _, q = _node_pairs(x, lo, hi, dims, h)
+    out = np.bincount(flat, weights=coef * (h * h - q) ** 3, minlength=int(np.prod(dims)))
     return out.reshape(tuple(dims))
 
 
 def density_grid_backward(pos, lo, hi, dims, h, g_grid):
     """Adjoint of ``density_grid`` w.r.t. the positions, (n, 4) FP64."""
     x = np.asarray(pos, np.float64)[:, :3]
-    nodes = _nodes(lo, hi, dims)
     g = np.asarray(g_grid, np.float64).ravel()
     coef = 315.0 / (64.0 * np.pi * h ** 9)
     out = np.zeros((len(x), 4))
-    for s in range(0, len(x), 2048):
-        r = x[None, s:s + 2048, :] - nodes[:, None, :]
-        q = (r * r).sum(-1)
-        w = np.where(q < h * h, h * h - q, 0.0)
-        dq = g[:, None] * (-3.0 * coef * w * w) * 2.0
-        out[s:s + 2048, :3] = (dq[:, :, None] * r).sum(0)
+    pi, flat, r, q = _node_pairs(x, lo, hi, dims, h)
+    w = h * h - q
+    dq = g[flat] * (-3.0 * coef * w * w) * 2.0
+    for a in range(3):
+        out[:, a] = np.bincount(pi, weights=dq * r[:, a], minlength=len(x))
     return out
 
 

@@ -12,11 +12,13 @@ Building blocks, all on the GPU through the C ABI:
 
 On top of them:
 
-* ``Rollout`` — T chained steps with checkpoints every K steps.  The reverse
-  sweep re-runs each K-step segment from its checkpoint with the tape on (a
-  stack of K taped steps) and pops the steps' reverse passes, last step
-  first.  Each step runs twice forward and once backward; memory: T/K
-  checkpoints + K tape records.
+* ``Rollout`` — T chained steps with checkpoints every K steps.  The last
+  ``keep`` segments are taped as the forward runs them; the reverse sweep pops
+  their reverse passes directly, then re-runs each earlier K-step segment from
+  its checkpoint with the tape on (a stack of K taped steps) and pops its
+  reverse passes, last step first.  A step of a re-run segment runs twice
+  forward and once backward; memory: T/K checkpoints + max(keep, 1) K tape
+  records.
 * ``step`` — one step as a ``torch.autograd.Function`` (its backward re-runs
   the step from saved copies of its inputs with the tape on).
 * ``DensityGrid`` — the density grid as a ``torch.autograd.Function``.
@@ -138,16 +140,21 @@ class Rollout:
     state.  ``backward(g_pos, g_vel)`` takes the adjoints of that final state
     (in its order) and returns the adjoints of the initial pos and vel (in
     their order) and a (steps, 6) tensor of the limits' adjoints per step
-    (ulim xyz, llim xyz).  The forward runs with the tape off; the reverse
-    sweep re-runs each segment from its checkpoint with a tape of ``every``
-    steps and pops their reverse passes.
+    (ulim xyz, llim xyz).  The forward tapes its last ``keep`` segments
+    (``keep`` = 0: none; a large value: the whole rollout, no re-runs); the
+    reverse sweep pops those, then re-runs each earlier segment from its
+    checkpoint with a tape of ``every`` steps and pops their reverse passes.
     """
 
-    def __init__(self, sim: Simulator, every: int = 10):
+    def __init__(self, sim: Simulator, every: int = 10, keep: int = 1):
         if every < 1:
             raise ValueError("every must be >= 1")
+        if keep < 0:
+            raise ValueError("keep must be >= 0")
         self.sim = sim
         self.every = int(every)
+        self.keep = int(keep)
+        self._first_taped = 0
         self._ckpt: List[Tuple[torch.Tensor, torch.Tensor, torch.Tensor]] = []
         self._steps = 0
         self._limits: Optional[Callable[[int], Limits]] = None
@@ -169,10 +176,14 @@ class Rollout:
         self._limits = limits
         self._ckpt = []
         self.sim.tape(0)
+        nseg = (self._steps + self.every - 1) // self.every
+        self._first_taped = nseg - min(self.keep, nseg)
         pos, vel, iid = pos.clone(), vel.clone(), iid.clone()
         for k in range(self._steps):
             if k % self.every == 0:
                 self._ckpt.append((pos.clone(), vel.clone(), iid.clone()))
+                if k // self.every == self._first_taped:  # tape from here to the end
+                    self.sim.tape(self._steps - k)
             pos, vel, iid = self._advance(pos, vel, iid, k)
         return pos, vel, iid
 
@@ -180,13 +191,15 @@ class Rollout:
         g_pos = g_pos.contiguous().clone()
         g_vel = g_vel.contiguous().clone()
         g_lim = torch.zeros((self._steps, 6), dtype=torch.float32, device=g_pos.device)
-        self.sim.tape(self.every)
         for seg in range(len(self._ckpt) - 1, -1, -1):
             start = seg * self.every
             end = min(start + self.every, self._steps)
-            pos, vel, iid = (t.clone() for t in self._ckpt[seg])
-            for k in range(start, end):
-                pos, vel, iid = self._advance(pos, vel, iid, k)
+            if seg < self._first_taped:  # not taped by the forward: re-run it taped
+                if seg == self._first_taped - 1:
+                    self.sim.tape(self.every)
+                pos, vel, iid = (t.clone() for t in self._ckpt[seg])
+                for k in range(start, end):
+                    pos, vel, iid = self._advance(pos, vel, iid, k)
             for k in range(end - 1, start - 1, -1):
                 g_pos, g_vel, gl = self.sim.backward(g_pos, g_vel)
                 g_lim[k] = gl

@@ -31,24 +31,27 @@ class InverseProblem:
     """One scene, one simulator, the rollout and the loss.
 
     ``scene``: a scenes.Scene (default scenes.inverse_scene()); ``frames``:
-    frames of STEPS_PER_FRAME steps; ``every``: checkpoint interval in frames;
-    ``period``: the wall sweep's period in seconds.
+    frames of STEPS_PER_FRAME steps (``steps``: a step count instead);
+    ``every``: checkpoint interval in frames; ``period``: the wall sweep's
+    period in seconds; ``keep``: trailing checkpoint segments the forward
+    tapes (adjoint.Rollout).
     """
 
     def __init__(self, scene: Optional[scenes.Scene] = None, frames: int = 60, every: int = 10,
-                 dims: Sequence[int] = GRID_DIMS, period: float = 4.0, device: str = "cuda"):
+                 dims: Sequence[int] = GRID_DIMS, period: float = 4.0, device: str = "cuda", keep: int = 1,
+                 steps: Optional[int] = None):
         self.scene = scene if scene is not None else scenes.inverse_scene()
         self.params = self.scene.params
         self.box = tuple(float(x) for x in self.scene.ulim)
         self.dims = tuple(int(d) for d in dims)
-        self.steps = int(frames) * STEPS_PER_FRAME
+        self.steps = int(frames) * STEPS_PER_FRAME if steps is None else int(steps)
         self.period = float(period)
         self.device = torch.device(device)
         self.n = self.scene.n
         self.dt = float(np.float32(self.params.dt))
         self.h = float(np.float32(self.params.h))
         self.sim = Simulator(self.params, self.box, (0.0, 0.0, 0.0), self.n)
-        self.rollout = Rollout(self.sim, every=int(every) * STEPS_PER_FRAME)
+        self.rollout = Rollout(self.sim, every=int(every) * STEPS_PER_FRAME, keep=keep)
         self.pos0 = torch.from_numpy(np.ascontiguousarray(self.scene.pos, np.float32)).to(self.device)
         self.target: Optional[torch.Tensor] = None
 
