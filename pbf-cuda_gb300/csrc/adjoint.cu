@@ -42,6 +42,14 @@ namespace {
 constexpr int kThreads = 128;
 // Below this many particles a warp shares each particle (see lane_sum).
 constexpr int kWarpPerParticleBelow = 131072;
+// PBF_BWD_LANES (a build-time tuning macro): lanes that split one particle's
+// window in the reverse kernels of steps under kWarpPerParticleBelow particles.
+#ifndef PBF_BWD_LANES
+#define PBF_BWD_LANES 8
+#endif
+constexpr int kSmallStepLanes = PBF_BWD_LANES;
+static_assert(kSmallStepLanes >= 1 && kSmallStepLanes <= 32 && (kSmallStepLanes & (kSmallStepLanes - 1)) == 0,
+              "lanes per particle: a power of two up to a warp");
 
 __device__ __forceinline__ void column_run(const SceneGeom& g, const uint32_t* __restrict__ cs,
                                            int n, int x, int y, int z, int& s, int& e) {
@@ -216,13 +224,18 @@ __device__ __forceinline__ void clear_nonfin(const BackwardArgs& a, int i, unsig
   if (nf & mask) a.sc_nonfin[i] = nf & ~mask;
 }
 
-// L lanes share one particle (L = 1, or a whole warp for small steps, where
-// one thread per particle would leave most SMs idle): its lanes split the
-// window and add their sums in a fixed tree, so lane 0 holds the result.
+// L lanes share one particle (L = 1, or kSmallStepLanes for small steps,
+// where one thread per particle would leave most SMs idle): its lanes split
+// the window and add their sums in a fixed tree, so lane 0 holds the result.
 template <int L>
 __device__ __forceinline__ float lane_sum(float v) {
   if constexpr (L > 1) {
-    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    // the L lanes of one particle are an aligned group of the warp (L divides
+    // 32 and the blocks hold whole warps); they return together, so only the
+    // group takes part: other groups of a warp may have returned already
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned mask = L == 32 ? 0xffffffffu : ((1u << L) - 1u) << (lane & ~(unsigned)(L - 1));
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_down_sync(mask, v, o, L);
   }
   return v;
 }
@@ -758,7 +771,7 @@ cudaError_t backward(const BackwardArgs& args, const BackwardTape& t, const uint
   k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.X0, a.gcell);
   k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.XK, a.kcell);
   if (a.n < kWarpPerParticleBelow)
-    return run_backward<32>(a, t, perm, g_pos, g_vel, g_lim, stream);
+    return run_backward<kSmallStepLanes>(a, t, perm, g_pos, g_vel, g_lim, stream);
   return run_backward<1>(a, t, perm, g_pos, g_vel, g_lim, stream);
 }
 
