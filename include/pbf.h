@@ -263,6 +263,8 @@ typedef struct pbf_tuning {
   float ms_per_step;  /* the chosen configuration's time per step */
   float ms_default;   /* the default configuration's time per step */
   int order;          /* 1: current-cell order (the default); 0: grid order */
+  int bwd_lanes;      /* pbf_backward, steps under 131072 particles: lanes per particle, 8, 16
+                         or 32 (0: the default, 32); not timed by pbf_autotune */
 } pbf_tuning;
 
 pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
@@ -273,7 +275,8 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
  * pbf_autotune returned): dense_window >= 32 candidates, or 0 for the
  * default; dense_all 1 (every particle dense), 0 (by window) or -1 (the
  * default: every particle dense below 131072 particles); order 1, 0 or -1
- * (the default, 1).  ms fields are ignored on set and 0 on get. */
+ * (the default, 1); bwd_lanes 0 (the default), 8, 16 or 32.  ms fields are
+ * ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
 

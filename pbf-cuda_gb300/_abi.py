@@ -135,7 +135,8 @@ class PbfTuning(ctypes.Structure):
     """Mirror of ``pbf_tuning`` (include/pbf.h)."""
 
     _fields_ = [("dense_window", ctypes.c_int), ("dense_all", ctypes.c_int),
-                ("ms_per_step", ctypes.c_float), ("ms_default", ctypes.c_float), ("order", ctypes.c_int)]
+                ("ms_per_step", ctypes.c_float), ("ms_default", ctypes.c_float), ("order", ctypes.c_int),
+                ("bwd_lanes", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

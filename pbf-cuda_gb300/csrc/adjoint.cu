@@ -42,14 +42,11 @@ namespace {
 constexpr int kThreads = 128;
 // Below this many particles a warp shares each particle (see lane_sum).
 constexpr int kWarpPerParticleBelow = 131072;
-// PBF_BWD_LANES (a build-time tuning macro): lanes that split one particle's
-// window in the reverse kernels of steps under kWarpPerParticleBelow particles.
-#ifndef PBF_BWD_LANES
-#define PBF_BWD_LANES 8
-#endif
-constexpr int kSmallStepLanes = PBF_BWD_LANES;
-static_assert(kSmallStepLanes >= 1 && kSmallStepLanes <= 32 && (kSmallStepLanes & (kSmallStepLanes - 1)) == 0,
-              "lanes per particle: a power of two up to a warp");
+// Lanes that split one particle's window in the reverse kernels of steps
+// under kWarpPerParticleBelow particles: BackwardArgs::lanes (8, 16 or 32;
+// pbf_tuning's bwd_lanes), 32 by default.  Few lanes suit windows of a few
+// hundred candidates (less reduction per particle); many lanes suit piled-up
+// states, where a handful of particles hold windows of thousands.
 
 __device__ __forceinline__ void column_run(const SceneGeom& g, const uint32_t* __restrict__ cs,
                                            int n, int x, int y, int z, int& s, int& e) {
@@ -224,7 +221,7 @@ __device__ __forceinline__ void clear_nonfin(const BackwardArgs& a, int i, unsig
   if (nf & mask) a.sc_nonfin[i] = nf & ~mask;
 }
 
-// L lanes share one particle (L = 1, or kSmallStepLanes for small steps,
+// L lanes share one particle (L = 1, or BackwardArgs::lanes for small steps,
 // where one thread per particle would leave most SMs idle): its lanes split
 // the window and add their sums in a fixed tree, so lane 0 holds the result.
 template <int L>
@@ -770,8 +767,11 @@ cudaError_t backward(const BackwardArgs& args, const BackwardTape& t, const uint
   const int blocks256 = (a.n + 255) / 256;
   k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.X0, a.gcell);
   k_bwd_cells<<<blocks256, 256, 0, stream>>>(a, a.XK, a.kcell);
-  if (a.n < kWarpPerParticleBelow)
-    return run_backward<kSmallStepLanes>(a, t, perm, g_pos, g_vel, g_lim, stream);
+  if (a.n < kWarpPerParticleBelow) {
+    if (a.lanes == 8) return run_backward<8>(a, t, perm, g_pos, g_vel, g_lim, stream);
+    if (a.lanes == 16) return run_backward<16>(a, t, perm, g_pos, g_vel, g_lim, stream);
+    return run_backward<32>(a, t, perm, g_pos, g_vel, g_lim, stream);
+  }
   return run_backward<1>(a, t, perm, g_pos, g_vel, g_lim, stream);
 }
 

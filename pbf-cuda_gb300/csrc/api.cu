@@ -76,6 +76,7 @@ struct pbf_solver {
   int tune_window;
   int tune_all;
   int tune_order;
+  int tune_bwd_lanes;  // 0: the default (32)
 };
 
 namespace {
@@ -794,6 +795,7 @@ pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, v
   a.fix = s->bw4 + 5 * np;
   a.fixv = s->bw4 + 6 * np;
   scatter_layout(s->bw_sc, np, a);
+  a.lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;
   a.gcell = s->bw8;
   a.kcell = s->bw8 + np;
   a.wall_part = s->wall_part;
@@ -1279,6 +1281,7 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
   out->dense_window = best_w;
   out->dense_all = best_all;
   out->order = best_ord;
+  out->bwd_lanes = 0;
   out->ms_per_step = best;
   out->ms_default = def_ms;
   return PBF_OK;
@@ -1316,6 +1319,7 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
   s->tune_window = out->dense_window;
   s->tune_all = out->dense_all;
   s->tune_order = out->order;
+  out->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;  // not timed: kept
   return PBF_OK;
 }
 
@@ -1327,9 +1331,12 @@ pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
     return fail(PBF_ERR_INVALID_ARG, "dense_all must be -1, 0 or 1 (got %d)", t->dense_all);
   if (t->order < -1 || t->order > 1)
     return fail(PBF_ERR_INVALID_ARG, "order must be -1, 0 or 1 (got %d)", t->order);
+  if (t->bwd_lanes != 0 && t->bwd_lanes != 8 && t->bwd_lanes != 16 && t->bwd_lanes != 32)
+    return fail(PBF_ERR_INVALID_ARG, "bwd_lanes must be 0, 8, 16 or 32 (got %d)", t->bwd_lanes);
   s->tune_window = t->dense_window;
   s->tune_all = t->dense_all;
   s->tune_order = t->order;
+  s->tune_bwd_lanes = t->bwd_lanes;
   return PBF_OK;
 }
 
@@ -1338,6 +1345,7 @@ pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
   t->dense_window = s->tune_window > 0 ? s->tune_window : pbf::kDefaultDenseWindow;
   t->dense_all = s->tune_all;
   t->order = s->tune_order >= 0 ? s->tune_order : 1;
+  t->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;
   t->ms_per_step = 0.f;
   t->ms_default = 0.f;
   return PBF_OK;

@@ -382,6 +382,7 @@ struct BackwardArgs {
   unsigned* sc_ctr;           // [2] terms listed, terms beyond the capacity; listed is 0 between folds
   int sc_cap;
   int sc_stride;
+  int lanes;        // lanes per particle below kWarpPerParticleBelow particles: 8, 16 or 32
 };
 
 // Bytes of the reverse pass's exact-scatter scratch for up to np particles

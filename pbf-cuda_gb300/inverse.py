@@ -111,6 +111,27 @@ class InverseProblem:
         g_amp = float((g_lim[:, 0].double().cpu() * dw).sum())
         return float((r.double() ** 2).sum()), g_vel0[:, :3], g_amp
 
+    def autotune_backward(self, vel0: torch.Tensor, amp: float, lanes=(8, 16, 32)) -> dict:
+        """Times one gradient evaluation per choice of the reverse pass's lanes
+        per particle (pbf_tuning.bwd_lanes) at (vel0, amp) and keeps the fastest
+        for the following evaluations; returns the choice and the times (ms).
+        The choice changes the order of the reverse pass's window sums only."""
+        times = {}
+        tune = self.sim.tuning()
+        for lane_count in lanes:
+            self.sim.set_tuning(tune["dense_window"], tune["dense_all"], tune["order"], int(lane_count))
+            self.loss_and_grad(vel0, amp)  # untimed: the first evaluation of a setting
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            self.loss_and_grad(vel0, amp)
+            e1.record()
+            torch.cuda.synchronize()
+            times[int(lane_count)] = e0.elapsed_time(e1)
+        best = min(times, key=times.get)
+        self.sim.set_tuning(tune["dense_window"], tune["dense_all"], tune["order"], best)
+        return {"bwd_lanes": best, "ms": times}
+
     def optimise(self, iters: int = 10, lr_vel: float = 1e-9, lr_amp: float = 1e-10,
                  vel0: Optional[torch.Tensor] = None, amp: float = 0.0):
         """Plain gradient descent on (vel0, amp); returns (vel0, amp, losses)."""

@@ -153,17 +153,19 @@ class Simulator:
                                    g_vel.data_ptr(), g_lim.data_ptr(), _stream_handle(stream)), "pbf_backward")
         return g_pos, g_vel, g_lim
 
-    def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1) -> None:
-        """The dense-kernel and particle-order choices of the following steps
-        (pbf_set_tuning); 0 / -1: the defaults."""
+    def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, bwd_lanes: int = 0) -> None:
+        """The dense-kernel and particle-order choices of the following steps, and
+        the reverse pass's lanes per particle (pbf_set_tuning); 0 / -1: the defaults."""
         t = PbfTuning()
         t.dense_window, t.dense_all, t.order = int(dense_window), int(dense_all), int(order)
+        t.bwd_lanes = int(bwd_lanes)
         check(self._L.pbf_set_tuning(self._h, ctypes.byref(t)), "pbf_set_tuning")
 
     def tuning(self) -> dict:
         t = PbfTuning()
         check(self._L.pbf_get_tuning(self._h, ctypes.byref(t)), "pbf_get_tuning")
-        return {"dense_window": t.dense_window, "dense_all": t.dense_all, "order": t.order}
+        return {"dense_window": t.dense_window, "dense_all": t.dense_all, "order": t.order,
+                "bwd_lanes": t.bwd_lanes}
 
     def autotune(self, pos: torch.Tensor, vel: torch.Tensor, iid: torch.Tensor, nparticle: Optional[int] = None,
                  steps: int = 3, stream=None) -> dict:

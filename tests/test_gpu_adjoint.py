@@ -39,8 +39,9 @@ def close(got, want, what):
     assert err <= REL * scale, f"{what}: max err {err:.3e} vs scale {scale:.3e}"
 
 
-def gpu_step_backward(pbf, p, ulim, llim, pos, vel, ga, gb):
-    """One taped step, then its reverse pass with g_npos = ga[iid], g_nvel = gb[iid]."""
+def gpu_step_backward(pbf, p, ulim, llim, pos, vel, ga, gb, lanes=0):
+    """One taped step, then its reverse pass with g_npos = ga[iid], g_nvel = gb[iid]
+    (lanes: the reverse pass's lanes per particle, 0 for the default)."""
     import torch
 
     n = len(pos)
@@ -50,6 +51,7 @@ def gpu_step_backward(pbf, p, ulim, llim, pos, vel, ga, gb):
     npos = torch.empty_like(d_pos)
     nvel = torch.empty_like(d_vel)
     with pbf.Simulator(p, ulim, llim, n) as sim:
+        sim.set_tuning(bwd_lanes=lanes)
         sim.tape(True)
         sim.step(d_pos, npos, d_vel, nvel, iid, n)
         order = iid.long()
@@ -60,11 +62,12 @@ def gpu_step_backward(pbf, p, ulim, llim, pos, vel, ga, gb):
         return g_pos.cpu().numpy(), g_vel.cpu().numpy(), g_lim.cpu().numpy(), iid.cpu().numpy()
 
 
-@pytest.mark.parametrize("seed,n", [(0, (5, 5, 5)), (1, (10, 8, 6)), (2, (12, 12, 12))])
-def test_backward_matches_oracle(pbf, oracle, cuda, seed, n):
+@pytest.mark.parametrize("seed,n,lanes", [(0, (5, 5, 5), 0), (1, (10, 8, 6), 0), (2, (12, 12, 12), 0),
+                                          (2, (12, 12, 12), 8), (1, (10, 8, 6), 16)])
+def test_backward_matches_oracle(pbf, oracle, cuda, seed, n, lanes):
     _, pos, vel, p, a, b = setup(pbf, seed=seed, n=n)
     ulim, llim = (1.2, 1.2, 1.2), (0.0, 0.0, 0.0)
-    g_pos, g_vel, g_lim, _ = gpu_step_backward(pbf, p, ulim, llim, pos, vel, a, b)
+    g_pos, g_vel, g_lim, _ = gpu_step_backward(pbf, p, ulim, llim, pos, vel, a, b, lanes)
     iid = np.arange(len(pos), dtype=np.uint32)
     r = oracle.step(p, ulim, llim, pos.astype(np.float64), vel.astype(np.float64), iid, "f64")
     want = oracle.step_backward(p, ulim, llim, pos.astype(np.float64), vel.astype(np.float64), iid,

@@ -79,18 +79,18 @@ def test_set_tuning_round_trip(pbf, oracle, cuda):
     vel = torch.zeros_like(pos)
     iid = torch.arange(n, dtype=torch.int32, device="cuda")
     with pbf.Simulator(p, sc.ulim, sc.llim, n) as sim:
-        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1}
+        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1, "bwd_lanes": 32}
         sim.set_tuning(128, 0, 0)
-        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0}
-        for bad in ((16, 0), (256, 2), (256, -2), (0, -1, 2), (0, -1, -2)):
+        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32}
+        for bad in ((16, 0), (256, 2), (256, -2), (0, -1, 2), (0, -1, -2), (0, -1, 1, 4)):
             with pytest.raises(pbf.PbfError):
                 sim.set_tuning(*bad)
-        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0}
+        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32}
         npos, nvel = torch.empty_like(pos), torch.empty_like(vel)
         sim.step(pos, npos, vel, nvel, iid, n)
         torch.cuda.synchronize()
         sim.set_tuning(0, -1)
-        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1}
+        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1, "bwd_lanes": 32}
     r = oracle.step(p, sc.ulim, sc.llim, sc.pos.astype(np.float64), np.zeros((n, 4)), np.arange(n, dtype=np.uint32),
                     "f64")
     np.testing.assert_array_equal(iid.cpu().numpy().astype(np.uint32), r["iid"])
