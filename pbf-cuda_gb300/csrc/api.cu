@@ -25,6 +25,48 @@ static_assert((long long)pbf::kMaskWords * PBF_MAX_PARTICLES - 1 <= 2147483647LL
               "mask index overflows int at PBF_MAX_PARTICLES");
 static_assert(8LL * PBF_MAX_PARTICLES - 1 <= 2147483647LL, "group hash index overflows int at PBF_MAX_PARTICLES");
 
+// Executable graphs of recent steps.  A step's launches depend only on its
+// constants (box, cells, coefficients, tuning), its buffers, its particle
+// count and its iterations, so a step whose key matches a cached graph's
+// replays that graph: no stream capture, no graph update.  A static box with
+// the reference's tic-toc buffers settles on two graphs.
+struct StepKey {
+  pbf::StepConsts c;
+  const void* bufs[5];
+  int n, niter;
+};
+
+struct GraphCache {
+  static constexpr int kEntries = 4;
+  struct Entry {
+    StepKey key;
+    bool valid = false;
+    cudaGraphExec_t exec = nullptr;
+    const uint32_t* keys_sorted = nullptr;  // host-side results of the capture, restored on replay
+    const uint32_t* perm = nullptr;
+  } e[kEntries];
+  int next = 0;
+  void clear() {
+    for (Entry& x : e) {
+      if (x.exec) cudaGraphExecDestroy(x.exec);
+      x = Entry();
+    }
+    next = 0;
+  }
+};
+
+StepKey make_key(const pbf::StepConsts& c, void* pos, void* npos, void* vel, void* nvel, void* iid, int n,
+                 int niter) {
+  StepKey k;
+  std::memset(&k, 0, sizeof(k));  // padding included: keys compare as bytes
+  k.c = c;
+  const void* b[5] = {pos, npos, vel, nvel, iid};
+  for (int a = 0; a < 5; ++a) k.bufs[a] = b[a];
+  k.n = n;
+  k.niter = niter;
+  return k;
+}
+
 // Phase boundaries recorded by pbf_step when profiling is on.
 enum { kEvStart, kEvGrid, kEvReorder, kEvXsphStart, kEvEnd, kEvFixed };
 constexpr int kMaxProfiledIters = 64;
@@ -50,9 +92,11 @@ struct pbf_solver {
   int last_launches;    // kernels launched by the last pbf_step
   int last_grid_launches;
   // CUDA graph of the step: captured on cap_stream, updated in place each step
+  // (profiled or taped steps), or replayed from the cache
   bool use_graph;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
+  GraphCache cache;
   // the tape (pbf_tape_enable): a stack of taped steps, each record holding
   // what the step's reverse pass needs, and the reverse pass's scratch
   int tape_depth;            // records the stack holds; 0: tape off
@@ -321,6 +365,7 @@ void free_all(pbf_solver* s) {
   for (cudaEvent_t& e : s->ev_it)
     if (e) cudaEventDestroy(e);
   if (s->exec) cudaGraphExecDestroy(s->exec);
+  s->cache.clear();
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   void* tape[] = {s->tape_mem, s->bw4, s->bw1, s->bw8, s->wall_part, s->bw_sc};
   for (void* p : tape)
@@ -414,9 +459,9 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (max_cells > scan_cap) max_cells = cells;
   if (max_cells > scan_cap) return fail(PBF_ERR_CAPACITY, "box needs %lld cells, limit %lld", cells, scan_cap);
 
-  pbf_solver* s = new (std::nothrow) pbf_solver;
+  // value-initialised: every pointer, handle and count zero, the graph cache empty
+  pbf_solver* s = new (std::nothrow) pbf_solver();
   if (!s) return fail(PBF_ERR_CAPACITY, "host allocation failed");
-  std::memset(s, 0, sizeof(*s));
   s->tune_all = -1;
   s->tune_order = -1;
   s->params = *params;
@@ -646,6 +691,37 @@ pbf_status launch_step_graph(const StepPlan& P, cudaStream_t cap, cudaGraphExec_
   return PBF_OK;
 }
 
+// Replays the cached graph of a step with this key, or captures the step into
+// a cache entry (the oldest) and launches it.
+pbf_status launch_cached(const StepPlan& P, GraphCache& cache, cudaStream_t cap, void* pos, void* npos,
+                         void* vel, void* nvel, uint32_t* iid, int n, cudaStream_t st_) {
+  const StepKey key = make_key(P.c, pos, npos, vel, nvel, iid, n, P.niter);
+  for (GraphCache::Entry& x : cache.e) {
+    if (x.valid && std::memcmp(&x.key, &key, sizeof(key)) == 0) {
+      P.grid->keys_sorted = x.keys_sorted;
+      P.sol->keys_sorted = x.keys_sorted;
+      P.sol->cell_start = P.grid->cell_start;
+      if (P.perm_out) *P.perm_out = x.perm;
+      PBF_CUDA(cudaGraphLaunch(x.exec, st_), "pbf_step: graph launch");
+      return PBF_OK;
+    }
+  }
+  GraphCache::Entry& x = cache.e[cache.next];
+  cache.next = (cache.next + 1) % GraphCache::kEntries;
+  x.valid = false;
+  const uint32_t* perm = nullptr;
+  StepPlan Q = P;
+  Q.perm_out = &perm;
+  const pbf_status st = launch_step_graph(Q, cap, &x.exec, pos, npos, vel, nvel, iid, n, st_);
+  if (st != PBF_OK) return st;
+  if (P.perm_out) *P.perm_out = perm;
+  x.key = key;
+  x.keys_sorted = P.grid->keys_sorted;
+  x.perm = perm;
+  x.valid = true;
+  return PBF_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -700,8 +776,12 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   P.tape_stride = s->max_particles;
   P.perm_out = &s->last_perm;
   const pbf::StepConsts& c = P.c;
-  st = s->use_graph ? launch_step_graph(P, s->cap_stream, &s->exec, pos, npos, vel, nvel, iid, n, st_)
-                    : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
+  if (!s->use_graph)
+    st = enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
+  else if (prof || taping)  // event and tape nodes are the step's own: capture it
+    st = launch_step_graph(P, s->cap_stream, &s->exec, pos, npos, vel, nvel, iid, n, st_);
+  else
+    st = launch_cached(P, s->cache, s->cap_stream, pos, npos, vel, nvel, iid, n, st_);
   if (st != PBF_OK) return st;
   const int niter = s->params.niter;
   s->last_grid_launches = pbf::grid_launches(c, n);
@@ -951,6 +1031,8 @@ struct pbf_batch {
   bool use_graph;
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
+  GraphCache cache;
+  std::vector<pbf::SceneGeom> geom_dev;  // the scene table as last uploaded
   int tune_window = 0;  // dense-kernel and order choices (pbf_batch_autotune); 0 / -1: the defaults
   int tune_all = -1;
   int tune_order = -1;
@@ -972,6 +1054,7 @@ void batch_free(pbf_batch* b) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);
+  b->cache.clear();
   if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
 }
 
@@ -1120,11 +1203,15 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   if (st != PBF_OK) return st;
   if (cells > b->max_cells) return fail(PBF_ERR_CAPACITY, "scenes need %lld cells", cells);
   cudaStream_t st_ = (cudaStream_t)stream;
-  // the scene table goes in stream order ahead of the step (pageable source:
-  // staged before the call returns, so the host copy may change afterwards)
-  PBF_CUDA(cudaMemcpyAsync(b->d_geom, b->geom.data(), sizeof(pbf::SceneGeom) * b->nscenes,
-                           cudaMemcpyHostToDevice, st_),
-           "pbf_batch_step: scene table");
+  // the scene table stays on the device; when a wall moved it goes in stream
+  // order ahead of the step (pageable source: staged before the call returns,
+  // so the host copy may change afterwards)
+  const size_t table = sizeof(pbf::SceneGeom) * b->nscenes;
+  if (b->geom_dev.size() != b->geom.size() || std::memcmp(b->geom_dev.data(), b->geom.data(), table) != 0) {
+    PBF_CUDA(cudaMemcpyAsync(b->d_geom, b->geom.data(), table, cudaMemcpyHostToDevice, st_),
+             "pbf_batch_step: scene table");
+    b->geom_dev = b->geom;
+  }
   StepPlan P;
   int unit_dims[3] = {1, 1, 1};
   P.c = make_consts(b->params, &b->ulim[0], &b->llim[0], unit_dims, b->num_sms);
@@ -1142,7 +1229,7 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   P.tape_x = P.tape_l = P.tape_xs = P.tape_rho = P.tape_perm = P.tape_cs = 0;
   P.tape_stride = 0;
   P.perm_out = nullptr;
-  st = b->use_graph ? launch_step_graph(P, b->cap_stream, &b->exec, pos, npos, vel, nvel, iid, n, st_)
+  st = b->use_graph ? launch_cached(P, b->cache, b->cap_stream, pos, npos, vel, nvel, iid, n, st_)
                     : enqueue_step(P, pos, npos, vel, nvel, iid, n, st_);
   if (st != PBF_OK) return st;
   b->last_n = n;

@@ -327,3 +327,45 @@ def test_large_sweep_one_iteration_vs_port(pbf, oracle, cuda):
     np.testing.assert_array_equal(got["iid"], ref["iid"])
     err = np.abs(got["npos"][:, :3] - ref["npos"][:, :3]).max()
     assert err <= 4 * 9.5367e-7, err
+
+
+def test_replayed_graphs_match_eager_steps(pbf, cuda):
+    """A static box with tic-toc buffers: after two captured steps every step
+    replays a cached graph (no capture).  12 such steps, then a change of the
+    box (a new capture) and 4 more: bitwise equal to the kernel-by-kernel
+    steps, for a single scene and for a batch."""
+    import torch
+
+    sc = pbf.scenes.dam_break(seed=9)
+    p = ref_params(pbf, 3)
+    out = []
+    for graphs in (True, False):
+        st = pbf.ParticleState(sc.pos, sc.vel)
+        with pbf.Simulator(p, (2.0, 1.0, 1.0), (0.0, 0.0, 0.0), sc.n) as sim:
+            sim.use_graphs(graphs)
+            for k in range(16):
+                if k == 12:
+                    sim.setLim((1.9, 1.0, 1.0), (0.0, 0.0, 0.0))
+                st.step(sim)
+            torch.cuda.synchronize()
+            out.append((st.pos.cpu().numpy(), st.vel.cpu().numpy(), st.iid[: st.n].cpu().numpy()))
+    for a, b in zip(*out):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    rng = np.random.default_rng(4)
+    parts = [pbf.scenes.lattice((8, 8, 8), (0.0, 0.0, 0.0), rng) for _ in range(3)]
+    pos = np.concatenate(parts)
+    counts = [len(q) for q in parts]
+    boxes = [(0.8, 0.8, 0.8)] * 3
+    out = []
+    for graphs in (True, False):
+        st = pbf.ParticleState(pos, np.zeros_like(pos))
+        with pbf.Ensemble(p, boxes, [(0.0, 0.0, 0.0)] * 3, counts) as ens:
+            ens.use_graphs(graphs)
+            for k in range(10):
+                if k == 6:
+                    ens.setLim(1, (0.7, 0.8, 0.8), (0.0, 0.0, 0.0))
+                st.step(ens)
+            torch.cuda.synchronize()
+            out.append((st.pos.cpu().numpy(), st.vel.cpu().numpy(), st.iid[: st.n].cpu().numpy()))
+    for a, b in zip(*out):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
