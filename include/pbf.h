@@ -246,16 +246,20 @@ pbf_status pbf_batch_use_graphs(pbf_batch* b, int on);
  * Autotuning (no counterpart in the reference).  Times a few choices of how
  * the neighbour passes split their work -- the window size above which a
  * particle's window goes to the dense kernel (a block of 8 warps splitting
- * the windows of 32 particles), whether every particle does, and the order in
+ * the windows of 32 particles), whether every particle does, the order in
  * which the passes take particles (the cell order of the grid, or the cell
- * each particle is in at that iteration) -- by running `steps` steps per
- * choice from copies of the caller's state (pos, vel, iid: device, n entries;
- * they are not modified), and keeps the fastest for the solver's following
- * steps.  The window and dense choices change the order in which window sums
- * are added, so results differ by rounding only; the particle order changes
- * nothing (each particle's sums are the same whichever warp computes them).
- * The trial steps are not taped.  The cell size stays h: with the reference's
- * stale grid, another cell size would change which neighbours a step sees.
+ * each particle is in at that iteration), and how many candidate positions a
+ * block of each pass kernel may stage in shared memory (bulk asynchronous
+ * copies of the column runs its particles' windows share, read there instead
+ * of through L1) -- by running `steps` steps per choice from copies of the
+ * caller's state (pos, vel, iid: device, n entries; they are not modified),
+ * and keeps the fastest for the solver's following steps.  The window and
+ * dense choices change the order in which window sums are added, so results
+ * differ by rounding only; the particle order and the staging change nothing
+ * (each particle's sums are the same whichever warp computes them, from
+ * whichever copy of the positions).  The trial steps are not taped.  The cell
+ * size stays h: with the reference's stale grid, another cell size would
+ * change which neighbours a step sees.
  */
 typedef struct pbf_tuning {
   int dense_window;   /* window entries above which a particle takes the dense kernel */
@@ -265,6 +269,10 @@ typedef struct pbf_tuning {
   int order;          /* 1: current-cell order (the default); 0: grid order */
   int bwd_lanes;      /* pbf_backward, steps under 131072 particles: lanes per particle, 8, 16
                          or 32 (0: the default, 32); not timed by pbf_autotune */
+  int stage_sparse;   /* slots (16 bytes each) a block of the one-thread-per-particle kernel
+                         copies into shared memory when its particles share one column of
+                         cells (0: none; at most 4096) */
+  int stage_dense;    /* the same for a block of the dense kernel */
 } pbf_tuning;
 
 pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
@@ -275,10 +283,23 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
  * pbf_autotune returned): dense_window >= 32 candidates, or 0 for the
  * default; dense_all 1 (every particle dense), 0 (by window) or -1 (the
  * default: every particle dense below 131072 particles); order 1, 0 or -1
- * (the default, 1); bwd_lanes 0 (the default), 8, 16 or 32.  ms fields are
+ * (the default, 1); bwd_lanes 0 (the default), 8, 16 or 32; stage_sparse and
+ * stage_dense 0 (off) to 4096 slots, or -1 (the default).  ms fields are
  * ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
+
+/*
+ * Errors the solver's kernels recorded on the device since the last call.
+ * Waits for the solver's work on `stream` (device, as for pbf_step), then
+ * returns PBF_ERR_TIMEOUT if a bounded device-side wait gave up since -- a
+ * block's copy of candidate positions into shared memory that did not
+ * complete; that block then read global memory instead, so the steps'
+ * results are unchanged -- else PBF_OK, and clears the record.  No
+ * counterpart in the reference, which does not check kernel errors.
+ */
+pbf_status pbf_check_device(pbf_solver* s, void* stream);
+pbf_status pbf_batch_check_device(pbf_batch* b, void* stream);
 
 /*
  * One step, same contract and results as pbf_step (bit for bit, with the

@@ -54,6 +54,8 @@ EXPORTED = (
     "pbf_batch_autotune",
     "pbf_set_tuning",
     "pbf_get_tuning",
+    "pbf_check_device",
+    "pbf_batch_check_device",
     "pbf_step_noalloc",
 )
 
@@ -136,7 +138,7 @@ class PbfTuning(ctypes.Structure):
 
     _fields_ = [("dense_window", ctypes.c_int), ("dense_all", ctypes.c_int),
                 ("ms_per_step", ctypes.c_float), ("ms_default", ctypes.c_float), ("order", ctypes.c_int),
-                ("bwd_lanes", ctypes.c_int)]
+                ("bwd_lanes", ctypes.c_int), ("stage_sparse", ctypes.c_int), ("stage_dense", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -225,6 +227,8 @@ def _declare(L) -> None:
         "pbf_batch_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, vp, vp]),
         "pbf_set_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
         "pbf_get_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
+        "pbf_check_device": (ctypes.c_int, [vp, vp]),
+        "pbf_batch_check_device": (ctypes.c_int, [vp, vp]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),
         "pbf_ssf_params_default": (None, [P(PbfSsfParams)]),
         "pbf_ssf_look_at": (ctypes.c_int, [P(PbfSsfParams), f3, f3, ctypes.c_float]),

@@ -121,6 +121,8 @@ struct pbf_solver {
   int tune_all;
   int tune_order;
   int tune_bwd_lanes;  // 0: the default (32)
+  int tune_stage_sparse;  // staged slots per sparse / dense block; -1: the defaults
+  int tune_stage_dense;
 };
 
 namespace {
@@ -145,6 +147,21 @@ pbf_status cuda_fail(cudaError_t e, const char* what) {
     cudaError_t e_ = (call);                         \
     if (e_ != cudaSuccess) return cuda_fail(e_, what); \
   } while (0)
+
+// Reads and clears a device error word (kErrorWord) after the work queued on
+// `stream`: PBF_ERR_TIMEOUT if a bounded device wait gave up.
+pbf_status check_device_word(uint32_t* word, cudaStream_t stream, const char* what) {
+  uint32_t bits = 0u;
+  PBF_CUDA(cudaMemcpyAsync(&bits, word, sizeof(bits), cudaMemcpyDeviceToHost, stream), what);
+  PBF_CUDA(cudaStreamSynchronize(stream), what);
+  if (bits == 0u) return PBF_OK;
+  PBF_CUDA(cudaMemsetAsync(word, 0, sizeof(uint32_t), stream), what);
+  PBF_CUDA(cudaStreamSynchronize(stream), what);
+  if (bits & pbf::kErrStageTimeout)
+    return fail(PBF_ERR_TIMEOUT, "%s: a shared-memory staging copy did not complete in time (the pass read "
+                                 "global memory instead)", what);
+  return fail(PBF_ERR_CUDA, "%s: device error bits 0x%x", what, bits);
+}
 
 bool finite_f(float v) { return std::isfinite(v); }
 
@@ -265,6 +282,8 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   c.dense_window = pbf::kDefaultDenseWindow;
   c.dense_all = -1;
   c.order = 1;
+  c.stage_sparse = pbf::kDefaultStageSparse;
+  c.stage_dense = pbf::kDefaultStageDense;
   return c;
 }
 
@@ -464,6 +483,8 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (!s) return fail(PBF_ERR_CAPACITY, "host allocation failed");
   s->tune_all = -1;
   s->tune_order = -1;
+  s->tune_stage_sparse = -1;
+  s->tune_stage_dense = -1;
   s->params = *params;
   std::memcpy(s->ulim, ulim, sizeof(s->ulim));
   std::memcpy(s->llim, llim, sizeof(s->llim));
@@ -486,7 +507,8 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc(&s->sol.iid_s, np);
   if (e == cudaSuccess) e = alloc(&s->sol.lambda, np);
   if (e == cudaSuccess) e = alloc(&s->sol.rho, np);
-  if (e == cudaSuccess) e = alloc(&s->sol.flags, (size_t)pbf::kNumFlags);
+  if (e == cudaSuccess) e = alloc(&s->sol.flags, (size_t)pbf::kFlagWords);
+  if (e == cudaSuccess) e = cudaMemset(s->sol.flags, 0, sizeof(uint32_t) * pbf::kFlagWords);
   if (e == cudaSuccess) e = alloc(&s->sol.dense, pbf::dense_list_len(max_particles));
   if (e == cudaSuccess) e = alloc(&s->sol.masks, (size_t)pbf::kMaskWords * np);
   s->sol.mask_stride = (int)np;
@@ -494,6 +516,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   if (e == cudaSuccess) e = alloc_groups(s->sol, max_particles);
   if (e == cudaSuccess) e = alloc_buckets(s->sol, np, nc);
   if (e == cudaSuccess) s->num_sms = current_sms();
+  if (e == cudaSuccess) e = pbf::set_pass_kernel_attributes();
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
   s->use_graph = true;
   if (e != cudaSuccess) {
@@ -754,6 +777,8 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   if (s->tune_window > 0) P.c.dense_window = s->tune_window;
   P.c.dense_all = s->tune_all;
   if (s->tune_order >= 0) P.c.order = s->tune_order;
+  if (s->tune_stage_sparse >= 0) P.c.stage_sparse = s->tune_stage_sparse;
+  if (s->tune_stage_dense >= 0) P.c.stage_dense = s->tune_stage_dense;
   P.G = pbf::Geometry{nullptr, nullptr};
   P.grid = &s->grid;
   P.sol = &s->sol;
@@ -1033,9 +1058,11 @@ struct pbf_batch {
   cudaGraphExec_t exec;
   GraphCache cache;
   std::vector<pbf::SceneGeom> geom_dev;  // the scene table as last uploaded
-  int tune_window = 0;  // dense-kernel and order choices (pbf_batch_autotune); 0 / -1: the defaults
+  int tune_window = 0;  // dense-kernel, order and staging choices (pbf_batch_autotune); 0 / -1: the defaults
   int tune_all = -1;
   int tune_order = -1;
+  int tune_stage_sparse = -1;
+  int tune_stage_dense = -1;
 };
 
 namespace {
@@ -1131,7 +1158,8 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
   if (e == cudaSuccess) e = alloc(&b->sol.iid_s, np);
   if (e == cudaSuccess) e = alloc(&b->sol.lambda, np);
   if (e == cudaSuccess) e = alloc(&b->sol.rho, np);
-  if (e == cudaSuccess) e = alloc(&b->sol.flags, (size_t)pbf::kNumFlags);
+  if (e == cudaSuccess) e = alloc(&b->sol.flags, (size_t)pbf::kFlagWords);
+  if (e == cudaSuccess) e = cudaMemset(b->sol.flags, 0, sizeof(uint32_t) * pbf::kFlagWords);
   if (e == cudaSuccess) e = alloc(&b->sol.dense, pbf::dense_list_len((int)np));
   if (e == cudaSuccess) e = alloc(&b->sol.masks, (size_t)pbf::kMaskWords * np);
   b->sol.mask_stride = (int)np;
@@ -1147,6 +1175,7 @@ pbf_status pbf_batch_create(const pbf_params* params, int nscenes, const float* 
       for (int j = 0; j < counts[sc]; ++j) sid[k++] = (uint16_t)sc;
     e = cudaMemcpy(b->d_sid, sid.data(), sizeof(uint16_t) * np, cudaMemcpyHostToDevice);
   }
+  if (e == cudaSuccess) e = pbf::set_pass_kernel_attributes();
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     batch_free(b);
@@ -1219,6 +1248,8 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   if (b->tune_window > 0) P.c.dense_window = b->tune_window;
   P.c.dense_all = b->tune_all;
   if (b->tune_order >= 0) P.c.order = b->tune_order;
+  if (b->tune_stage_sparse >= 0) P.c.stage_sparse = b->tune_stage_sparse;
+  if (b->tune_stage_dense >= 0) P.c.stage_dense = b->tune_stage_dense;
   P.G = pbf::Geometry{b->d_geom, b->d_sid};
   P.grid = &b->grid;
   P.sol = &b->sol;
@@ -1306,9 +1337,19 @@ namespace {
 
 // Candidate dense-kernel choices, timed by pbf_autotune / pbf_batch_autotune.
 constexpr int kTuneWindows[] = {64, 128, 256, 512, 1024, 2048};
+// Candidate stage sizes (slots per block) of the sparse and dense kernels.
+constexpr int kTuneStageSparse[] = {0, 1024, 2048};
+constexpr int kTuneStageDense[] = {0, 1536, 3072};
+
+// One configuration of the neighbour passes.
+struct TuneChoice {
+  int window, all, order, stage_sparse, stage_dense;
+};
 
 // Runs `steps` steps per candidate on copies of (pos, vel, iid) through
-// step(window, all, bufs...) and returns the fastest choice.
+// step(choice, bufs...) and returns the fastest choice: first over the
+// window, dense and order choices with the default stages, then, from the
+// best of those, over the sparse kernel's stage, then the dense kernel's.
 template <class Step>
 pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid, int steps, cudaStream_t st,
                     Step step, pbf_tuning* out) {
@@ -1325,50 +1366,66 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   pbf_status result = PBF_OK;
-  float best = -1.f, def_ms = -1.f;
-  int best_w = pbf::kDefaultDenseWindow, best_all = -1, best_ord = 1;
-  for (int ord = 1; ord >= 0 && e == cudaSuccess && result == PBF_OK; --ord)
-  for (int all = 0; all <= 1 && e == cudaSuccess && result == PBF_OK; ++all) {
-    for (int w : kTuneWindows) {
-      if (all == 1 && w != pbf::kDefaultDenseWindow) continue;  // the window plays no part then
-      e = cudaMemcpyAsync(p[0], pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(v[0], vel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
-      if (e == cudaSuccess) e = cudaMemcpyAsync(id, iid, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
-      if (e != cudaSuccess) break;
-      int cur = 0;
-      float ms = 0.f;
-      for (int k = -1; k < steps && result == PBF_OK; ++k) {  // one untimed step first
-        if (k == 0) e = cudaEventRecord(e0, st);
-        result = step(w, all, ord, p[cur], p[1 - cur], v[cur], v[1 - cur], id, st);
-        cur = 1 - cur;
-      }
-      if (result != PBF_OK) break;
-      if (e == cudaSuccess) e = cudaEventRecord(e1, st);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-      if (e != cudaSuccess) break;
-      ms /= (float)steps;
-      const bool is_default =
-          ord == 1 && w == pbf::kDefaultDenseWindow && all == (n < pbf::kDenseAllBelow ? 1 : 0);
-      if (is_default) def_ms = ms;
-      if (best < 0.f || ms < best) {
-        best = ms;
-        best_w = w;
-        best_all = all;
-        best_ord = ord;
-      }
+  // ms per step of one choice (negative: a failure, recorded in e / result)
+  auto time_choice = [&](const TuneChoice& ch) -> float {
+    if (e != cudaSuccess || result != PBF_OK) return -1.f;
+    e = cudaMemcpyAsync(p[0], pos, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(v[0], vel, sizeof(float4) * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(id, iid, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return -1.f;
+    int cur = 0;
+    float ms = 0.f;
+    for (int k = -1; k < steps && result == PBF_OK; ++k) {  // one untimed step first
+      if (k == 0) e = cudaEventRecord(e0, st);
+      if (e != cudaSuccess) return -1.f;
+      result = step(ch, p[cur], p[1 - cur], v[cur], v[1 - cur], id, st);
+      cur = 1 - cur;
     }
-  }
+    if (result != PBF_OK) return -1.f;
+    e = cudaEventRecord(e1, st);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    return e == cudaSuccess ? ms / (float)steps : -1.f;
+  };
+  const TuneChoice def{pbf::kDefaultDenseWindow, n < pbf::kDenseAllBelow ? 1 : 0, 1, pbf::kDefaultStageSparse,
+                       pbf::kDefaultStageDense};
+  float best = -1.f, def_ms = -1.f;
+  TuneChoice best_ch{pbf::kDefaultDenseWindow, -1, 1, pbf::kDefaultStageSparse, pbf::kDefaultStageDense};
+  auto consider = [&](const TuneChoice& ch) {
+    const float ms = time_choice(ch);
+    if (ms < 0.f) return;
+    if (ch.window == def.window && ch.all == def.all && ch.order == def.order &&
+        ch.stage_sparse == def.stage_sparse && ch.stage_dense == def.stage_dense)
+      def_ms = ms;
+    if (best < 0.f || ms < best) {
+      best = ms;
+      best_ch = ch;
+    }
+  };
+  for (int ord = 1; ord >= 0; --ord)
+    for (int all = 0; all <= 1; ++all)
+      for (int w : kTuneWindows) {
+        if (all == 1 && w != pbf::kDefaultDenseWindow) continue;  // the window plays no part then
+        consider(TuneChoice{w, all, ord, pbf::kDefaultStageSparse, pbf::kDefaultStageDense});
+      }
+  const TuneChoice base = best_ch;
+  for (int ss : kTuneStageSparse)
+    if (ss != base.stage_sparse && !base.all) consider(TuneChoice{base.window, base.all, base.order, ss, base.stage_dense});
+  const TuneChoice base2 = best_ch;
+  for (int sd : kTuneStageDense)
+    if (sd != base2.stage_dense) consider(TuneChoice{base2.window, base2.all, base2.order, base2.stage_sparse, sd});
   for (void* q : {(void*)p[0], (void*)p[1], (void*)v[0], (void*)v[1], (void*)id})
     if (q) cudaFree(q);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (result != PBF_OK) return result;
   if (e != cudaSuccess) return cuda_fail(e, "pbf_autotune");
-  out->dense_window = best_w;
-  out->dense_all = best_all;
-  out->order = best_ord;
+  out->dense_window = best_ch.window;
+  out->dense_all = best_ch.all;
+  out->order = best_ch.order;
   out->bwd_lanes = 0;
+  out->stage_sparse = best_ch.stage_sparse;
+  out->stage_dense = best_ch.stage_dense;
   out->ms_per_step = best;
   out->ms_default = def_ms;
   return PBF_OK;
@@ -1386,12 +1443,15 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
   const int depth = s->tape_depth, top = s->tape_top;
   s->tape_depth = 0;  // the trial steps are not taped
   const int w0 = s->tune_window, a0 = s->tune_all, o0 = s->tune_order;
+  const int ss0 = s->tune_stage_sparse, sd0 = s->tune_stage_dense;
   const pbf_status st = autotune(
       n, pos, vel, iid, steps, (cudaStream_t)stream,
-      [&](int w, int all, int ord, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
-        s->tune_window = w;
-        s->tune_all = all;
-        s->tune_order = ord;
+      [&](const TuneChoice& ch, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+        s->tune_window = ch.window;
+        s->tune_all = ch.all;
+        s->tune_order = ch.order;
+        s->tune_stage_sparse = ch.stage_sparse;
+        s->tune_stage_dense = ch.stage_dense;
         return pbf_step(s, p, np, v, nv, id, n, strm);
       },
       out);
@@ -1401,11 +1461,15 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
     s->tune_window = w0;
     s->tune_all = a0;
     s->tune_order = o0;
+    s->tune_stage_sparse = ss0;
+    s->tune_stage_dense = sd0;
     return st;
   }
   s->tune_window = out->dense_window;
   s->tune_all = out->dense_all;
   s->tune_order = out->order;
+  s->tune_stage_sparse = out->stage_sparse;
+  s->tune_stage_dense = out->stage_dense;
   out->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;  // not timed: kept
   return PBF_OK;
 }
@@ -1420,10 +1484,16 @@ pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
     return fail(PBF_ERR_INVALID_ARG, "order must be -1, 0 or 1 (got %d)", t->order);
   if (t->bwd_lanes != 0 && t->bwd_lanes != 8 && t->bwd_lanes != 16 && t->bwd_lanes != 32)
     return fail(PBF_ERR_INVALID_ARG, "bwd_lanes must be 0, 8, 16 or 32 (got %d)", t->bwd_lanes);
+  if (t->stage_sparse < -1 || t->stage_sparse > pbf::kStageMax || t->stage_dense < -1 ||
+      t->stage_dense > pbf::kStageMax)
+    return fail(PBF_ERR_INVALID_ARG, "stage_sparse / stage_dense must be -1 to %d (got %d / %d)", pbf::kStageMax,
+                t->stage_sparse, t->stage_dense);
   s->tune_window = t->dense_window;
   s->tune_all = t->dense_all;
   s->tune_order = t->order;
   s->tune_bwd_lanes = t->bwd_lanes;
+  s->tune_stage_sparse = t->stage_sparse;
+  s->tune_stage_dense = t->stage_dense;
   return PBF_OK;
 }
 
@@ -1433,9 +1503,21 @@ pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
   t->dense_all = s->tune_all;
   t->order = s->tune_order >= 0 ? s->tune_order : 1;
   t->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;
+  t->stage_sparse = s->tune_stage_sparse >= 0 ? s->tune_stage_sparse : pbf::kDefaultStageSparse;
+  t->stage_dense = s->tune_stage_dense >= 0 ? s->tune_stage_dense : pbf::kDefaultStageDense;
   t->ms_per_step = 0.f;
   t->ms_default = 0.f;
   return PBF_OK;
+}
+
+pbf_status pbf_check_device(pbf_solver* s, void* stream) {
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  return check_device_word(s->sol.flags + pbf::kErrorWord, (cudaStream_t)stream, "pbf_check_device");
+}
+
+pbf_status pbf_batch_check_device(pbf_batch* b, void* stream) {
+  if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
+  return check_device_word(b->sol.flags + pbf::kErrorWord, (cudaStream_t)stream, "pbf_batch_check_device");
 }
 
 pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, const uint32_t* iid, int steps,
@@ -1443,12 +1525,15 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
   const pbf::NvtxRange range("pbf_batch_autotune");
   if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
   const int w0 = b->tune_window, a0 = b->tune_all, o0 = b->tune_order;
+  const int ss0 = b->tune_stage_sparse, sd0 = b->tune_stage_dense;
   const pbf_status st = autotune(
       b->n, pos, vel, iid, steps, (cudaStream_t)stream,
-      [&](int w, int all, int ord, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
-        b->tune_window = w;
-        b->tune_all = all;
-        b->tune_order = ord;
+      [&](const TuneChoice& ch, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+        b->tune_window = ch.window;
+        b->tune_all = ch.all;
+        b->tune_order = ch.order;
+        b->tune_stage_sparse = ch.stage_sparse;
+        b->tune_stage_dense = ch.stage_dense;
         return pbf_batch_step(b, p, np, v, nv, id, strm);
       },
       out);
@@ -1456,11 +1541,15 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
     b->tune_window = w0;
     b->tune_all = a0;
     b->tune_order = o0;
+    b->tune_stage_sparse = ss0;
+    b->tune_stage_dense = sd0;
     return st;
   }
   b->tune_window = out->dense_window;
   b->tune_all = out->dense_all;
   b->tune_order = out->order;
+  b->tune_stage_sparse = out->stage_sparse;
+  b->tune_stage_dense = out->stage_dense;
   return PBF_OK;
 }
 

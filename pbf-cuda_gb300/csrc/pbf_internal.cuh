@@ -58,6 +58,8 @@ struct StepConsts {
   int dense_window;        // candidates above which a warp takes the dense kernel
   int dense_all;           // 1: every warp takes the dense kernel; 0: never; -1: by particle count
   int order;               // 1: the passes take particles in current-cell order (bucketed); 0: grid order
+  int stage_sparse;        // slots a sparse-kernel block may stage in shared memory (0: none)
+  int stage_dense;         // slots a dense-kernel block may stage in shared memory (0: none)
   SceneGeom geom;          // the box of a single-scene step
 };
 
@@ -286,6 +288,19 @@ enum StepFlag {
   kNumFlags = 11
 };
 
+// One more word after the step flags, cleared only when the host reads it:
+// device-side errors (ErrorBit) recorded by any step since.
+constexpr int kErrorWord = kNumFlags;
+constexpr int kFlagWords = kNumFlags + 1;
+enum ErrorBit : uint32_t {
+  kErrStageTimeout = 1u,     // a shared-memory staging copy did not complete in time
+};
+
+// Largest stage (slots, 16 bytes each) a neighbour-pass block may ask for;
+// the pass kernels allow that much dynamic shared memory (set_pass_kernel_attributes).
+constexpr int kStageMax = 4096;
+cudaError_t set_pass_kernel_attributes();
+
 // Entries of the dense list: one per particle.
 constexpr size_t dense_list_len(int max_particles) { return (size_t)max_particles + 1; }
 
@@ -316,6 +331,13 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
 // count below which every warp does (defaults; pbf_autotune can override).
 constexpr int kDefaultDenseWindow = 512;
 constexpr int kDenseAllBelow = 131072;
+// Slots a block of the sparse / dense pass kernel stages in shared memory
+// (defaults; 0: no staging; pbf_autotune can override, up to kStageMax).
+// Sparse: 16 KB of dynamic shared memory beside the 16 KB hit queue; dense:
+// 24 KB beside the queue and partial sums -- both under the 48 KB a launch
+// gets without the kernel attribute.
+constexpr int kDefaultStageSparse = 0;
+constexpr int kDefaultStageDense = 0;
 
 // Vorticity confinement after XSPH, on its output NV (positions X = npos):
 // omega_i = sum_j (u_j - u_i) x g_ij and eta_i = sum_j |omega_j| g_ij over

@@ -190,77 +190,163 @@ __device__ __forceinline__ int window_chunks(const SceneGeom& g, const uint32_t*
   return chunks;
 }
 
+// ---- where a pass reads candidate positions ---------------------------------------------
+//
+// From global memory (X[j], read-only path), or from the block's staged copy
+// of its window in shared memory.  Run r = 3 (dx + 1) + (dy + 1) of a window
+// is one column of three z-consecutive cells; a block stages, per run, the
+// slots of the z-range its particles' runs cover, and slot j of run r sits at
+// S[j + D[r]].  Either source gives bitwise the same positions, so a pass's
+// sums do not depend on which one it read.
+struct FromGlobal {
+  const float4* __restrict__ X;
+  __device__ __forceinline__ float4 at(int j, int) const { return __ldg(X + j); }
+  // hit-queue entry of a chunk starting at slot j of run r, and back
+  __device__ __forceinline__ int tag(int j, int) const { return j; }
+  __device__ __forceinline__ float4 untag(int t, int bit, int& j) const {
+    j = t + bit;
+    return __ldg(X + j);
+  }
+};
+
+struct FromStage {
+  const float4* S;  // shared memory: the staged runs
+  const int* D;     // shared memory: per run, staged index - slot
+  __device__ __forceinline__ float4 at(int j, int r) const { return S[j + D[r]]; }
+  // staged index (< 2^16) and run
+  __device__ __forceinline__ int tag(int j, int r) const { return (j + D[r]) | (r << 16); }
+  __device__ __forceinline__ float4 untag(int t, int bit, int& j) const {
+    const int v = (t & 0xffff) + bit;
+    j = v - D[t >> 16];
+    return S[v];
+  }
+};
+
 // Every candidate of the window, in order.
-template <class P>
+template <class P, class Src>
 __device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t* __restrict__ cs,
-                                             int n, int3 q, const float4* __restrict__ X, P& p) {
+                                             int n, int3 q, const Src& src, P& p) {
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
     if (x < 0 || x >= g.dims[0]) continue;
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
       if (y < 0 || y >= g.dims[1]) continue;
+      const int r = 3 * (dx + 1) + (dy + 1);
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
-      for (int j = s; j < e; ++j) p.visit(__ldg(X + j), j);
+      for (int j = s; j < e; ++j) p.visit(src.at(j, r), j);
     }
   }
 }
 
-// Candidates [j0, j1) of one run, in order: with skip_misses (the pass's exact
-// rules do not need every candidate) a hit mask per chunk of 32 (four loads in
-// flight), then p.visit() on the set bits; else every candidate, four loads in
-// flight.  Same result as visiting each candidate in turn.
-template <class P>
-__device__ __forceinline__ void visit_run(const float4* __restrict__ X, int j0, int j1, P& p, bool skip_misses) {
-  if (skip_misses) {
-    for (int jb = j0; jb < j1; jb += 32) {
-      const int m = min(32, j1 - jb);
-      uint32_t mask = 0u;
-      int k = 0;
-      for (; k + 3 < m; k += 4) {
-        const float4 a = __ldg(X + jb + k), b = __ldg(X + jb + k + 1), c2 = __ldg(X + jb + k + 2),
-                     d = __ldg(X + jb + k + 3);
-        mask |= (uint32_t)p.hit(a, jb + k) << k;
-        mask |= (uint32_t)p.hit(b, jb + k + 1) << (k + 1);
-        mask |= (uint32_t)p.hit(c2, jb + k + 2) << (k + 2);
-        mask |= (uint32_t)p.hit(d, jb + k + 3) << (k + 3);
+// ---- hit queue ------------------------------------------------------------------------
+//
+// The masked walks below test a chunk of up to 32 consecutive candidates at a
+// time into a bit mask (cheap, every lane busy) and run the pair body on the
+// set bits only.  Running the body right after each chunk costs a warp
+// max-over-lanes(hits of that chunk) body iterations per chunk; lanes whose
+// particle has fewer hits in that chunk idle, chunk after chunk.  Instead each
+// thread queues its non-empty chunks (mask + where the chunk starts) in shared
+// memory and HitQueue::flush runs the body once per queued hit in one flat
+// loop, so the warp pays max-over-lanes of the hits of the whole queued span.
+// Hits are visited in the order they were queued -- the window's visiting
+// order -- so the sums are bitwise those of visiting each chunk's hits right
+// away.  The capacity (chunks queued per thread before a flush) is a template
+// parameter of the kernel (1: the body right after each chunk).
+struct HitQueue {
+  uint32_t* mask;  // this thread's column: entry k at mask[k * stride]
+  int* base;       // where queued chunk k starts (Src::tag)
+  int stride;
+  int cap;
+  int n = 0;
+
+  __device__ HitQueue(uint32_t* mask_, int* base_, int stride_, int cap_)
+      : mask(mask_), base(base_), stride(stride_), cap(cap_) {}
+  template <class P, class Src>
+  __device__ __forceinline__ void flush(const Src& src, P& p) {
+    uint32_t m = 0u;
+    int b = 0, k = 0;
+    for (;;) {
+      if (!m) {
+        if (k == n) break;
+        m = mask[k * stride];  // every queued mask has a bit set
+        b = base[k * stride];
+        ++k;
       }
-      for (; k < m; ++k) mask |= (uint32_t)p.hit(__ldg(X + jb + k), jb + k) << k;
-      while (mask) {
-        const int b = __ffs(mask) - 1;
-        mask &= mask - 1u;
-        p.visit(__ldg(X + jb + b), jb + b);
-      }
+      const int bit = __ffs(m) - 1;
+      m &= m - 1u;
+      int j;
+      const float4 xj = src.untag(b, bit, j);
+      p.visit(xj, j);
     }
+    n = 0;
+  }
+  template <class P, class Src>
+  __device__ __forceinline__ void push(uint32_t m, int tag, const Src& src, P& p) {
+    if (!m) return;
+    mask[n * stride] = m;
+    base[n * stride] = tag;
+    if (++n == cap) flush(src, p);
+  }
+};
+
+// Hit mask of candidates [jb, jb + min(32, j1 - jb)) of run r (four loads in flight).
+template <class P, class Src>
+__device__ __forceinline__ uint32_t chunk_mask(const Src& src, int jb, int j1, int r, const P& p) {
+  const int m = min(32, j1 - jb);
+  uint32_t mask = 0u;
+  int k = 0;
+  for (; k + 3 < m; k += 4) {
+    const float4 a = src.at(jb + k, r), b = src.at(jb + k + 1, r), c2 = src.at(jb + k + 2, r),
+                 d = src.at(jb + k + 3, r);
+    mask |= (uint32_t)p.hit(a, jb + k) << k;
+    mask |= (uint32_t)p.hit(b, jb + k + 1) << (k + 1);
+    mask |= (uint32_t)p.hit(c2, jb + k + 2) << (k + 2);
+    mask |= (uint32_t)p.hit(d, jb + k + 3) << (k + 3);
+  }
+  for (; k < m; ++k) mask |= (uint32_t)p.hit(src.at(jb + k, r), jb + k) << k;
+  return mask;
+}
+
+// Candidates [j0, j1) of run r, in order: with skip_misses (the pass's exact
+// rules do not need every candidate) a hit mask per chunk of 32 (four loads in
+// flight), its hits queued for p.visit() (the caller flushes hq); else every
+// candidate, four loads in flight, after flushing what is queued.  Same result
+// as visiting each candidate in turn.
+template <class P, class Src>
+__device__ __forceinline__ void visit_run(const Src& src, int j0, int j1, int r, P& p, bool skip_misses,
+                                          HitQueue& hq) {
+  if (skip_misses) {
+    for (int jb = j0; jb < j1; jb += 32) hq.push(chunk_mask(src, jb, j1, r, p), src.tag(jb, r), src, p);
   } else {
+    hq.flush(src, p);
     int j = j0;
     for (; j + 3 < j1; j += 4) {
-      const float4 q0 = __ldg(X + j), q1 = __ldg(X + j + 1), q2 = __ldg(X + j + 2), q3 = __ldg(X + j + 3);
+      const float4 q0 = src.at(j, r), q1 = src.at(j + 1, r), q2 = src.at(j + 2, r), q3 = src.at(j + 3, r);
       p.visit(q0, j);
       p.visit(q1, j + 1);
       p.visit(q2, j + 2);
       p.visit(q3, j + 3);
     }
-    for (; j < j1; ++j) p.visit(__ldg(X + j), j);
+    for (; j < j1; ++j) p.visit(src.at(j, r), j);
   }
 }
 
 // Every candidate of the window, in order, in two stages per chunk of 32
 // consecutive slots of a run: a cheap test p.hit() of each candidate (four
 // loads in flight) into a bit mask, then p.visit() on the set bits in
-// ascending order.  p.visit() leaves non-hits untouched, so the result is that
-// of visit_window; the neighbour body runs max(hits) times per warp and chunk
-// instead of once per candidate.
+// ascending order, through the hit queue.  p.visit() leaves non-hits
+// untouched, so the result is that of visit_window.
 //
 // save_masks: store chunk k's mask at masks[k * stride + i] (k < kMaskWords)
 // for the next pass over the same positions.
-template <class P>
+template <class P, class Src>
 __device__ __forceinline__ void visit_window_masked(const SceneGeom& g,
                                                     const uint32_t* __restrict__ cs, int n,
-                                                    int3 q, const float4* __restrict__ X, P& p,
+                                                    int3 q, const Src& src, P& p,
                                                     uint32_t* __restrict__ masks, int stride,
-                                                    int i) {
+                                                    int i, HitQueue& hq) {
   int chunk = 0;
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
@@ -268,42 +354,30 @@ __device__ __forceinline__ void visit_window_masked(const SceneGeom& g,
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
       if (y < 0 || y >= g.dims[1]) continue;
+      const int r = 3 * (dx + 1) + (dy + 1);
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
       for (int j0 = s; j0 < e; j0 += 32) {
-        const int m = min(32, e - j0);
-        uint32_t mask = 0u;
-        int k = 0;
-        for (; k + 3 < m; k += 4) {
-          const float4 a = __ldg(X + j0 + k), b = __ldg(X + j0 + k + 1),
-                       c2 = __ldg(X + j0 + k + 2), d = __ldg(X + j0 + k + 3);
-          mask |= (uint32_t)p.hit(a, j0 + k) << k;
-          mask |= (uint32_t)p.hit(b, j0 + k + 1) << (k + 1);
-          mask |= (uint32_t)p.hit(c2, j0 + k + 2) << (k + 2);
-          mask |= (uint32_t)p.hit(d, j0 + k + 3) << (k + 3);
-        }
-        for (; k < m; ++k) mask |= (uint32_t)p.hit(__ldg(X + j0 + k), j0 + k) << k;
+        const uint32_t mask = chunk_mask(src, j0, e, r, p);
         if (masks && chunk < kMaskWords) masks[chunk * stride + i] = mask;
         ++chunk;
-        while (mask) {
-          const int b = __ffs(mask) - 1;
-          mask &= mask - 1u;
-          p.visit(__ldg(X + j0 + b), j0 + b);
-        }
+        hq.push(mask, src.tag(j0, r), src, p);
       }
     }
   }
+  hq.flush(src, p);
 }
 
 // The window's neighbours from the masks a previous pass over the same
 // positions saved (visit_window_masked with save): p.visit() on the set bits,
-// in order.  The saved hits are a superset of p's (p.visit re-tests).
-template <class P>
+// in order, through the hit queue.  The saved hits are a superset of p's
+// (p.visit re-tests).
+template <class P, class Src>
 __device__ __forceinline__ void visit_window_saved(const SceneGeom& g,
                                                    const uint32_t* __restrict__ cs, int n, int3 q,
-                                                   const float4* __restrict__ X, P& p,
+                                                   const Src& src, P& p,
                                                    const uint32_t* __restrict__ masks, int stride,
-                                                   int i) {
+                                                   int i, HitQueue& hq) {
   int chunk = 0;
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
@@ -311,18 +385,14 @@ __device__ __forceinline__ void visit_window_saved(const SceneGeom& g,
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
       if (y < 0 || y >= g.dims[1]) continue;
+      const int r = 3 * (dx + 1) + (dy + 1);
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
-      for (int j0 = s; j0 < e; j0 += 32, ++chunk) {
-        uint32_t mask = __ldg(masks + chunk * stride + i);
-        while (mask) {
-          const int b = __ffs(mask) - 1;
-          mask &= mask - 1u;
-          p.visit(__ldg(X + j0 + b), j0 + b);
-        }
-      }
+      for (int j0 = s; j0 < e; j0 += 32, ++chunk)
+        hq.push(__ldg(masks + chunk * stride + i), src.tag(j0, r), src, p);
     }
   }
+  hq.flush(src, p);
 }
 
 // Candidates [v_lo, v_hi) of the window (numbered in visiting order), four
@@ -398,9 +468,9 @@ __device__ __forceinline__ int window_total_grouped(const SceneGeom& g, const Pa
 // contributing their groups (p.visit_group; `own`: i belongs to the cell) and
 // the other cells their particles (p.visit).  Without grouped cells this
 // visits exactly what visit_window_chunk does, in the same order.
-template <class P>
+template <class P, class Src>
 __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const PassArgs& a, int3 q,
-                                                     P& p, int v_lo, int v_hi) {
+                                                     const Src& src, P& p, int v_lo, int v_hi, HitQueue& hq) {
   const int zlo = max(q.z - 1, 0), zhi = min(q.z + 1, g.dims[2] - 1);
   int v0 = 0;
   for (int dx = -1; dx <= 1; ++dx) {
@@ -409,6 +479,7 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
       if (y < 0 || y >= g.dims[1]) continue;
+      const int r = 3 * (dx + 1) + (dy + 1);
       const int base = g.cell_base + (x * g.dims[1] + y) * g.dims[2];
       for (int z = zlo; z <= zhi; ++z) {
         int slot;
@@ -419,6 +490,7 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
         const int lo = max(v_lo, v0), hi = min(v_hi, v0 + len);
         if (lo < hi) {
           if (ng > 0) {
+            hq.flush(src, p);  // queued hits come first in visiting order
             const int t0 = __ldg(a.grp_off + slot);
             const bool own = p.i >= s0 && p.i < e0;  // i is one of the cell's particles
             int t = t0 + (lo - v0);
@@ -441,13 +513,14 @@ __device__ __forceinline__ void visit_window_grouped(const SceneGeom& g, const P
               p.visit_group(__ldg(a.grp_pos + t), __ldg(a.grp_cnt + t), __ldg(a.grp_sum + t),
                             __ldg(a.grp_aux + t), own);
           } else {
-            visit_run(a.X, s0 + (lo - v0), s0 + (hi - v0), p, p.skip_misses());
+            visit_run(src, s0 + (lo - v0), s0 + (hi - v0), r, p, p.skip_misses(), hq);
           }
         }
         v0 += len;
       }
     }
   }
+  hq.flush(src, p);
 }
 
 // ---- the passes: per-candidate visit, partial-sum fields, finish ----------------------
@@ -733,11 +806,231 @@ __device__ __forceinline__ bool exact_path(int kind, const PassArgs& a, const Sc
   return false;
 }
 
+// ---- window staging: bulk async copies into shared memory ------------------------------
+//
+// With the passes taking particles in current-cell order, the particles of a
+// block usually sit in cells of one column (scene, x, y), z-consecutive: their
+// windows are then made of the same 9 column runs, each particle's run r a
+// z-sub-range of the block's run r, which covers cells [zmin - 1, zmax + 1] of
+// column (x + dx, y + dy) -- one contiguous range of sorted slots.  Such a
+// block copies its runs' positions (16 bytes a slot, 16-byte aligned) into
+// shared memory with one cp.async.bulk per run, all completing on one
+// mbarrier, and its threads then walk their windows there (FromStage) instead
+// of through L1 (FromGlobal).  Blocks whose particles span several columns,
+// whose runs exceed the stage, or whose runs hold a grouped cell read global
+// memory as before.  The wait is bounded: past kStageSpins polls the block
+// records kErrStageTimeout, stops staging and reads global memory (same
+// results), and waits once more (bounded) for the copy before it exits.
+
+constexpr int kStageSpins = 1 << 20;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0u;
+}
+// Bounded wait for the phase of the given parity to complete.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (int k = 0; k < kStageSpins; ++k)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// bytes (a multiple of 16) from global src to shared dst (both 16-byte
+// aligned), completing as transaction bytes on bar.  A CTA's own shared
+// memory address is a valid shared::cluster address (no cluster launch, no
+// multicast).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// Orders this thread's earlier generic-proxy accesses of shared memory (the
+// previous item's reads of the stage) before its following async-proxy writes.
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// A block's staging state in shared memory.
+struct StageState {
+  uint64_t bar;
+  int D[9];           // per run: staged index - first slot
+  int ok;             // this item's runs are staged
+  int failed;         // a wait gave up: the block stages no more
+  int wx[kDenseThreads / 32], wy[kDenseThreads / 32], wcb[kDenseThreads / 32];
+  int wzmin[kDenseThreads / 32], wzmax[kDenseThreads / 32], wi[kDenseThreads / 32];
+  int wsame[kDenseThreads / 32];
+};
+
+// Votes of one warp: whether its participating lanes share (scene, x, y), the
+// z-range they cover and one participating particle (lane 0 of the warp writes
+// st.w*[w]).  Every lane of the warp calls it.
+__device__ __forceinline__ void stage_vote(StageState& st, int w, bool part, const SceneGeom& g, int3 q,
+                                           int i) {
+  const unsigned pm = __ballot_sync(kFull, part);
+  const int lead = pm ? __ffs(pm) - 1 : 0;
+  const int lx = __shfl_sync(kFull, q.x, lead), ly = __shfl_sync(kFull, q.y, lead);
+  const int lcb = __shfl_sync(kFull, g.cell_base, lead), li = __shfl_sync(kFull, i, lead);
+  const bool same = __all_sync(kFull, !part || (q.x == lx && q.y == ly && g.cell_base == lcb));
+  const int zmin = __reduce_min_sync(kFull, part ? q.z : INT_MAX);
+  const int zmax = __reduce_max_sync(kFull, part ? q.z : INT_MIN);
+  if ((threadIdx.x & 31) == 0) {
+    st.wsame[w] = pm == 0u ? -1 : (same ? 1 : 0);  // -1: no participating lane
+    st.wx[w] = lx, st.wy[w] = ly, st.wcb[w] = lcb, st.wi[w] = li;
+    st.wzmin[w] = zmin, st.wzmax[w] = zmax;
+  }
+}
+
+// Thread 0, after the votes of warps [0, nw): when every participating lane
+// shares one column and its runs fit in `cap` slots and hold no grouped cell,
+// sets st.D, arms st.bar for the runs' bytes and issues one bulk copy per
+// non-empty run into S; st.ok says whether it did.
+__device__ __forceinline__ void stage_issue(StageState& st, int nw, const PassArgs& a, float4* S, int cap) {
+  st.ok = 0;
+  if (st.failed || cap <= 0) return;
+  int w0 = -1, zmin = INT_MAX, zmax = INT_MIN;
+  for (int w = 0; w < nw; ++w) {
+    if (st.wsame[w] < 0) continue;
+    if (st.wsame[w] == 0) return;
+    if (w0 < 0) {
+      w0 = w;
+    } else if (st.wx[w] != st.wx[w0] || st.wy[w] != st.wy[w0] || st.wcb[w] != st.wcb[w0]) {
+      return;
+    }
+    zmin = min(zmin, st.wzmin[w]);
+    zmax = max(zmax, st.wzmax[w]);
+  }
+  if (w0 < 0) return;
+  const SceneGeom g = geom_of(a.c, a.G, st.wi[w0]);
+  const int x0 = st.wx[w0], y0 = st.wy[w0];
+  const int zlo = max(zmin - 1, 0), zhi = min(zmax + 1, g.dims[2] - 1);
+  const bool groups = a.flags[kGroupCount] != 0u;
+  int s[9], e[9], total = 0;
+  for (int r = 0; r < 9; ++r) {
+    const int x = x0 + r / 3 - 1, y = y0 + r % 3 - 1;
+    s[r] = e[r] = 0;
+    if (x < 0 || x >= g.dims[0] || y < 0 || y >= g.dims[1]) continue;
+    const int base = g.cell_base + (x * g.dims[1] + y) * g.dims[2];
+    s[r] = (int)__ldg(a.cs + base + zlo);
+    e[r] = max(min((int)__ldg(a.cs + base + zhi + 1), a.n), s[r]);
+    total += e[r] - s[r];
+    if (groups)
+      for (int z = zlo; z <= zhi; ++z)
+        if (__ldg(a.cell_flags + base + z) >> kCellSlotShift) return;  // a grouped cell
+  }
+  if (total > cap) return;
+  fence_proxy_async_smem();
+  mbar_arrive_expect_tx(&st.bar, (uint32_t)total * (uint32_t)sizeof(float4));
+  int v = 0;
+  for (int r = 0; r < 9; ++r) {
+    st.D[r] = v - s[r];
+    const int len = e[r] - s[r];
+    if (len > 0) bulk_g2s(S + v, a.X + s[r], (uint32_t)len * (uint32_t)sizeof(float4), &st.bar);
+    v += len;
+  }
+  st.ok = 1;
+}
+
+// Every thread, after stage_issue and a barrier: waits (bounded) for the
+// staged runs.  Returns whether the item reads them; a wait that gave up
+// (block-uniform through the barrier) records the error and stops staging.
+__device__ __forceinline__ bool stage_wait(StageState& st, const PassArgs& a, uint32_t& phase) {
+  if (!st.ok) return false;  // uniform: written before the barrier
+  const bool done = mbar_wait_bounded(&st.bar, phase);
+  const bool any_failed = __syncthreads_or(!done);
+  if (any_failed) {
+    if (threadIdx.x == 0) {
+      st.failed = 1;
+      atomicOr(&a.flags[kErrorWord], (uint32_t)kErrStageTimeout);
+    }
+    return false;  // st.failed is read only after the next barrier
+  }
+  phase ^= 1u;
+  return true;
+}
+
+// Before a block that staged exits: a wait that gave up leaves its copy in
+// flight, so wait once more (bounded) for it.
+__device__ __forceinline__ void stage_drain(StageState& st, uint32_t phase) {
+  if (threadIdx.x == 0 && st.failed) mbar_wait_bounded(&st.bar, phase);
+}
+
 // ---- kernels ------------------------------------------------------------------------
 
+// The plain (not grouped) walk of a sparse-kernel particle's window.
+template <int kKind, class P, class Src>
+__device__ __forceinline__ void sparse_visit(const PassArgs& a, const SceneGeom& g, int3 q, const Src& src,
+                                             P& p, bool exact, int i, HitQueue& hq) {
+  if (exact) {
+    visit_window(g, a.cs, a.n, q, src, p);  // non-neighbours matter: visit every candidate
+  } else if (kKind == kLambda) {
+    visit_window_masked(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // saves its masks
+  } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) &&
+             window_chunks(g, a.cs, a.n, q) <= kMaskWords) {
+    visit_window_saved(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // lambda's masks
+  } else {
+    visit_window_masked(g, a.cs, a.n, q, src, p, nullptr, 0, i, hq);
+  }
+}
+
+// The stage's barrier, before first use (thread 0).
+__device__ __forceinline__ void stage_init(StageState& st) {
+  st.failed = 0;
+  st.ok = 0;
+  mbar_init(&st.bar, 1u);
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Hit-queue capacities (chunks per thread) of the two pass kernels.
+// PBF_SPARSE_QUEUE / PBF_DENSE_QUEUE: build-time tuning macros.
+#ifndef PBF_SPARSE_QUEUE
+#define PBF_SPARSE_QUEUE 16
+#endif
+#ifndef PBF_DENSE_QUEUE
+#define PBF_DENSE_QUEUE 8
+#endif
+constexpr int kSparseQueue = PBF_SPARSE_QUEUE;
+constexpr int kDenseQueue = PBF_DENSE_QUEUE;
+
+// One thread slot of the work list (or of all particles) per thread; the
+// grid covers every particle, blocks past the list's end return at once.
+// PBF_SPARSE_MIN_BLOCKS (a build-time tuning macro): resident blocks per SM the
+// compiler must allow for, which caps the sparse kernels' registers.
+#ifdef PBF_SPARSE_MIN_BLOCKS
+#define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads, PBF_SPARSE_MIN_BLOCKS)
+#else
+#define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads)
+#endif
+
 template <int kKind>
-__device__ __forceinline__ void sparse_slot(const PassArgs& a, int t, int count) {
+__global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   using P = typename PassOf<kKind>::type;
+  __shared__ uint32_t q_mask[kSparseQueue * kSparseThreads];
+  __shared__ int q_base[kSparseQueue * kSparseThreads];
+  __shared__ StageState st;
+  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_sparse slots when staging
+  if (a.dense_all) return;
+  const int count = work_count(a);
+  if ((int)(blockIdx.x * kSparseThreads) >= count) return;  // uniform over the block
+  HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kSparseThreads, kSparseQueue);
+  const int t = blockIdx.x * kSparseThreads + threadIdx.x;
   const bool valid = t < count;
   const int i = valid ? work_particle(a, t) : 0;
   const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -761,53 +1054,52 @@ __device__ __forceinline__ void sparse_slot(const PassArgs& a, int t, int count)
     base = __shfl_sync(kFull, base, leader);
     if (go_dense) a.dense[base + __popc(dmask & ((1u << lane) - 1u))] = (uint32_t)t;
   }
-  if (!valid || go_dense) return;
-  const bool exact = exact_path(kKind, a, g, q, i);
-  P p(a, g, xi, i, exact);
-  if (grouped) {
-    visit_window_grouped(g, a, q, p, 0, entries);
-  } else if (exact) {
-    visit_window(g, a.cs, a.n, q, a.X, p);  // non-neighbours matter: visit every candidate
-  } else if (kKind == kLambda) {
-    visit_window_masked(g, a.cs, a.n, q, a.X, p, a.masks, a.mask_stride, i);  // saves its masks
-  } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) &&
-             window_chunks(g, a.cs, a.n, q) <= kMaskWords) {
-    visit_window_saved(g, a.cs, a.n, q, a.X, p, a.masks, a.mask_stride, i);  // lambda's masks
-  } else {
-    visit_window_masked(g, a.cs, a.n, q, a.X, p, nullptr, 0, i);
+  const bool active = valid && !go_dense;
+  const bool exact = active && exact_path(kKind, a, g, q, i);
+  // the block's plain windows staged in shared memory (block-uniform branch)
+  const int cap = a.c.stage_sparse;
+  bool staged = false;
+  uint32_t phase = 0u;
+  if (cap > 0) {
+    if (threadIdx.x == 0) stage_init(st);
+    stage_vote(st, threadIdx.x >> 5, active && !grouped, g, q, i);
+    __syncthreads();
+    if (threadIdx.x == 0) stage_issue(st, kSparseThreads / 32, a, stage, cap);
+    __syncthreads();
+    staged = stage_wait(st, a, phase);
   }
-  p.finish(a);
-}
-
-// One thread slot of the work list (or of all particles) per thread; the
-// grid covers every particle, blocks past the list's end return at once.
-// PBF_SPARSE_MIN_BLOCKS (a build-time tuning macro): resident blocks per SM the
-// compiler must allow for, which caps the sparse kernels' registers.
-#ifdef PBF_SPARSE_MIN_BLOCKS
-#define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads, PBF_SPARSE_MIN_BLOCKS)
-#else
-#define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads)
-#endif
-
-template <int kKind>
-__global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
-  if (a.dense_all) return;
-  const int count = work_count(a);
-  if ((int)(blockIdx.x * kSparseThreads) >= count) return;
-  sparse_slot<kKind>(a, blockIdx.x * kSparseThreads + threadIdx.x, count);
+  if (active) {
+    P p(a, g, xi, i, exact);
+    if (grouped)
+      visit_window_grouped(g, a, q, FromGlobal{a.X}, p, 0, entries, hq);
+    else if (staged)
+      sparse_visit<kKind>(a, g, q, FromStage{stage, st.D}, p, exact, i, hq);
+    else
+      sparse_visit<kKind>(a, g, q, FromGlobal{a.X}, p, exact, i, hq);
+    p.finish(a);
+  }
+  if (cap > 0) stage_drain(st, phase);
 }
 
 template <int kKind>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   using P = typename PassOf<kKind>::type;
   __shared__ float part[kDenseWarps][kMaxFields][32];
+  __shared__ uint32_t q_mask[kDenseQueue * kDenseThreads];
+  __shared__ int q_base[kDenseQueue * kDenseThreads];
+  __shared__ StageState st;
+  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_dense slots when staging
   static_assert(P::kFields <= kMaxFields, "partial-sum fields");
+  HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kDenseThreads, kDenseQueue);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cap = a.c.stage_dense;
+  if (threadIdx.x == 0 && cap > 0) stage_init(st);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
   // the slots the sparse kernel listed, or all of them, 32 per item
   const int work = work_count(a);
   const uint32_t listed = a.dense_all ? (uint32_t)work : a.flags[a.counter];
   const uint32_t count = (listed + 31) / 32;
+  uint32_t phase = 0u;
   for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
     const uint32_t e = item * 32 + lane;
     const bool valid = e < listed;
@@ -819,13 +1111,27 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     const bool exact = valid && exact_path(kKind, a, g, q, i);
     // grouped cells are visited by groups (the exact rules apply per group)
     const bool grouped = a.c.keps2 > 0.f;
+    // the item's windows staged in shared memory: every warp holds the same
+    // 32 particles, so warp 0's vote is the block's (block-uniform branch)
+    bool staged = false;
+    if (cap > 0) {
+      if (warp == 0) stage_vote(st, 0, valid, g, q, i);
+      __syncthreads();  // also: the previous item's reads of the stage are done
+      if (threadIdx.x == 0) stage_issue(st, 1, a, stage, cap);
+      __syncthreads();
+      staged = stage_wait(st, a, phase);
+    }
     if (valid) {
       const int total = grouped ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
       const int lo = (int)((long long)total * warp / kDenseWarps);
       const int hi = (int)((long long)total * (warp + 1) / kDenseWarps);
       P p(a, g, xi, i, exact);
-      if (grouped)
-        visit_window_grouped(g, a, q, p, lo, hi);
+      // a staged window holds no grouped cell: the grouped walk visits its
+      // candidates in the order visit_window_chunk does
+      if (staged)
+        visit_window_grouped(g, a, q, FromStage{stage, st.D}, p, lo, hi, hq);
+      else if (grouped)
+        visit_window_grouped(g, a, q, FromGlobal{a.X}, p, lo, hi, hq);
       else
         visit_window_chunk(g, a.cs, a.n, q, a.X, p, lo, hi);
       p.store(&part[warp][0][lane], 32);
@@ -838,6 +1144,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     }
     __syncthreads();
   }
+  if (cap > 0) stage_drain(st, phase);
 }
 
 // Also registers every cell holding >= kGroupCell particles (its first
@@ -1518,13 +1825,34 @@ void use_buckets(PassArgs& a, const SolverScratch& s) {
 
 template <int kKind>
 cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
+  const size_t sparse_smem = sizeof(float4) * (size_t)max(a.c.stage_sparse, 0);
+  const size_t dense_smem = sizeof(float4) * (size_t)max(a.c.stage_dense, 0);
   if (!a.dense_all)  // else the sparse kernel has nothing to do
-    k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, 0, stream>>>(a);
-  k_dense<kKind><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
+    k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, sparse_smem, stream>>>(a);
+  k_dense<kKind><<<a.c.dense_grid, kDenseThreads, dense_smem, stream>>>(a);
   return cudaGetLastError();
 }
 
+template <int kKind>
+cudaError_t allow_stage(int bytes) {
+  cudaError_t e = cudaFuncSetAttribute(k_sparse<kKind>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_dense<kKind>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
+}
+
 }  // namespace
+
+// Lets the pass kernels take up to kStageMax staged slots of dynamic shared
+// memory (the current device; call before any capture).
+cudaError_t set_pass_kernel_attributes() {
+  const int bytes = (int)sizeof(float4) * kStageMax;
+  cudaError_t e = allow_stage<kLambda>(bytes);
+  if (e == cudaSuccess) e = allow_stage<kDeltaP>(bytes);
+  if (e == cudaSuccess) e = allow_stage<kDeltaPFinal>(bytes);
+  if (e == cudaSuccess) e = allow_stage<kXsph>(bytes);
+  return e;
+}
 
 cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos, const float4* vel,
                     const uint32_t* iid, int n, SolverScratch& s, cudaStream_t stream) {
@@ -1665,7 +1993,7 @@ k_vort_omega(StepConsts c, Geometry G, const float4* __restrict__ X, const float
   const float4 xi = X[i];
   const SceneGeom g = geom_of(c, G, i);
   VortOmega p{c, U, xi, U[i], i};
-  visit_window(g, cs, n, cell_of(c, g, xi), X, p);
+  visit_window(g, cs, n, cell_of(c, g, xi), FromGlobal{X}, p);
   W[i] = make_float4(p.wx, p.wy, p.wz, sqrtf(dist2(p.wx, p.wy, p.wz)));
 }
 
@@ -1677,7 +2005,7 @@ k_vort_force(StepConsts c, Geometry G, const float4* __restrict__ X, const float
   const float4 xi = X[i];
   const SceneGeom g = geom_of(c, G, i);
   VortEta p{c, W, xi, i};
-  visit_window(g, cs, n, cell_of(c, g, xi), X, p);
+  visit_window(g, cs, n, cell_of(c, g, xi), FromGlobal{X}, p);
   const float len = sqrtf(dist2(p.ex, p.ey, p.ez));
   if (!(len > 0.f) || !isfinite(len)) return;
   const float nx = p.ex / len, ny = p.ey / len, nz = p.ez / len;

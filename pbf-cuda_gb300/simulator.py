@@ -153,19 +153,27 @@ class Simulator:
                                    g_vel.data_ptr(), g_lim.data_ptr(), _stream_handle(stream)), "pbf_backward")
         return g_pos, g_vel, g_lim
 
-    def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, bwd_lanes: int = 0) -> None:
-        """The dense-kernel and particle-order choices of the following steps, and
-        the reverse pass's lanes per particle (pbf_set_tuning); 0 / -1: the defaults."""
+    def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, bwd_lanes: int = 0,
+                   stage_sparse: int = -1, stage_dense: int = -1) -> None:
+        """The dense-kernel, particle-order and shared-memory staging choices of
+        the following steps, and the reverse pass's lanes per particle
+        (pbf_set_tuning); 0 / -1: the defaults (stage_*: 0 turns staging off)."""
         t = PbfTuning()
         t.dense_window, t.dense_all, t.order = int(dense_window), int(dense_all), int(order)
         t.bwd_lanes = int(bwd_lanes)
+        t.stage_sparse, t.stage_dense = int(stage_sparse), int(stage_dense)
         check(self._L.pbf_set_tuning(self._h, ctypes.byref(t)), "pbf_set_tuning")
 
     def tuning(self) -> dict:
         t = PbfTuning()
         check(self._L.pbf_get_tuning(self._h, ctypes.byref(t)), "pbf_get_tuning")
         return {"dense_window": t.dense_window, "dense_all": t.dense_all, "order": t.order,
-                "bwd_lanes": t.bwd_lanes}
+                "bwd_lanes": t.bwd_lanes, "stage_sparse": t.stage_sparse, "stage_dense": t.stage_dense}
+
+    def check_device(self, stream=None) -> None:
+        """Raise PbfError (PBF_ERR_TIMEOUT) if a bounded device-side wait of the
+        steps since the last check gave up (pbf_check_device)."""
+        check(self._L.pbf_check_device(self._h, _stream_handle(stream)), "pbf_check_device")
 
     def autotune(self, pos: torch.Tensor, vel: torch.Tensor, iid: torch.Tensor, nparticle: Optional[int] = None,
                  steps: int = 3, stream=None) -> dict:

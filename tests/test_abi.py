@@ -35,26 +35,29 @@ def test_library_exports_every_declared_symbol(pbf):
     assert set(declared_functions()) <= exported
 
 
-def test_params_layout_matches_c(pbf, tmp_path):
+@pytest.mark.parametrize("cname, pyname", [("pbf_params", "PbfParams"), ("pbf_tuning", "PbfTuning"),
+                                           ("pbf_step_profile", "PbfStepProfile")])
+def test_struct_layout_matches_c(pbf, tmp_path, cname, pyname):
     """ctypes mirror == C struct (size and every field offset), checked by gcc."""
-    fields = [f for f, _ in pbf.PbfParams._fields_]
+    cls = getattr(pbf, pyname)
+    fields = [f for f, _ in cls._fields_]
     src = tmp_path / "layout.c"
     src.write_text(textwrap.dedent(f"""
         #include <stdio.h>
         #include <stddef.h>
         #include "{HEADER}"
         int main(void) {{
-          printf("%zu\\n", sizeof(pbf_params));
-          {''.join(f'printf("%zu\\n", offsetof(pbf_params, {f}));' for f in fields)}
+          printf("%zu\\n", sizeof({cname}));
+          {''.join(f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields)}
           return 0;
         }}
     """))
     exe = tmp_path / "layout"
     subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
     vals = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    assert vals[0] == ctypes.sizeof(pbf.PbfParams)
+    assert vals[0] == ctypes.sizeof(cls)
     for f, off in zip(fields, vals[1:]):
-        assert getattr(pbf.PbfParams, f).offset == off, f
+        assert getattr(cls, f).offset == off, f
 
 
 def test_max_particles_matches_header(pbf):

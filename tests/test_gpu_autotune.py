@@ -10,6 +10,9 @@ from test_gpu_parity import TOL_X, ref_params
 
 pytestmark = pytest.mark.gpu
 
+# the library's default shared-memory stages of the two pass kernels (slots)
+STAGE_DEFAULT = {"stage_sparse": 0, "stage_dense": 0}
+
 
 def test_autotune_single(pbf, oracle, cuda):
     import torch
@@ -79,18 +82,19 @@ def test_set_tuning_round_trip(pbf, oracle, cuda):
     vel = torch.zeros_like(pos)
     iid = torch.arange(n, dtype=torch.int32, device="cuda")
     with pbf.Simulator(p, sc.ulim, sc.llim, n) as sim:
-        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1, "bwd_lanes": 32}
+        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1, "bwd_lanes": 32, **STAGE_DEFAULT}
         sim.set_tuning(128, 0, 0)
-        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32}
-        for bad in ((16, 0), (256, 2), (256, -2), (0, -1, 2), (0, -1, -2), (0, -1, 1, 4)):
+        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32, **STAGE_DEFAULT}
+        for bad in ((16, 0), (256, 2), (256, -2), (0, -1, 2), (0, -1, -2), (0, -1, 1, 4), (0, -1, 1, 0, 4097),
+                    (0, -1, 1, 0, -2), (0, -1, 1, 0, 0, 4097)):
             with pytest.raises(pbf.PbfError):
                 sim.set_tuning(*bad)
-        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32}
+        assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32, **STAGE_DEFAULT}
         npos, nvel = torch.empty_like(pos), torch.empty_like(vel)
         sim.step(pos, npos, vel, nvel, iid, n)
         torch.cuda.synchronize()
         sim.set_tuning(0, -1)
-        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1, "bwd_lanes": 32}
+        assert sim.tuning() == {"dense_window": 512, "dense_all": -1, "order": 1, "bwd_lanes": 32, **STAGE_DEFAULT}
     r = oracle.step(p, sc.ulim, sc.llim, sc.pos.astype(np.float64), np.zeros((n, 4)), np.arange(n, dtype=np.uint32),
                     "f64")
     np.testing.assert_array_equal(iid.cpu().numpy().astype(np.uint32), r["iid"])
