@@ -288,6 +288,9 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
  * ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
+/* The same for a batch (bwd_lanes is ignored: a batch has no reverse pass). */
+pbf_status pbf_batch_set_tuning(pbf_batch* b, const pbf_tuning* t);
+pbf_status pbf_batch_get_tuning(const pbf_batch* b, pbf_tuning* t);
 
 /*
  * Errors the solver's kernels recorded on the device since the last call.

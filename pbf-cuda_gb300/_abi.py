@@ -54,6 +54,8 @@ EXPORTED = (
     "pbf_batch_autotune",
     "pbf_set_tuning",
     "pbf_get_tuning",
+    "pbf_batch_set_tuning",
+    "pbf_batch_get_tuning",
     "pbf_check_device",
     "pbf_batch_check_device",
     "pbf_step_noalloc",
@@ -227,6 +229,8 @@ def _declare(L) -> None:
         "pbf_batch_autotune": (ctypes.c_int, [vp, vp, vp, vp, ctypes.c_int, vp, vp]),
         "pbf_set_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
         "pbf_get_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
+        "pbf_batch_set_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
+        "pbf_batch_get_tuning": (ctypes.c_int, [vp, P(PbfTuning)]),
         "pbf_check_device": (ctypes.c_int, [vp, vp]),
         "pbf_batch_check_device": (ctypes.c_int, [vp, vp]),
         "pbf_step_noalloc": (ctypes.c_int, [P(PbfParams), f3, f3, vp, vp, vp, vp, vp, ctypes.c_int, vp]),

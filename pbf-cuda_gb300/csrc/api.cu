@@ -1431,6 +1431,9 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
   return PBF_OK;
 }
 
+// Validates a pbf_tuning for pbf_set_tuning / pbf_batch_set_tuning.
+pbf_status check_tuning(const pbf_tuning* t);
+
 }  // namespace
 
 extern "C" {
@@ -1476,6 +1479,45 @@ pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const u
 
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
   if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
+  if (pbf_status st = check_tuning(t); st != PBF_OK) return st;
+  s->tune_window = t->dense_window;
+  s->tune_all = t->dense_all;
+  s->tune_order = t->order;
+  s->tune_bwd_lanes = t->bwd_lanes;
+  s->tune_stage_sparse = t->stage_sparse;
+  s->tune_stage_dense = t->stage_dense;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_set_tuning(pbf_batch* b, const pbf_tuning* t) {
+  if (!b || !t) return fail(PBF_ERR_INVALID_ARG, "batch or tuning is NULL");
+  if (pbf_status st = check_tuning(t); st != PBF_OK) return st;
+  b->tune_window = t->dense_window;
+  b->tune_all = t->dense_all;
+  b->tune_order = t->order;
+  b->tune_stage_sparse = t->stage_sparse;
+  b->tune_stage_dense = t->stage_dense;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_get_tuning(const pbf_batch* b, pbf_tuning* t) {
+  if (!b || !t) return fail(PBF_ERR_INVALID_ARG, "batch or tuning is NULL");
+  t->dense_window = b->tune_window > 0 ? b->tune_window : pbf::kDefaultDenseWindow;
+  t->dense_all = b->tune_all;
+  t->order = b->tune_order >= 0 ? b->tune_order : 1;
+  t->bwd_lanes = 0;
+  t->stage_sparse = b->tune_stage_sparse >= 0 ? b->tune_stage_sparse : pbf::kDefaultStageSparse;
+  t->stage_dense = b->tune_stage_dense >= 0 ? b->tune_stage_dense : pbf::kDefaultStageDense;
+  t->ms_per_step = 0.f;
+  t->ms_default = 0.f;
+  return PBF_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+pbf_status check_tuning(const pbf_tuning* t) {
   if (t->dense_window != 0 && t->dense_window < 32)
     return fail(PBF_ERR_INVALID_ARG, "dense_window must be 0 (default) or >= 32 (got %d)", t->dense_window);
   if (t->dense_all < -1 || t->dense_all > 1)
@@ -1488,14 +1530,12 @@ pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
       t->stage_dense > pbf::kStageMax)
     return fail(PBF_ERR_INVALID_ARG, "stage_sparse / stage_dense must be -1 to %d (got %d / %d)", pbf::kStageMax,
                 t->stage_sparse, t->stage_dense);
-  s->tune_window = t->dense_window;
-  s->tune_all = t->dense_all;
-  s->tune_order = t->order;
-  s->tune_bwd_lanes = t->bwd_lanes;
-  s->tune_stage_sparse = t->stage_sparse;
-  s->tune_stage_dense = t->stage_dense;
   return PBF_OK;
 }
+
+}  // namespace
+
+extern "C" {
 
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
   if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");

@@ -1019,13 +1019,15 @@ constexpr int kDenseQueue = PBF_DENSE_QUEUE;
 #define PBF_SPARSE_BOUNDS __launch_bounds__(kSparseThreads)
 #endif
 
-template <int kKind>
+// kStage: the variant that stages its block's column runs (launched when
+// stage_sparse > 0); the other carries no staging code.
+template <int kKind, bool kStage>
 __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   using P = typename PassOf<kKind>::type;
   __shared__ uint32_t q_mask[kSparseQueue * kSparseThreads];
   __shared__ int q_base[kSparseQueue * kSparseThreads];
   __shared__ StageState st;
-  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_sparse slots when staging
+  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_sparse slots (kStage)
   if (a.dense_all) return;
   const int count = work_count(a);
   if ((int)(blockIdx.x * kSparseThreads) >= count) return;  // uniform over the block
@@ -1057,10 +1059,10 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   const bool active = valid && !go_dense;
   const bool exact = active && exact_path(kKind, a, g, q, i);
   // the block's plain windows staged in shared memory (block-uniform branch)
-  const int cap = a.c.stage_sparse;
+  const int cap = kStage ? a.c.stage_sparse : 0;
   bool staged = false;
   uint32_t phase = 0u;
-  if (cap > 0) {
+  if (kStage && cap > 0) {
     if (threadIdx.x == 0) stage_init(st);
     stage_vote(st, threadIdx.x >> 5, active && !grouped, g, q, i);
     __syncthreads();
@@ -1072,28 +1074,30 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
     P p(a, g, xi, i, exact);
     if (grouped)
       visit_window_grouped(g, a, q, FromGlobal{a.X}, p, 0, entries, hq);
-    else if (staged)
+    else if (kStage && staged)
       sparse_visit<kKind>(a, g, q, FromStage{stage, st.D}, p, exact, i, hq);
     else
       sparse_visit<kKind>(a, g, q, FromGlobal{a.X}, p, exact, i, hq);
     p.finish(a);
   }
-  if (cap > 0) stage_drain(st, phase);
+  if (kStage && cap > 0) stage_drain(st, phase);
 }
 
-template <int kKind>
+// kStage: the variant that stages each item's column runs (launched when
+// stage_dense > 0); the other carries no staging code.
+template <int kKind, bool kStage>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   using P = typename PassOf<kKind>::type;
   __shared__ float part[kDenseWarps][kMaxFields][32];
   __shared__ uint32_t q_mask[kDenseQueue * kDenseThreads];
   __shared__ int q_base[kDenseQueue * kDenseThreads];
   __shared__ StageState st;
-  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_dense slots when staging
+  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_dense slots (kStage)
   static_assert(P::kFields <= kMaxFields, "partial-sum fields");
   HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kDenseThreads, kDenseQueue);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int cap = a.c.stage_dense;
-  if (threadIdx.x == 0 && cap > 0) stage_init(st);
+  const int cap = kStage ? a.c.stage_dense : 0;
+  if (kStage && threadIdx.x == 0 && cap > 0) stage_init(st);
   if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
   // the slots the sparse kernel listed, or all of them, 32 per item
   const int work = work_count(a);
@@ -1114,7 +1118,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     // the item's windows staged in shared memory: every warp holds the same
     // 32 particles, so warp 0's vote is the block's (block-uniform branch)
     bool staged = false;
-    if (cap > 0) {
+    if (kStage && cap > 0) {
       if (warp == 0) stage_vote(st, 0, valid, g, q, i);
       __syncthreads();  // also: the previous item's reads of the stage are done
       if (threadIdx.x == 0) stage_issue(st, 1, a, stage, cap);
@@ -1128,7 +1132,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
       P p(a, g, xi, i, exact);
       // a staged window holds no grouped cell: the grouped walk visits its
       // candidates in the order visit_window_chunk does
-      if (staged)
+      if (kStage && staged)
         visit_window_grouped(g, a, q, FromStage{stage, st.D}, p, lo, hi, hq);
       else if (grouped)
         visit_window_grouped(g, a, q, FromGlobal{a.X}, p, lo, hi, hq);
@@ -1144,7 +1148,7 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     }
     __syncthreads();
   }
-  if (cap > 0) stage_drain(st, phase);
+  if (kStage && cap > 0) stage_drain(st, phase);
 }
 
 // Also registers every cell holding >= kGroupCell particles (its first
@@ -1827,17 +1831,26 @@ template <int kKind>
 cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
   const size_t sparse_smem = sizeof(float4) * (size_t)max(a.c.stage_sparse, 0);
   const size_t dense_smem = sizeof(float4) * (size_t)max(a.c.stage_dense, 0);
-  if (!a.dense_all)  // else the sparse kernel has nothing to do
-    k_sparse<kKind><<<(a.n + kSparseThreads - 1) / kSparseThreads, kSparseThreads, sparse_smem, stream>>>(a);
-  k_dense<kKind><<<a.c.dense_grid, kDenseThreads, dense_smem, stream>>>(a);
+  const int sparse_blocks = (a.n + kSparseThreads - 1) / kSparseThreads;
+  if (a.dense_all) {
+    // else the sparse kernel has nothing to do
+  } else if (sparse_smem) {
+    k_sparse<kKind, true><<<sparse_blocks, kSparseThreads, sparse_smem, stream>>>(a);
+  } else {
+    k_sparse<kKind, false><<<sparse_blocks, kSparseThreads, 0, stream>>>(a);
+  }
+  if (dense_smem)
+    k_dense<kKind, true><<<a.c.dense_grid, kDenseThreads, dense_smem, stream>>>(a);
+  else
+    k_dense<kKind, false><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
 template <int kKind>
 cudaError_t allow_stage(int bytes) {
-  cudaError_t e = cudaFuncSetAttribute(k_sparse<kKind>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaError_t e = cudaFuncSetAttribute(k_sparse<kKind, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_dense<kKind>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    e = cudaFuncSetAttribute(k_dense<kKind, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   return e;
 }
 

@@ -297,6 +297,25 @@ class Ensemble:
     def setLim(self, scene: int, ulim: Sequence[float], llim: Sequence[float]) -> None:
         check(self._L.pbf_batch_set_limits(self._h, int(scene), _vec3(ulim), _vec3(llim)), "pbf_batch_set_limits")
 
+    def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, stage_sparse: int = -1,
+                   stage_dense: int = -1) -> None:
+        """The neighbour passes' choices for the following steps (pbf_batch_set_tuning)."""
+        t = PbfTuning()
+        t.dense_window, t.dense_all, t.order = int(dense_window), int(dense_all), int(order)
+        t.stage_sparse, t.stage_dense = int(stage_sparse), int(stage_dense)
+        check(self._L.pbf_batch_set_tuning(self._h, ctypes.byref(t)), "pbf_batch_set_tuning")
+
+    def tuning(self) -> dict:
+        t = PbfTuning()
+        check(self._L.pbf_batch_get_tuning(self._h, ctypes.byref(t)), "pbf_batch_get_tuning")
+        return {"dense_window": t.dense_window, "dense_all": t.dense_all, "order": t.order,
+                "stage_sparse": t.stage_sparse, "stage_dense": t.stage_dense}
+
+    def check_device(self, stream=None) -> None:
+        """Raise PbfError (PBF_ERR_TIMEOUT) if a bounded device-side wait of the
+        steps since the last check gave up (pbf_batch_check_device)."""
+        check(self._L.pbf_batch_check_device(self._h, _stream_handle(stream)), "pbf_batch_check_device")
+
     def density(self, stream=None) -> torch.Tensor:
         out = torch.empty(max(self.n, 1), dtype=torch.float32, device="cuda")
         check(self._L.pbf_batch_get_density(self._h, out.data_ptr(), _stream_handle(stream)),
