@@ -413,8 +413,9 @@ def tune(sim, st, n, args):
     if not args.tune:
         return None
     t = sim.autotune(st.pos, st.vel, st.iid, n, steps=3)
-    return {"dense_window": int(t["dense_window"]), "dense_all": int(t["dense_all"]), "order": int(t["order"]),
-            "trial_ms_per_step": round(float(t["ms_per_step"]), 4),
+    keys = ("dense_window", "dense_all", "order", "dense_split", "queue_sparse", "queue_dense", "stage_sparse",
+            "stage_dense")
+    return {**{k: int(t[k]) for k in keys}, "trial_ms_per_step": round(float(t["ms_per_step"]), 4),
             "trial_ms_per_step_default": round(float(t["ms_default"]), 4)}
 
 
@@ -678,8 +679,7 @@ def adjoint_times(pkg, torch, args, evals: int, frames: int) -> dict:
         if not lane_choice:
             lane_choice.update(ip.autotune_backward(v0, 0.0))
         else:
-            t0 = ip.sim.tuning()
-            ip.sim.set_tuning(t0["dense_window"], t0["dense_all"], t0["order"], lane_choice["bwd_lanes"])
+            ip.sim.set_tuning(**{**ip.sim.tuning(), "bwd_lanes": lane_choice["bwd_lanes"]})
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(evals):

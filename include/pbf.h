@@ -248,16 +248,19 @@ pbf_status pbf_batch_use_graphs(pbf_batch* b, int on);
  * particle's window goes to the dense kernel (a block of 8 warps splitting
  * the windows of 32 particles), whether every particle does, the order in
  * which the passes take particles (the cell order of the grid, or the cell
- * each particle is in at that iteration), and how many candidate positions a
- * block of each pass kernel may stage in shared memory (bulk asynchronous
- * copies of the column runs its particles' windows share, read there instead
- * of through L1) -- by running `steps` steps per choice from copies of the
+ * each particle is in at that iteration), how many warps of the dense kernel
+ * split a batch's windows, how many neighbour chunks a thread queues before
+ * running their pair terms, and how many candidate positions a block of each
+ * pass kernel may stage in shared memory (bulk asynchronous copies of the
+ * column runs its particles' windows share, read there instead of through
+ * L1) -- by running `steps` steps per choice from copies of the
  * caller's state (pos, vel, iid: device, n entries; they are not modified),
  * and keeps the fastest for the solver's following steps.  The window and
  * dense choices change the order in which window sums are added, so results
- * differ by rounding only; the particle order and the staging change nothing
- * (each particle's sums are the same whichever warp computes them, from
- * whichever copy of the positions).  The trial steps are not taped.  The cell
+ * differ by rounding only, and so does the dense split; the particle order,
+ * the queues and the staging change nothing (each particle's sums are the
+ * same whichever warp computes them, in whichever loop, from whichever copy
+ * of the positions).  The trial steps are not taped.  The cell
  * size stays h: with the reference's stale grid, another cell size would
  * change which neighbours a step sees.
  */
@@ -273,6 +276,13 @@ typedef struct pbf_tuning {
                          copies into shared memory when its particles share one column of
                          cells (0: none; at most 4096) */
   int stage_dense;    /* the same for a block of the dense kernel */
+  int queue_sparse;   /* neighbour chunks of 32 candidates whose hits a thread of the
+                         one-thread-per-particle kernel queues before running their pair terms
+                         in one loop (1: each chunk's right away; at most 16) */
+  int queue_dense;    /* the same for the dense kernel (at most 8) */
+  int dense_split;    /* warps of the dense kernel that split one batch of 32 particles'
+                         windows: 1, 2, 4 or 8 (a block of 8 warps takes 8 / dense_split
+                         batches at a time) */
 } pbf_tuning;
 
 pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
@@ -284,8 +294,9 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
  * default; dense_all 1 (every particle dense), 0 (by window) or -1 (the
  * default: every particle dense below 131072 particles); order 1, 0 or -1
  * (the default, 1); bwd_lanes 0 (the default), 8, 16 or 32; stage_sparse and
- * stage_dense 0 (off) to 4096 slots, or -1 (the default).  ms fields are
- * ignored on set and 0 on get. */
+ * stage_dense 0 (off) to 4096 slots, or -1 (the default); queue_sparse 1-16,
+ * queue_dense 1-8 and dense_split 1, 2, 4 or 8, or 0 (the defaults: 16, 8,
+ * 8).  ms fields are ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
 /* The same for a batch (bwd_lanes is ignored: a batch has no reverse pass). */

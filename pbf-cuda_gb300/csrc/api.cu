@@ -123,6 +123,9 @@ struct pbf_solver {
   int tune_bwd_lanes;  // 0: the default (32)
   int tune_stage_sparse;  // staged slots per sparse / dense block; -1: the defaults
   int tune_stage_dense;
+  int tune_queue_sparse;  // hit-queue chunks per sparse / dense thread; 0: the defaults
+  int tune_queue_dense;
+  int tune_split;         // dense warps per item; 0: the default
 };
 
 namespace {
@@ -284,6 +287,9 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   c.order = 1;
   c.stage_sparse = pbf::kDefaultStageSparse;
   c.stage_dense = pbf::kDefaultStageDense;
+  c.queue_sparse = pbf::kDefaultQueueSparse;
+  c.queue_dense = pbf::kDefaultQueueDense;
+  c.dense_split = pbf::kDefaultDenseSplit;
   return c;
 }
 
@@ -779,6 +785,9 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   if (s->tune_order >= 0) P.c.order = s->tune_order;
   if (s->tune_stage_sparse >= 0) P.c.stage_sparse = s->tune_stage_sparse;
   if (s->tune_stage_dense >= 0) P.c.stage_dense = s->tune_stage_dense;
+  if (s->tune_queue_sparse > 0) P.c.queue_sparse = s->tune_queue_sparse;
+  if (s->tune_queue_dense > 0) P.c.queue_dense = s->tune_queue_dense;
+  if (s->tune_split > 0) P.c.dense_split = s->tune_split;
   P.G = pbf::Geometry{nullptr, nullptr};
   P.grid = &s->grid;
   P.sol = &s->sol;
@@ -1063,6 +1072,9 @@ struct pbf_batch {
   int tune_order = -1;
   int tune_stage_sparse = -1;
   int tune_stage_dense = -1;
+  int tune_queue_sparse = 0;
+  int tune_queue_dense = 0;
+  int tune_split = 0;
 };
 
 namespace {
@@ -1250,6 +1262,9 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   if (b->tune_order >= 0) P.c.order = b->tune_order;
   if (b->tune_stage_sparse >= 0) P.c.stage_sparse = b->tune_stage_sparse;
   if (b->tune_stage_dense >= 0) P.c.stage_dense = b->tune_stage_dense;
+  if (b->tune_queue_sparse > 0) P.c.queue_sparse = b->tune_queue_sparse;
+  if (b->tune_queue_dense > 0) P.c.queue_dense = b->tune_queue_dense;
+  if (b->tune_split > 0) P.c.dense_split = b->tune_split;
   P.G = pbf::Geometry{b->d_geom, b->d_sid};
   P.grid = &b->grid;
   P.sol = &b->sol;
@@ -1335,21 +1350,77 @@ pbf_status pbf_density_grid_backward(const void* pos, int n, const float lo[3], 
 
 namespace {
 
-// Candidate dense-kernel choices, timed by pbf_autotune / pbf_batch_autotune.
+// Candidate choices timed by pbf_autotune / pbf_batch_autotune.
 constexpr int kTuneWindows[] = {64, 128, 256, 512, 1024, 2048};
-// Candidate stage sizes (slots per block) of the sparse and dense kernels.
+constexpr int kTuneSplits[] = {1, 2, 4, 8};
+constexpr int kTuneQueueSparse[] = {1, 16};
+constexpr int kTuneQueueDense[] = {1, 8};
 constexpr int kTuneStageSparse[] = {0, 1024, 2048};
 constexpr int kTuneStageDense[] = {0, 1536, 3072};
 
-// One configuration of the neighbour passes.
+// One configuration of the neighbour passes (the fields of pbf_tuning that
+// pbf_autotune times).
 struct TuneChoice {
-  int window, all, order, stage_sparse, stage_dense;
+  int window, all, order, split, queue_sparse, queue_dense, stage_sparse, stage_dense;
+  bool operator==(const TuneChoice& o) const {
+    return window == o.window && all == o.all && order == o.order && split == o.split &&
+           queue_sparse == o.queue_sparse && queue_dense == o.queue_dense && stage_sparse == o.stage_sparse &&
+           stage_dense == o.stage_dense;
+  }
 };
+
+TuneChoice default_choice(int n) {
+  return TuneChoice{pbf::kDefaultDenseWindow, n < pbf::kDenseAllBelow ? 1 : 0, 1, pbf::kDefaultDenseSplit,
+                    pbf::kDefaultQueueSparse, pbf::kDefaultQueueDense, pbf::kDefaultStageSparse,
+                    pbf::kDefaultStageDense};
+}
+
+// The tuning fields a solver or batch keeps (0 / -1: the defaults).
+struct TuneState {
+  int window = 0, all = -1, order = -1, split = 0, queue_sparse = 0, queue_dense = 0, stage_sparse = -1,
+      stage_dense = -1;
+};
+
+template <class T>
+TuneState tune_state(const T* h) {
+  return TuneState{h->tune_window,  h->tune_all,          h->tune_order,        h->tune_split,
+                   h->tune_queue_sparse, h->tune_queue_dense, h->tune_stage_sparse, h->tune_stage_dense};
+}
+
+template <class T>
+void set_tune_state(T* h, const TuneState& t) {
+  h->tune_window = t.window;
+  h->tune_all = t.all;
+  h->tune_order = t.order;
+  h->tune_split = t.split;
+  h->tune_queue_sparse = t.queue_sparse;
+  h->tune_queue_dense = t.queue_dense;
+  h->tune_stage_sparse = t.stage_sparse;
+  h->tune_stage_dense = t.stage_dense;
+}
+
+TuneState state_of(const TuneChoice& c) {
+  return TuneState{c.window, c.all, c.order, c.split, c.queue_sparse, c.queue_dense, c.stage_sparse,
+                   c.stage_dense};
+}
+
+// pbf_tuning fields of a tune state (defaults resolved).
+void fill_tuning(const TuneState& t, pbf_tuning* out) {
+  out->dense_window = t.window > 0 ? t.window : pbf::kDefaultDenseWindow;
+  out->dense_all = t.all;
+  out->order = t.order >= 0 ? t.order : 1;
+  out->dense_split = t.split > 0 ? t.split : pbf::kDefaultDenseSplit;
+  out->queue_sparse = t.queue_sparse > 0 ? t.queue_sparse : pbf::kDefaultQueueSparse;
+  out->queue_dense = t.queue_dense > 0 ? t.queue_dense : pbf::kDefaultQueueDense;
+  out->stage_sparse = t.stage_sparse >= 0 ? t.stage_sparse : pbf::kDefaultStageSparse;
+  out->stage_dense = t.stage_dense >= 0 ? t.stage_dense : pbf::kDefaultStageDense;
+}
 
 // Runs `steps` steps per candidate on copies of (pos, vel, iid) through
 // step(choice, bufs...) and returns the fastest choice: first over the
-// window, dense and order choices with the default stages, then, from the
-// best of those, over the sparse kernel's stage, then the dense kernel's.
+// window, dense and order choices with the other fields at their defaults,
+// then, from the best so far, one field at a time: the dense split, the
+// sparse and dense hit queues, the sparse and dense stages.
 template <class Step>
 pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid, int steps, cudaStream_t st,
                     Step step, pbf_tuning* out) {
@@ -1387,16 +1458,14 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
     if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
     return e == cudaSuccess ? ms / (float)steps : -1.f;
   };
-  const TuneChoice def{pbf::kDefaultDenseWindow, n < pbf::kDenseAllBelow ? 1 : 0, 1, pbf::kDefaultStageSparse,
-                       pbf::kDefaultStageDense};
+  const TuneChoice def = default_choice(n);
   float best = -1.f, def_ms = -1.f;
-  TuneChoice best_ch{pbf::kDefaultDenseWindow, -1, 1, pbf::kDefaultStageSparse, pbf::kDefaultStageDense};
+  TuneChoice best_ch = def;
+  best_ch.all = -1;
   auto consider = [&](const TuneChoice& ch) {
     const float ms = time_choice(ch);
     if (ms < 0.f) return;
-    if (ch.window == def.window && ch.all == def.all && ch.order == def.order &&
-        ch.stage_sparse == def.stage_sparse && ch.stage_dense == def.stage_dense)
-      def_ms = ms;
+    if (ch == def) def_ms = ms;
     if (best < 0.f || ms < best) {
       best = ms;
       best_ch = ch;
@@ -1406,116 +1475,39 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
     for (int all = 0; all <= 1; ++all)
       for (int w : kTuneWindows) {
         if (all == 1 && w != pbf::kDefaultDenseWindow) continue;  // the window plays no part then
-        consider(TuneChoice{w, all, ord, pbf::kDefaultStageSparse, pbf::kDefaultStageDense});
+        TuneChoice ch = def;
+        ch.window = w, ch.all = all, ch.order = ord;
+        consider(ch);
       }
-  const TuneChoice base = best_ch;
-  for (int ss : kTuneStageSparse)
-    if (ss != base.stage_sparse && !base.all) consider(TuneChoice{base.window, base.all, base.order, ss, base.stage_dense});
-  const TuneChoice base2 = best_ch;
-  for (int sd : kTuneStageDense)
-    if (sd != base2.stage_dense) consider(TuneChoice{base2.window, base2.all, base2.order, base2.stage_sparse, sd});
+  // one field at a time from the best so far (a field already at a
+  // candidate's value is not timed again)
+  auto sweep = [&](int TuneChoice::*field, const int* vals, int count) {
+    const TuneChoice base = best_ch;
+    for (int k = 0; k < count; ++k) {
+      if (vals[k] == base.*field) continue;
+      TuneChoice ch = base;
+      ch.*field = vals[k];
+      consider(ch);
+    }
+  };
+  sweep(&TuneChoice::split, kTuneSplits, 4);
+  if (!best_ch.all) sweep(&TuneChoice::queue_sparse, kTuneQueueSparse, 2);
+  sweep(&TuneChoice::queue_dense, kTuneQueueDense, 2);
+  if (!best_ch.all) sweep(&TuneChoice::stage_sparse, kTuneStageSparse, 3);
+  sweep(&TuneChoice::stage_dense, kTuneStageDense, 3);
   for (void* q : {(void*)p[0], (void*)p[1], (void*)v[0], (void*)v[1], (void*)id})
     if (q) cudaFree(q);
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   if (result != PBF_OK) return result;
   if (e != cudaSuccess) return cuda_fail(e, "pbf_autotune");
-  out->dense_window = best_ch.window;
+  fill_tuning(state_of(best_ch), out);
   out->dense_all = best_ch.all;
-  out->order = best_ch.order;
   out->bwd_lanes = 0;
-  out->stage_sparse = best_ch.stage_sparse;
-  out->stage_dense = best_ch.stage_dense;
   out->ms_per_step = best;
   out->ms_default = def_ms;
   return PBF_OK;
 }
-
-// Validates a pbf_tuning for pbf_set_tuning / pbf_batch_set_tuning.
-pbf_status check_tuning(const pbf_tuning* t);
-
-}  // namespace
-
-extern "C" {
-
-pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
-                        pbf_tuning* out, void* stream) {
-  const pbf::NvtxRange range("pbf_autotune");
-  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
-  if (n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
-  const int depth = s->tape_depth, top = s->tape_top;
-  s->tape_depth = 0;  // the trial steps are not taped
-  const int w0 = s->tune_window, a0 = s->tune_all, o0 = s->tune_order;
-  const int ss0 = s->tune_stage_sparse, sd0 = s->tune_stage_dense;
-  const pbf_status st = autotune(
-      n, pos, vel, iid, steps, (cudaStream_t)stream,
-      [&](const TuneChoice& ch, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
-        s->tune_window = ch.window;
-        s->tune_all = ch.all;
-        s->tune_order = ch.order;
-        s->tune_stage_sparse = ch.stage_sparse;
-        s->tune_stage_dense = ch.stage_dense;
-        return pbf_step(s, p, np, v, nv, id, n, strm);
-      },
-      out);
-  s->tape_depth = depth;
-  s->tape_top = top;
-  if (st != PBF_OK) {
-    s->tune_window = w0;
-    s->tune_all = a0;
-    s->tune_order = o0;
-    s->tune_stage_sparse = ss0;
-    s->tune_stage_dense = sd0;
-    return st;
-  }
-  s->tune_window = out->dense_window;
-  s->tune_all = out->dense_all;
-  s->tune_order = out->order;
-  s->tune_stage_sparse = out->stage_sparse;
-  s->tune_stage_dense = out->stage_dense;
-  out->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;  // not timed: kept
-  return PBF_OK;
-}
-
-pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
-  if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
-  if (pbf_status st = check_tuning(t); st != PBF_OK) return st;
-  s->tune_window = t->dense_window;
-  s->tune_all = t->dense_all;
-  s->tune_order = t->order;
-  s->tune_bwd_lanes = t->bwd_lanes;
-  s->tune_stage_sparse = t->stage_sparse;
-  s->tune_stage_dense = t->stage_dense;
-  return PBF_OK;
-}
-
-pbf_status pbf_batch_set_tuning(pbf_batch* b, const pbf_tuning* t) {
-  if (!b || !t) return fail(PBF_ERR_INVALID_ARG, "batch or tuning is NULL");
-  if (pbf_status st = check_tuning(t); st != PBF_OK) return st;
-  b->tune_window = t->dense_window;
-  b->tune_all = t->dense_all;
-  b->tune_order = t->order;
-  b->tune_stage_sparse = t->stage_sparse;
-  b->tune_stage_dense = t->stage_dense;
-  return PBF_OK;
-}
-
-pbf_status pbf_batch_get_tuning(const pbf_batch* b, pbf_tuning* t) {
-  if (!b || !t) return fail(PBF_ERR_INVALID_ARG, "batch or tuning is NULL");
-  t->dense_window = b->tune_window > 0 ? b->tune_window : pbf::kDefaultDenseWindow;
-  t->dense_all = b->tune_all;
-  t->order = b->tune_order >= 0 ? b->tune_order : 1;
-  t->bwd_lanes = 0;
-  t->stage_sparse = b->tune_stage_sparse >= 0 ? b->tune_stage_sparse : pbf::kDefaultStageSparse;
-  t->stage_dense = b->tune_stage_dense >= 0 ? b->tune_stage_dense : pbf::kDefaultStageDense;
-  t->ms_per_step = 0.f;
-  t->ms_default = 0.f;
-  return PBF_OK;
-}
-
-}  // extern "C"
-
-namespace {
 
 pbf_status check_tuning(const pbf_tuning* t) {
   if (t->dense_window != 0 && t->dense_window < 32)
@@ -1530,21 +1522,79 @@ pbf_status check_tuning(const pbf_tuning* t) {
       t->stage_dense > pbf::kStageMax)
     return fail(PBF_ERR_INVALID_ARG, "stage_sparse / stage_dense must be -1 to %d (got %d / %d)", pbf::kStageMax,
                 t->stage_sparse, t->stage_dense);
+  if (t->queue_sparse < 0 || t->queue_sparse > pbf::kMaxQueueSparse || t->queue_dense < 0 ||
+      t->queue_dense > pbf::kMaxQueueDense)
+    return fail(PBF_ERR_INVALID_ARG, "queue_sparse must be 0 to %d and queue_dense 0 to %d (got %d / %d)",
+                pbf::kMaxQueueSparse, pbf::kMaxQueueDense, t->queue_sparse, t->queue_dense);
+  if (t->dense_split != 0 && t->dense_split != 1 && t->dense_split != 2 && t->dense_split != 4 &&
+      t->dense_split != 8)
+    return fail(PBF_ERR_INVALID_ARG, "dense_split must be 0, 1, 2, 4 or 8 (got %d)", t->dense_split);
   return PBF_OK;
+}
+
+TuneState state_of(const pbf_tuning* t) {
+  return TuneState{t->dense_window, t->dense_all,   t->order,        t->dense_split,
+                   t->queue_sparse, t->queue_dense, t->stage_sparse, t->stage_dense};
 }
 
 }  // namespace
 
 extern "C" {
 
+pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
+                        pbf_tuning* out, void* stream) {
+  const pbf::NvtxRange range("pbf_autotune");
+  if (!s) return fail(PBF_ERR_INVALID_ARG, "solver is NULL");
+  if (n > s->max_particles) return fail(PBF_ERR_CAPACITY, "n = %d exceeds max_particles = %d", n, s->max_particles);
+  const int depth = s->tape_depth, top = s->tape_top;
+  s->tape_depth = 0;  // the trial steps are not taped
+  const TuneState keep = tune_state(s);
+  const pbf_status st = autotune(
+      n, pos, vel, iid, steps, (cudaStream_t)stream,
+      [&](const TuneChoice& ch, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
+        set_tune_state(s, state_of(ch));
+        return pbf_step(s, p, np, v, nv, id, n, strm);
+      },
+      out);
+  s->tape_depth = depth;
+  s->tape_top = top;
+  if (st != PBF_OK) {
+    set_tune_state(s, keep);
+    return st;
+  }
+  set_tune_state(s, state_of(out));
+  out->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;  // not timed: kept
+  return PBF_OK;
+}
+
+pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t) {
+  if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
+  if (pbf_status st = check_tuning(t); st != PBF_OK) return st;
+  set_tune_state(s, state_of(t));
+  s->tune_bwd_lanes = t->bwd_lanes;
+  return PBF_OK;
+}
+
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t) {
   if (!s || !t) return fail(PBF_ERR_INVALID_ARG, "solver or tuning is NULL");
-  t->dense_window = s->tune_window > 0 ? s->tune_window : pbf::kDefaultDenseWindow;
-  t->dense_all = s->tune_all;
-  t->order = s->tune_order >= 0 ? s->tune_order : 1;
+  fill_tuning(tune_state(s), t);
   t->bwd_lanes = s->tune_bwd_lanes > 0 ? s->tune_bwd_lanes : 32;
-  t->stage_sparse = s->tune_stage_sparse >= 0 ? s->tune_stage_sparse : pbf::kDefaultStageSparse;
-  t->stage_dense = s->tune_stage_dense >= 0 ? s->tune_stage_dense : pbf::kDefaultStageDense;
+  t->ms_per_step = 0.f;
+  t->ms_default = 0.f;
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_set_tuning(pbf_batch* b, const pbf_tuning* t) {
+  if (!b || !t) return fail(PBF_ERR_INVALID_ARG, "batch or tuning is NULL");
+  if (pbf_status st = check_tuning(t); st != PBF_OK) return st;
+  set_tune_state(b, state_of(t));
+  return PBF_OK;
+}
+
+pbf_status pbf_batch_get_tuning(const pbf_batch* b, pbf_tuning* t) {
+  if (!b || !t) return fail(PBF_ERR_INVALID_ARG, "batch or tuning is NULL");
+  fill_tuning(tune_state(b), t);
+  t->bwd_lanes = 0;
   t->ms_per_step = 0.f;
   t->ms_default = 0.f;
   return PBF_OK;
@@ -1564,32 +1614,19 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
                               pbf_tuning* out, void* stream) {
   const pbf::NvtxRange range("pbf_batch_autotune");
   if (!b) return fail(PBF_ERR_INVALID_ARG, "batch is NULL");
-  const int w0 = b->tune_window, a0 = b->tune_all, o0 = b->tune_order;
-  const int ss0 = b->tune_stage_sparse, sd0 = b->tune_stage_dense;
+  const TuneState keep = tune_state(b);
   const pbf_status st = autotune(
       b->n, pos, vel, iid, steps, (cudaStream_t)stream,
       [&](const TuneChoice& ch, float4* p, float4* np, float4* v, float4* nv, uint32_t* id, cudaStream_t strm) {
-        b->tune_window = ch.window;
-        b->tune_all = ch.all;
-        b->tune_order = ch.order;
-        b->tune_stage_sparse = ch.stage_sparse;
-        b->tune_stage_dense = ch.stage_dense;
+        set_tune_state(b, state_of(ch));
         return pbf_batch_step(b, p, np, v, nv, id, strm);
       },
       out);
   if (st != PBF_OK) {
-    b->tune_window = w0;
-    b->tune_all = a0;
-    b->tune_order = o0;
-    b->tune_stage_sparse = ss0;
-    b->tune_stage_dense = sd0;
+    set_tune_state(b, keep);
     return st;
   }
-  b->tune_window = out->dense_window;
-  b->tune_all = out->dense_all;
-  b->tune_order = out->order;
-  b->tune_stage_sparse = out->stage_sparse;
-  b->tune_stage_dense = out->stage_dense;
+  set_tune_state(b, state_of(out));
   return PBF_OK;
 }
 

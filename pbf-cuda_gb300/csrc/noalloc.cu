@@ -74,7 +74,7 @@ constexpr size_t kOffIid = kOffXb + align_up(16 * kNp);
 constexpr size_t kOffLambda = kOffIid + align_up(4 * kNp);
 constexpr size_t kOffRho = kOffLambda + align_up(4 * kNp);
 constexpr size_t kOffFlags = kOffRho + align_up(4 * kNp);
-constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kNumFlags);
+constexpr size_t kOffDense = kOffFlags + align_up(4 * (size_t)pbf::kFlagWords);
 constexpr size_t kOffMasks = kOffDense + align_up(4 * pbf::dense_list_len(kNoAllocMaxParticles));
 constexpr size_t kOffCellFlags = kOffMasks + align_up(4 * (size_t)pbf::kMaskWords * kNp);
 constexpr size_t kSlots = (size_t)kNoAllocMaxParticles / pbf::kGroupCell + 1;

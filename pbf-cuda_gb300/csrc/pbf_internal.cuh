@@ -60,6 +60,9 @@ struct StepConsts {
   int order;               // 1: the passes take particles in current-cell order (bucketed); 0: grid order
   int stage_sparse;        // slots a sparse-kernel block may stage in shared memory (0: none)
   int stage_dense;         // slots a dense-kernel block may stage in shared memory (0: none)
+  int queue_sparse;        // hit-queue chunks per thread of the sparse / dense kernel (1: none)
+  int queue_dense;
+  int dense_split;         // warps of the dense kernel sharing one item's windows: 1, 2, 4 or 8
   SceneGeom geom;          // the box of a single-scene step
 };
 
@@ -71,6 +74,50 @@ struct Geometry {
   const SceneGeom* scenes;  // nullptr: single scene
   const uint16_t* sid;      // [n] scene of each particle slot
 };
+
+// ---- programmatic dependent launch --------------------------------------------------
+//
+// The kernels of a step are launched with programmatic stream serialization
+// (launch_step_kernel): a kernel may be scheduled while the kernel before it
+// on the stream still runs, which hides its launch latency.  Each of them
+// calls pdl_enter() before it touches global memory: griddepcontrol.wait
+// returns once the previous kernel has completed and its writes are visible,
+// then griddepcontrol.launch_dependents lets the next kernel be scheduled.
+// Memory effects therefore keep plain stream order.  Without the launch
+// attribute both instructions do nothing.  PBF_PDL=0 (a build-time macro)
+// launches without the attribute.
+#ifndef PBF_PDL
+#define PBF_PDL 1
+#endif
+
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_step_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                                      cudaStream_t stream, Args... args) {
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cfg.attrs = attr;
+  cfg.numAttrs = PBF_PDL ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+
+// launch_step_kernel from a function returning cudaError_t, returning its error.
+#define PBF_LAUNCH(kernel, grid, block, smem, stream, ...)                                           \
+  do {                                                                                             \
+    const cudaError_t pbf_launch_e_ =                                                             \
+        ::pbf::launch_step_kernel(kernel, dim3(grid), dim3(block), smem, stream, __VA_ARGS__);    \
+    if (pbf_launch_e_ != cudaSuccess) return pbf_launch_e_;                                        \
+  } while (0)
 
 __device__ __forceinline__ SceneGeom geom_of(const StepConsts& c, const Geometry& G, int i) {
   return G.scenes ? G.scenes[G.sid[i]] : c.geom;
@@ -338,6 +385,14 @@ constexpr int kDenseAllBelow = 131072;
 // gets without the kernel attribute.
 constexpr int kDefaultStageSparse = 0;
 constexpr int kDefaultStageDense = 0;
+// Hit-queue capacities (chunks per thread; 1: the pair body right after each
+// chunk) and the dense kernel's warps per item (defaults; pbf_autotune can
+// override, queues up to kMaxQueue* chunks).
+constexpr int kMaxQueueSparse = 16;
+constexpr int kMaxQueueDense = 8;
+constexpr int kDefaultQueueSparse = 16;
+constexpr int kDefaultQueueDense = 8;
+constexpr int kDefaultDenseSplit = 8;
 
 // Vorticity confinement after XSPH, on its output NV (positions X = npos):
 // omega_i = sum_j (u_j - u_i) x g_ij and eta_i = sum_j |omega_j| g_ij over

@@ -395,13 +395,12 @@ __device__ __forceinline__ void visit_window_saved(const SceneGeom& g,
   hq.flush(src, p);
 }
 
-// Candidates [v_lo, v_hi) of the window (numbered in visiting order), four
-// loads in flight at a time.
-template <class P>
-__device__ __forceinline__ void visit_window_chunk(const SceneGeom& g,
-                                                   const uint32_t* __restrict__ cs, int n, int3 q,
-                                                   const float4* __restrict__ X, P& p, int v_lo,
-                                                   int v_hi) {
+// Candidates [v_lo, v_hi) of the window (numbered in visiting order), run by
+// run through visit_run (hit masks and the hit queue, or every candidate on
+// the exact path).  The caller flushes hq.
+template <class P, class Src>
+__device__ __forceinline__ void visit_window_chunk(const SceneGeom& g, const uint32_t* __restrict__ cs, int n,
+                                                   int3 q, const Src& src, P& p, int v_lo, int v_hi, HitQueue& hq) {
   int v0 = 0;
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
@@ -409,25 +408,16 @@ __device__ __forceinline__ void visit_window_chunk(const SceneGeom& g,
     for (int dy = -1; dy <= 1; ++dy) {
       const int y = q.y + dy;
       if (y < 0 || y >= g.dims[1]) continue;
+      const int r = 3 * (dx + 1) + (dy + 1);
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
       const int len = e - s;
       const int a = max(v_lo, v0), b = min(v_hi, v0 + len);
+      if (a < b) visit_run(src, s + (a - v0), s + (b - v0), r, p, p.skip_misses(), hq);
       v0 += len;
-      if (a >= b) continue;
-      int j = s + (a - (v0 - len));
-      const int jend = s + (b - (v0 - len));
-      for (; j + 3 < jend; j += 4) {
-        const float4 q0 = __ldg(X + j), q1 = __ldg(X + j + 1), q2 = __ldg(X + j + 2),
-                     q3 = __ldg(X + j + 3);
-        p.visit(q0, j);
-        p.visit(q1, j + 1);
-        p.visit(q2, j + 2);
-        p.visit(q3, j + 3);
-      }
-      for (; j < jend; ++j) p.visit(__ldg(X + j), j);
     }
   }
+  hq.flush(src, p);
 }
 
 // Groups of cell `cell` in the pass's table, or -1 when the cell is visited
@@ -998,17 +988,6 @@ __device__ __forceinline__ void stage_init(StageState& st) {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// Hit-queue capacities (chunks per thread) of the two pass kernels.
-// PBF_SPARSE_QUEUE / PBF_DENSE_QUEUE: build-time tuning macros.
-#ifndef PBF_SPARSE_QUEUE
-#define PBF_SPARSE_QUEUE 16
-#endif
-#ifndef PBF_DENSE_QUEUE
-#define PBF_DENSE_QUEUE 8
-#endif
-constexpr int kSparseQueue = PBF_SPARSE_QUEUE;
-constexpr int kDenseQueue = PBF_DENSE_QUEUE;
-
 // One thread slot of the work list (or of all particles) per thread; the
 // grid covers every particle, blocks past the list's end return at once.
 // PBF_SPARSE_MIN_BLOCKS (a build-time tuning macro): resident blocks per SM the
@@ -1023,15 +1002,19 @@ constexpr int kDenseQueue = PBF_DENSE_QUEUE;
 // stage_sparse > 0); the other carries no staging code.
 template <int kKind, bool kStage>
 __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
+  pdl_enter();
   using P = typename PassOf<kKind>::type;
-  __shared__ uint32_t q_mask[kSparseQueue * kSparseThreads];
-  __shared__ int q_base[kSparseQueue * kSparseThreads];
+  __shared__ uint32_t q_mask[kMaxQueueSparse * kSparseThreads];
+  __shared__ int q_base[kMaxQueueSparse * kSparseThreads];
   __shared__ StageState st;
   extern __shared__ __align__(16) float4 stage[];  // a.c.stage_sparse slots (kStage)
   if (a.dense_all) return;
   const int count = work_count(a);
   if ((int)(blockIdx.x * kSparseThreads) >= count) return;  // uniform over the block
-  HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kSparseThreads, kSparseQueue);
+  // the queue is flushed once, at the window's end: a window of more chunks
+  // than it holds runs each chunk's hits right away (a flush in mid-window
+  // would run for some lanes while the others wait)
+  HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kSparseThreads, 1);
   const int t = blockIdx.x * kSparseThreads + threadIdx.x;
   const bool valid = t < count;
   const int i = valid ? work_particle(a, t) : 0;
@@ -1072,6 +1055,8 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   }
   if (active) {
     P p(a, g, xi, i, exact);
+    if (!grouped && !exact && a.c.queue_sparse > 1 && window_chunks(g, a.cs, a.n, q) <= a.c.queue_sparse)
+      hq.cap = a.c.queue_sparse;
     if (grouped)
       visit_window_grouped(g, a, q, FromGlobal{a.X}, p, 0, entries, hq);
     else if (kStage && staged)
@@ -1087,14 +1072,15 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
 // stage_dense > 0); the other carries no staging code.
 template <int kKind, bool kStage>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
+  pdl_enter();
   using P = typename PassOf<kKind>::type;
   __shared__ float part[kDenseWarps][kMaxFields][32];
-  __shared__ uint32_t q_mask[kDenseQueue * kDenseThreads];
-  __shared__ int q_base[kDenseQueue * kDenseThreads];
+  __shared__ uint32_t q_mask[kMaxQueueDense * kDenseThreads];
+  __shared__ int q_base[kMaxQueueDense * kDenseThreads];
   __shared__ StageState st;
   extern __shared__ __align__(16) float4 stage[];  // a.c.stage_dense slots (kStage)
   static_assert(P::kFields <= kMaxFields, "partial-sum fields");
-  HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kDenseThreads, kDenseQueue);
+  HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kDenseThreads, a.c.queue_dense);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cap = kStage ? a.c.stage_dense : 0;
   if (kStage && threadIdx.x == 0 && cap > 0) stage_init(st);
@@ -1103,18 +1089,28 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   const int work = work_count(a);
   const uint32_t listed = a.dense_all ? (uint32_t)work : a.flags[a.counter];
   const uint32_t count = (listed + 31) / 32;
+  // kSplit warps share an item (each walks one contiguous part of every
+  // lane's window); the block runs kDenseWarps / kSplit items at a time.  The
+  // staged variant gives each item the whole block.
+  const int split = kStage ? kDenseWarps : a.c.dense_split;
+  const int slots = kDenseWarps / split;
+  const int slot = warp / split, sub = warp % split;
+  // no grouped cell this step: windows are walked as 9 column runs (the same
+  // candidates in the same order as cell by cell, with fewer table reads)
+  const bool groups = a.c.keps2 > 0.f && a.flags[kGroupCount] != 0u;
+  const uint32_t per_round = gridDim.x * (uint32_t)slots;
+  const uint32_t rounds = (count + per_round - 1) / per_round;
   uint32_t phase = 0u;
-  for (uint32_t item = blockIdx.x; item < count; item += gridDim.x) {
+  for (uint32_t rd = 0; rd < rounds; ++rd) {  // the same count for every warp of the block
+    const uint32_t item = (rd * gridDim.x + blockIdx.x) * (uint32_t)slots + (uint32_t)slot;
     const uint32_t e = item * 32 + lane;
-    const bool valid = e < listed;
+    const bool valid = item < count && e < listed;
     const int t = valid ? (int)(a.dense_all ? e : a.dense[e]) : 0;
     const int i = valid ? work_particle(a, t) : 0;
     const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
     const int3 q = cell_of(a.c, g, xi);
     const bool exact = valid && exact_path(kKind, a, g, q, i);
-    // grouped cells are visited by groups (the exact rules apply per group)
-    const bool grouped = a.c.keps2 > 0.f;
     // the item's windows staged in shared memory: every warp holds the same
     // 32 particles, so warp 0's vote is the block's (block-uniform branch)
     bool staged = false;
@@ -1126,24 +1122,23 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
       staged = stage_wait(st, a, phase);
     }
     if (valid) {
-      const int total = grouped ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
-      const int lo = (int)((long long)total * warp / kDenseWarps);
-      const int hi = (int)((long long)total * (warp + 1) / kDenseWarps);
+      const int total = groups ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
+      const int lo = (int)((long long)total * sub / split);
+      const int hi = (int)((long long)total * (sub + 1) / split);
       P p(a, g, xi, i, exact);
-      // a staged window holds no grouped cell: the grouped walk visits its
-      // candidates in the order visit_window_chunk does
+      // a staged window holds no grouped cell: its runs are walked as runs
       if (kStage && staged)
-        visit_window_grouped(g, a, q, FromStage{stage, st.D}, p, lo, hi, hq);
-      else if (grouped)
+        visit_window_chunk(g, a.cs, a.n, q, FromStage{stage, st.D}, p, lo, hi, hq);
+      else if (groups)
         visit_window_grouped(g, a, q, FromGlobal{a.X}, p, lo, hi, hq);
       else
-        visit_window_chunk(g, a.cs, a.n, q, a.X, p, lo, hi);
+        visit_window_chunk(g, a.cs, a.n, q, FromGlobal{a.X}, p, lo, hi, hq);
       p.store(&part[warp][0][lane], 32);
     }
     __syncthreads();
-    if (warp == 0 && valid) {
+    if (sub == 0 && valid) {
       P p(a, g, xi, i, exact);
-      for (int k = 0; k < kDenseWarps; ++k) p.add(&part[k][0][lane], 32);
+      for (int k = 0; k < split; ++k) p.add(&part[slot * split + k][0][lane], 32);
       p.finish(a);
     }
     __syncthreads();
@@ -1160,6 +1155,7 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
           uint32_t* __restrict__ flags, const uint32_t* __restrict__ skeys,
           const uint32_t* __restrict__ cs, uint32_t* __restrict__ cell_flags, int* __restrict__ grp_cell,
           int* __restrict__ grp_off, int* __restrict__ grp_item_off, int* __restrict__ grp_item_slot) {
+  pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint32_t key = skeys[k];
@@ -1347,6 +1343,7 @@ __device__ __forceinline__ bool last_item(const GroupArgs& a, const Item& it, in
 // sum.w = its density), h_rank, ng, and clears the claimed entries.
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_group_insert(GroupArgs a) {
+  pdl_enter();
   __shared__ int sh[80];
   __shared__ int s_last;
   __shared__ int s_buf[2 * kGroupList];
@@ -1494,6 +1491,7 @@ __device__ __forceinline__ float group_dev(const GroupArgs& a, const Item& it, i
 // (lambda: sum = (lambda_rep, sum dev); xsph: sum.xyz) and clears gmax / acc.
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_group_devmax(GroupArgs a) {
+  pdl_enter();
   constexpr int C = kWhat == kGroupsLambda ? 1 : 3;
   __shared__ int s_last, s_flag;
   const int items = (int)a.flags[kGroupItems];
@@ -1538,6 +1536,7 @@ __global__ void __launch_bounds__(kGroupThreads) k_group_devmax(GroupArgs a) {
 
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_group_devsum(GroupArgs a) {
+  pdl_enter();
   constexpr int C = kWhat == kGroupsLambda ? 1 : 3;
   __shared__ int s_last;
   const int items = (int)a.flags[kGroupItems];
@@ -1602,6 +1601,7 @@ k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cel
             const int* __restrict__ grp_n, const int* __restrict__ grp_off, const int* __restrict__ grp_id,
             const int* __restrict__ grp_hash, const int* __restrict__ grp_rep, int np, int n,
             int* __restrict__ follow, int* __restrict__ blocks, uint32_t* __restrict__ flags) {
+  pdl_enter();
   __shared__ int sh[80];
   __shared__ int s_last;
   if (flags[kGroupCount] == 0u) {  // no grouped cell this step: every particle computes, in order
@@ -1655,6 +1655,7 @@ k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cel
 __global__ void __launch_bounds__(kWorkThreads)
 k_work_list(const int* __restrict__ follow, const int* __restrict__ blocks, int n, int* __restrict__ list,
             const uint32_t* __restrict__ flags) {
+  pdl_enter();
   __shared__ int sh[80];
   if (flags[kWorkIdentity]) return;
   const int i = blockIdx.x * kWorkThreads + threadIdx.x;
@@ -1672,6 +1673,7 @@ k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __re
          const uint32_t* __restrict__ iid_s, float4* __restrict__ npos, float4* __restrict__ vel,
          float4* __restrict__ pos, uint32_t* __restrict__ iid, const uint32_t* __restrict__ skeys,
          uint32_t* __restrict__ cell_flags, uint32_t* __restrict__ flags) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || flags[kWorkIdentity]) return;
   const int r = follow[i];
@@ -1709,6 +1711,7 @@ k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __re
 // particle), so the arbitrary ranks leave results bitwise reproducible.
 __global__ void __launch_bounds__(256) k_bucket_count(PassArgs a, uint32_t* __restrict__ bcnt,
                                                       uint2* __restrict__ bent) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int count = work_count(a);
   if (t == 0) a.flags[kBucketCount] = (uint32_t)count;
@@ -1722,6 +1725,7 @@ __global__ void __launch_bounds__(256) k_bucket_count(PassArgs a, uint32_t* __re
 
 __global__ void __launch_bounds__(256) k_bucket_scatter(PassArgs a, const uint32_t* __restrict__ bstart,
                                                         const uint2* __restrict__ bent, int* __restrict__ bucket) {
+  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= work_count(a)) return;
   const uint2 e = bent[t];
@@ -1767,10 +1771,10 @@ cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const flo
   if (n < kGroupCell) return cudaSuccess;  // no cell can hold kGroupCell particles
   const GroupArgs a = group_args(s, X, V, n);
   const int grid = c.dense_grid;
-  if constexpr (kWhat != kGroupsLambda) k_group_insert<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
+  if constexpr (kWhat != kGroupsLambda) PBF_LAUNCH(k_group_insert<kWhat>, grid, kGroupThreads, 0, stream, a);
   if constexpr (kWhat != kGroupsPos) {
-    k_group_devmax<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
-    k_group_devsum<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
+    PBF_LAUNCH(k_group_devmax<kWhat>, grid, kGroupThreads, 0, stream, a);
+    PBF_LAUNCH(k_group_devsum<kWhat>, grid, kGroupThreads, 0, stream, a);
   }
   return cudaGetLastError();
 }
@@ -1811,9 +1815,9 @@ cudaError_t bucket_by_cell(PassArgs& a, const SolverScratch& s, int n, cudaStrea
   cudaError_t e = cudaMemsetAsync(s.bcnt, 0, sizeof(uint32_t) * (a.c.cells + 1), stream);
   if (e != cudaSuccess) return e;
   const int blocks = (n + 255) / 256;
-  k_bucket_count<<<blocks, 256, 0, stream>>>(a, s.bcnt, s.bent);
+  PBF_LAUNCH(k_bucket_count, blocks, 256, 0, stream, a, s.bcnt, s.bent);
   if ((e = exclusive_scan(s.bcnt, s.bstart, a.c.cells + 1, s.bpart, stream)) != cudaSuccess) return e;
-  k_bucket_scatter<<<blocks, 256, 0, stream>>>(a, s.bstart, s.bent, s.bucket);
+  PBF_LAUNCH(k_bucket_scatter, blocks, 256, 0, stream, a, s.bstart, s.bent, s.bucket);
   a.list = s.bucket;
   a.count_word = kBucketCount;
   a.identity_word = -1;
@@ -1835,14 +1839,14 @@ cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
   if (a.dense_all) {
     // else the sparse kernel has nothing to do
   } else if (sparse_smem) {
-    k_sparse<kKind, true><<<sparse_blocks, kSparseThreads, sparse_smem, stream>>>(a);
+    PBF_LAUNCH((k_sparse<kKind, true>), sparse_blocks, kSparseThreads, sparse_smem, stream, a);
   } else {
-    k_sparse<kKind, false><<<sparse_blocks, kSparseThreads, 0, stream>>>(a);
+    PBF_LAUNCH((k_sparse<kKind, false>), sparse_blocks, kSparseThreads, 0, stream, a);
   }
   if (dense_smem)
-    k_dense<kKind, true><<<a.c.dense_grid, kDenseThreads, dense_smem, stream>>>(a);
+    PBF_LAUNCH((k_dense<kKind, true>), a.c.dense_grid, kDenseThreads, dense_smem, stream, a);
   else
-    k_dense<kKind, false><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
+    PBF_LAUNCH((k_dense<kKind, false>), a.c.dense_grid, kDenseThreads, 0, stream, a);
   return cudaGetLastError();
 }
 
@@ -1872,7 +1876,7 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
   cudaError_t e = cudaMemsetAsync(s.cell_flags, 0, sizeof(uint32_t) * (c.cells + 1), stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.flags, 0, sizeof(uint32_t) * kNumFlags, stream);
   if (e != cudaSuccess) return e;
-  k_reorder<<<(n + 255) / 256, 256, 0, stream>>>(perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
+  PBF_LAUNCH(k_reorder, (n + 255) / 256, 256, 0, stream, perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
                                                   s.flags, s.keys_sorted, s.cell_start, s.cell_flags,
                                                   s.grp_cell, s.grp_off, s.grp_item_off, s.grp_item_slot);
   return cudaGetLastError();
@@ -1887,17 +1891,17 @@ bool use_work_list(const StepConsts& c, int n) { return n >= kGroupCell && c.kep
 
 cudaError_t launch_work_list(const SolverScratch& s, int n, cudaStream_t stream) {
   const int blocks = (n + kWorkThreads - 1) / kWorkThreads;
-  k_work_mark<<<blocks, kWorkThreads, 0, stream>>>(s.keys_sorted, s.cell_flags, s.grp_n, s.grp_off, s.grp_id,
+  PBF_LAUNCH(k_work_mark, blocks, kWorkThreads, 0, stream, s.keys_sorted, s.cell_flags, s.grp_n, s.grp_off, s.grp_id,
                                                    s.grp_hash, s.grp_rep, s.grp_pool, n, s.work_follow,
                                                    s.work_blocks, s.flags);
-  k_work_list<<<blocks, kWorkThreads, 0, stream>>>(s.work_follow, s.work_blocks, n, s.work_list, s.flags);
+  PBF_LAUNCH(k_work_list, blocks, kWorkThreads, 0, stream, s.work_follow, s.work_blocks, n, s.work_list, s.flags);
   return cudaGetLastError();
 }
 
 template <int kKind>
 cudaError_t launch_follow(const StepConsts& c, const SolverScratch& s, const float4* X, int n, float4* T,
                           float4* pos, float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream) {
-  k_follow<kKind><<<(n + 255) / 256, 256, 0, stream>>>(s.work_follow, n, c, X, s.lambda, s.rho, T, s.xs, s.iid_s,
+  PBF_LAUNCH(k_follow<kKind>, (n + 255) / 256, 256, 0, stream, s.work_follow, n, c, X, s.lambda, s.rho, T, s.xs, s.iid_s,
                                                        npos, vel, pos, iid, s.keys_sorted, s.cell_flags, s.flags);
   return cudaGetLastError();
 }
@@ -2001,6 +2005,7 @@ struct VortEta {
 __global__ void __launch_bounds__(128)
 k_vort_omega(StepConsts c, Geometry G, const float4* __restrict__ X, const float4* __restrict__ U,
              const uint32_t* __restrict__ cs, int n, float4* __restrict__ W) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = X[i];
@@ -2013,6 +2018,7 @@ k_vort_omega(StepConsts c, Geometry G, const float4* __restrict__ X, const float
 __global__ void __launch_bounds__(128)
 k_vort_force(StepConsts c, Geometry G, const float4* __restrict__ X, const float4* __restrict__ W,
              const uint32_t* __restrict__ cs, int n, float4* __restrict__ U) {
+  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = X[i];
@@ -2036,8 +2042,8 @@ k_vort_force(StepConsts c, Geometry G, const float4* __restrict__ X, const float
 cudaError_t launch_vorticity(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                              const SolverScratch& s, float4* NV, cudaStream_t stream) {
   const int blocks = (n + 127) / 128;
-  k_vort_omega<<<blocks, 128, 0, stream>>>(c, G, X, NV, cs, n, s.xb);
-  k_vort_force<<<blocks, 128, 0, stream>>>(c, G, X, s.xb, cs, n, NV);
+  PBF_LAUNCH(k_vort_omega, blocks, 128, 0, stream, c, G, X, NV, cs, n, s.xb);
+  PBF_LAUNCH(k_vort_force, blocks, 128, 0, stream, c, G, X, s.xb, cs, n, NV);
   return cudaGetLastError();
 }
 

@@ -119,7 +119,7 @@ class InverseProblem:
         times = {}
         tune = self.sim.tuning()
         for lane_count in lanes:
-            self.sim.set_tuning(tune["dense_window"], tune["dense_all"], tune["order"], int(lane_count))
+            self.sim.set_tuning(**{**tune, "bwd_lanes": int(lane_count)})
             self.loss_and_grad(vel0, amp)  # untimed: the first evaluation of a setting
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -129,7 +129,7 @@ class InverseProblem:
             torch.cuda.synchronize()
             times[int(lane_count)] = e0.elapsed_time(e1)
         best = min(times, key=times.get)
-        self.sim.set_tuning(tune["dense_window"], tune["dense_all"], tune["order"], best)
+        self.sim.set_tuning(**{**tune, "bwd_lanes": best})
         return {"bwd_lanes": best, "ms": times}
 
     def optimise(self, iters: int = 10, lr_vel: float = 1e-9, lr_amp: float = 1e-10,

@@ -42,6 +42,20 @@ def _check_state(t: torch.Tensor, name: str, n: int, cols: Optional[int]) -> Non
         raise ValueError(f"{name} must be float32 of shape (>= {n}, {cols})")
 
 
+def _tuning(dense_window, dense_all, order, bwd_lanes, stage_sparse, stage_dense, queue_sparse, queue_dense,
+            dense_split) -> PbfTuning:
+    t = PbfTuning()
+    t.dense_window, t.dense_all, t.order, t.bwd_lanes = int(dense_window), int(dense_all), int(order), int(bwd_lanes)
+    t.stage_sparse, t.stage_dense = int(stage_sparse), int(stage_dense)
+    t.queue_sparse, t.queue_dense, t.dense_split = int(queue_sparse), int(queue_dense), int(dense_split)
+    return t
+
+
+def _tuning_dict(t: PbfTuning) -> dict:
+    return {k: getattr(t, k) for k in ("dense_window", "dense_all", "order", "bwd_lanes", "stage_sparse",
+                                       "stage_dense", "queue_sparse", "queue_dense", "dense_split")}
+
+
 class Simulator:
     """One PBF solver instance: ``Simulator(params, ulim, llim)`` + ``step``.
 
@@ -154,21 +168,20 @@ class Simulator:
         return g_pos, g_vel, g_lim
 
     def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, bwd_lanes: int = 0,
-                   stage_sparse: int = -1, stage_dense: int = -1) -> None:
-        """The dense-kernel, particle-order and shared-memory staging choices of
-        the following steps, and the reverse pass's lanes per particle
-        (pbf_set_tuning); 0 / -1: the defaults (stage_*: 0 turns staging off)."""
-        t = PbfTuning()
-        t.dense_window, t.dense_all, t.order = int(dense_window), int(dense_all), int(order)
-        t.bwd_lanes = int(bwd_lanes)
-        t.stage_sparse, t.stage_dense = int(stage_sparse), int(stage_dense)
-        check(self._L.pbf_set_tuning(self._h, ctypes.byref(t)), "pbf_set_tuning")
+                   stage_sparse: int = -1, stage_dense: int = -1, queue_sparse: int = 0, queue_dense: int = 0,
+                   dense_split: int = 0) -> None:
+        """The neighbour passes' choices for the following steps (dense window,
+        dense-for-all, particle order, shared-memory stages, hit queues, dense
+        split) and the reverse pass's lanes per particle (pbf_set_tuning); 0 /
+        -1: the defaults (stage_*: 0 turns staging off)."""
+        check(self._L.pbf_set_tuning(self._h, ctypes.byref(_tuning(
+            dense_window, dense_all, order, bwd_lanes, stage_sparse, stage_dense, queue_sparse, queue_dense,
+            dense_split))), "pbf_set_tuning")
 
     def tuning(self) -> dict:
         t = PbfTuning()
         check(self._L.pbf_get_tuning(self._h, ctypes.byref(t)), "pbf_get_tuning")
-        return {"dense_window": t.dense_window, "dense_all": t.dense_all, "order": t.order,
-                "bwd_lanes": t.bwd_lanes, "stage_sparse": t.stage_sparse, "stage_dense": t.stage_dense}
+        return _tuning_dict(t)
 
     def check_device(self, stream=None) -> None:
         """Raise PbfError (PBF_ERR_TIMEOUT) if a bounded device-side wait of the
@@ -298,18 +311,18 @@ class Ensemble:
         check(self._L.pbf_batch_set_limits(self._h, int(scene), _vec3(ulim), _vec3(llim)), "pbf_batch_set_limits")
 
     def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, stage_sparse: int = -1,
-                   stage_dense: int = -1) -> None:
+                   stage_dense: int = -1, queue_sparse: int = 0, queue_dense: int = 0, dense_split: int = 0) -> None:
         """The neighbour passes' choices for the following steps (pbf_batch_set_tuning)."""
-        t = PbfTuning()
-        t.dense_window, t.dense_all, t.order = int(dense_window), int(dense_all), int(order)
-        t.stage_sparse, t.stage_dense = int(stage_sparse), int(stage_dense)
-        check(self._L.pbf_batch_set_tuning(self._h, ctypes.byref(t)), "pbf_batch_set_tuning")
+        check(self._L.pbf_batch_set_tuning(self._h, ctypes.byref(_tuning(
+            dense_window, dense_all, order, 0, stage_sparse, stage_dense, queue_sparse, queue_dense,
+            dense_split))), "pbf_batch_set_tuning")
 
     def tuning(self) -> dict:
         t = PbfTuning()
         check(self._L.pbf_batch_get_tuning(self._h, ctypes.byref(t)), "pbf_batch_get_tuning")
-        return {"dense_window": t.dense_window, "dense_all": t.dense_all, "order": t.order,
-                "stage_sparse": t.stage_sparse, "stage_dense": t.stage_dense}
+        d = _tuning_dict(t)
+        del d["bwd_lanes"]
+        return d
 
     def check_device(self, stream=None) -> None:
         """Raise PbfError (PBF_ERR_TIMEOUT) if a bounded device-side wait of the

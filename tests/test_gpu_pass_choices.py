@@ -1,15 +1,19 @@
-"""GPU tests of the neighbour passes' shared-memory staging (pbf_tuning
-stage_sparse / stage_dense): a block whose particles share one column of
-cells copies the column runs of their windows into shared memory with bulk
-asynchronous copies and reads candidate positions there.
+"""GPU tests of the neighbour passes' tunable choices beyond the dense window
+(pbf_tuning): shared-memory staging (stage_sparse / stage_dense: a block whose
+particles share one column of cells copies the column runs of their windows
+into shared memory with bulk asynchronous copies and reads candidate
+positions there), the hit queues (queue_sparse / queue_dense) and the dense
+kernel's warps per batch (dense_split).
 
 Bars:
-  * staging on or off, in either kernel, gives bitwise the same states over
-    many steps (the same candidates in the same order from either copy of
-    the positions) -- on scenes that pile particles up (dam-break parameters)
-    and on scenes at rest (the reference's parameters), single and batched;
+  * staging and the hit queues change nothing: on or off, in either kernel,
+    bitwise the same states over many steps (the same candidates summed in
+    the same order) -- on scenes that pile particles up (dam-break
+    parameters) and on scenes at rest (the reference's parameters), single
+    and batched;
   * no staging wait gives up (pbf_check_device);
-  * one staged step matches the FP64 oracle within 1e-5 h.
+  * a staged step, and a step at every dense split (which changes the order of
+    window sums), match the FP64 oracle within 1e-5 h.
 """
 from __future__ import annotations
 
@@ -22,7 +26,8 @@ pytestmark = pytest.mark.gpu
 
 OFF = {"stage_sparse": 0, "stage_dense": 0}
 CHOICES = [{"stage_sparse": 1024, "stage_dense": 0}, {"stage_sparse": 0, "stage_dense": 1536},
-           {"stage_sparse": 2048, "stage_dense": 4096}]
+           {"stage_sparse": 2048, "stage_dense": 4096}, {"queue_sparse": 1, "queue_dense": 1},
+           {"queue_sparse": 4, "queue_dense": 2}]
 
 
 def run_steps(pbf, scene, params, steps, tuning):
@@ -101,6 +106,28 @@ def test_staged_step_matches_fp64(pbf, oracle, cuda):
         sim.step(pos, npos, vel, nvel, iid, n)
         torch.cuda.synchronize()
         sim.check_device()
+    r = oracle.step(p, sc.ulim, sc.llim, sc.pos.astype(np.float64), np.zeros((n, 4)), np.arange(n, dtype=np.uint32),
+                    "f64")
+    np.testing.assert_array_equal(iid.cpu().numpy().astype(np.uint32), r["iid"])
+    assert np.abs(npos.cpu().numpy()[:, :3] - r["npos"][:, :3]).max() <= TOL_X
+
+
+@pytest.mark.parametrize("split", [1, 2, 4, 8])
+def test_dense_split_step_matches_fp64(pbf, oracle, cuda, split):
+    import torch
+
+    sc = pbf.scenes.dam_break(seed=7)
+    p = ref_params(pbf)
+    n = sc.n
+    pos = torch.from_numpy(sc.pos).cuda()
+    vel = torch.zeros_like(pos)
+    iid = torch.arange(n, dtype=torch.int32, device="cuda")
+    npos, nvel = torch.empty_like(pos), torch.empty_like(vel)
+    with pbf.Simulator(p, sc.ulim, sc.llim, n) as sim:
+        sim.set_tuning(dense_all=1, dense_split=split)
+        assert sim.tuning()["dense_split"] == split
+        sim.step(pos, npos, vel, nvel, iid, n)
+        torch.cuda.synchronize()
     r = oracle.step(p, sc.ulim, sc.llim, sc.pos.astype(np.float64), np.zeros((n, 4)), np.arange(n, dtype=np.uint32),
                     "f64")
     np.testing.assert_array_equal(iid.cpu().numpy().astype(np.uint32), r["iid"])
