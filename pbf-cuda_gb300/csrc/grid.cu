@@ -63,7 +63,6 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
 
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_reduce(const uint32_t* __restrict__ in, int len, uint32_t* __restrict__ partials) {
-  pdl_enter();
   __shared__ uint32_t smem[kScanThreads / 32 + 1];
   const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   uint32_t sum = 0;
@@ -77,7 +76,6 @@ k_scan_reduce(const uint32_t* __restrict__ in, int len, uint32_t* __restrict__ p
 
 __global__ void __launch_bounds__(kTopThreads)
 k_scan_top(uint32_t* __restrict__ partials, int count) {
-  pdl_enter();
   __shared__ uint32_t smem[kTopThreads / 32 + 1];
   constexpr int kItems = kMaxScanPartials / kTopThreads;
   const int base = threadIdx.x * kItems;
@@ -99,7 +97,6 @@ k_scan_top(uint32_t* __restrict__ partials, int count) {
 
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_down(const uint32_t* in, int len, const uint32_t* __restrict__ partials, uint32_t* out) {
-  pdl_enter();
   // in and out may alias (in-place scan): every thread reads its items before
   // writing them, and no thread touches another thread's items.
   __shared__ uint32_t smem[kScanThreads / 32 + 1];
@@ -127,9 +124,9 @@ cudaError_t exclusive_scan(const uint32_t* in, uint32_t* out, int len, uint32_t*
                            cudaStream_t stream) {
   const int tiles = (len + kScanTile - 1) / kScanTile;
   if (tiles > kMaxScanPartials) return cudaErrorInvalidValue;
-  PBF_LAUNCH(k_scan_reduce, tiles, kScanThreads, 0, stream, in, len, partials);
-  PBF_LAUNCH(k_scan_top, 1, kTopThreads, 0, stream, partials, tiles);
-  PBF_LAUNCH(k_scan_down, tiles, kScanThreads, 0, stream, in, len, partials, out);
+  k_scan_reduce<<<tiles, kScanThreads, 0, stream>>>(in, len, partials);
+  k_scan_top<<<1, kTopThreads, 0, stream>>>(partials, tiles);
+  k_scan_down<<<tiles, kScanThreads, 0, stream>>>(in, len, partials, out);
   return cudaGetLastError();
 }
 
@@ -145,7 +142,6 @@ template <bool kPredict>
 __global__ void __launch_bounds__(256)
 k_hash(const float4* __restrict__ pos, const float4* __restrict__ vel, int n, StepConsts c,
        Geometry G, uint32_t* __restrict__ keys, uint32_t* __restrict__ cell_count) {
-  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float4 x = pos[i];
@@ -170,7 +166,6 @@ k_hash(const float4* __restrict__ pos, const float4* __restrict__ vel, int n, St
 __global__ void __launch_bounds__(kSortThreads)
 k_radix_upsweep(const uint32_t* __restrict__ keys, int n, int shift,
                 uint32_t* __restrict__ counts, int ntiles) {
-  pdl_enter();
   __shared__ uint32_t hist[kRadix];
   hist[threadIdx.x] = 0;
   __syncthreads();
@@ -197,7 +192,6 @@ __global__ void __launch_bounds__(kSortThreads)
 k_radix_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                   uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int n,
                   int shift, const uint32_t* __restrict__ counts_scanned, int ntiles) {
-  pdl_enter();
   __shared__ uint32_t whist[kSortWarps][kRadix];
   const int warp = threadIdx.x >> 5;
   const unsigned lane = threadIdx.x & 31;
@@ -249,7 +243,6 @@ k_radix_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restri
 
 __global__ void k_export_ranges(const uint32_t* __restrict__ cs, int cells,
                                 uint32_t* __restrict__ start, uint32_t* __restrict__ end) {
-  pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= cells) return;
   const uint32_t s = cs[k], e = cs[k + 1];
@@ -287,9 +280,9 @@ cudaError_t build_grid(const StepConsts& c, const Geometry& G, const float4* pos
     return err;
   const int blocks = (n + 255) / 256;
   if (xstar)
-    PBF_LAUNCH(k_hash<false>, blocks, 256, 0, stream, xstar, nullptr, n, c, G, s.keys_a, s.cell_count);
+    k_hash<false><<<blocks, 256, 0, stream>>>(xstar, nullptr, n, c, G, s.keys_a, s.cell_count);
   else
-    PBF_LAUNCH(k_hash<true>, blocks, 256, 0, stream, pos, vel, n, c, G, s.keys_a, s.cell_count);
+    k_hash<true><<<blocks, 256, 0, stream>>>(pos, vel, n, c, G, s.keys_a, s.cell_count);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   if (keys_copy &&
       (err = cudaMemcpyAsync(keys_copy, s.keys_a, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice,
@@ -311,11 +304,11 @@ cudaError_t build_grid(const StepConsts& c, const Geometry& G, const float4* pos
   for (int p = 0; p < passes; ++p) {
     const int shift = p * kRadixBits;
     const bool last = p == passes - 1;  // its keys stay: the passes flag cells by them
-    PBF_LAUNCH(k_radix_upsweep, ntiles, kSortThreads, 0, stream, kin, n, shift, s.radix_counts, ntiles);
+    k_radix_upsweep<<<ntiles, kSortThreads, 0, stream>>>(kin, n, shift, s.radix_counts, ntiles);
     if ((err = exclusive_scan(s.radix_counts, s.radix_counts, clen, s.scan_partials, stream)) !=
         cudaSuccess)
       return err;
-    PBF_LAUNCH(k_radix_downsweep, ntiles, kSortThreads, 0, stream, kin, vin, kout, vout, n, shift,
+    k_radix_downsweep<<<ntiles, kSortThreads, 0, stream>>>(kin, vin, kout, vout, n, shift,
                                                            s.radix_counts, ntiles);
     if (last) s.keys_sorted = kout;
     if ((err = cudaGetLastError()) != cudaSuccess) return err;
@@ -332,7 +325,7 @@ cudaError_t build_grid(const StepConsts& c, const Geometry& G, const float4* pos
 cudaError_t export_ranges(const StepConsts& c, const uint32_t* cell_start, uint32_t* start,
                           uint32_t* end, cudaStream_t stream) {
   if (c.cells <= 0) return cudaSuccess;
-  PBF_LAUNCH(k_export_ranges, (c.cells + 255) / 256, 256, 0, stream, cell_start, c.cells, start, end);
+  k_export_ranges<<<(c.cells + 255) / 256, 256, 0, stream>>>(cell_start, c.cells, start, end);
   return cudaGetLastError();
 }
 

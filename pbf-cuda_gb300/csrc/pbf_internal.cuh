@@ -75,50 +75,6 @@ struct Geometry {
   const uint16_t* sid;      // [n] scene of each particle slot
 };
 
-// ---- programmatic dependent launch --------------------------------------------------
-//
-// The kernels of a step are launched with programmatic stream serialization
-// (launch_step_kernel): a kernel may be scheduled while the kernel before it
-// on the stream still runs, which hides its launch latency.  Each of them
-// calls pdl_enter() before it touches global memory: griddepcontrol.wait
-// returns once the previous kernel has completed and its writes are visible,
-// then griddepcontrol.launch_dependents lets the next kernel be scheduled.
-// Memory effects therefore keep plain stream order.  Without the launch
-// attribute both instructions do nothing.  PBF_PDL=0 (a build-time macro)
-// launches without the attribute.
-#ifndef PBF_PDL
-#define PBF_PDL 1
-#endif
-
-__device__ __forceinline__ void pdl_enter() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-template <typename... KArgs, typename... Args>
-inline cudaError_t launch_step_kernel(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                                      cudaStream_t stream, Args... args) {
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = stream;
-  cfg.attrs = attr;
-  cfg.numAttrs = PBF_PDL ? 1 : 0;
-  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
-}
-
-// launch_step_kernel from a function returning cudaError_t, returning its error.
-#define PBF_LAUNCH(kernel, grid, block, smem, stream, ...)                                           \
-  do {                                                                                             \
-    const cudaError_t pbf_launch_e_ =                                                             \
-        ::pbf::launch_step_kernel(kernel, dim3(grid), dim3(block), smem, stream, __VA_ARGS__);    \
-    if (pbf_launch_e_ != cudaSuccess) return pbf_launch_e_;                                        \
-  } while (0)
-
 __device__ __forceinline__ SceneGeom geom_of(const StepConsts& c, const Geometry& G, int i) {
   return G.scenes ? G.scenes[G.sid[i]] : c.geom;
 }

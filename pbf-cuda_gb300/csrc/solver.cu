@@ -153,6 +153,27 @@ __device__ __forceinline__ int window_total(const SceneGeom& g, const uint32_t* 
   return total;
 }
 
+// Candidates of the window and the chunks of 32 consecutive candidates it
+// splits into (per run), from one walk over its runs.
+__device__ __forceinline__ int window_total_chunks(const SceneGeom& g, const uint32_t* __restrict__ cs, int n,
+                                                   int3 q, int& chunks) {
+  int total = 0;
+  chunks = 0;
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      int s, e;
+      column_run(g, cs, n, x, y, q.z, s, e);
+      total += e - s;
+      chunks += (e - s + 31) >> 5;
+    }
+  }
+  return total;
+}
+
 // Whether a cell of the window carries any of `bits`.
 __device__ __forceinline__ bool window_flagged(const SceneGeom& g,
                                                const uint32_t* __restrict__ cell_flags, int3 q,
@@ -170,24 +191,6 @@ __device__ __forceinline__ bool window_flagged(const SceneGeom& g,
     }
   }
   return false;
-}
-
-// Chunks of 32 consecutive candidates the window splits into (per run).
-__device__ __forceinline__ int window_chunks(const SceneGeom& g, const uint32_t* __restrict__ cs,
-                                             int n, int3 q) {
-  int chunks = 0;
-  for (int dx = -1; dx <= 1; ++dx) {
-    const int x = q.x + dx;
-    if (x < 0 || x >= g.dims[0]) continue;
-    for (int dy = -1; dy <= 1; ++dy) {
-      const int y = q.y + dy;
-      if (y < 0 || y >= g.dims[1]) continue;
-      int s, e;
-      column_run(g, cs, n, x, y, q.z, s, e);
-      chunks += (e - s + 31) >> 5;
-    }
-  }
-  return chunks;
 }
 
 // ---- where a pass reads candidate positions ---------------------------------------------
@@ -967,13 +970,12 @@ __device__ __forceinline__ void stage_drain(StageState& st, uint32_t phase) {
 // The plain (not grouped) walk of a sparse-kernel particle's window.
 template <int kKind, class P, class Src>
 __device__ __forceinline__ void sparse_visit(const PassArgs& a, const SceneGeom& g, int3 q, const Src& src,
-                                             P& p, bool exact, int i, HitQueue& hq) {
+                                             P& p, bool exact, int i, int chunks, HitQueue& hq) {
   if (exact) {
     visit_window(g, a.cs, a.n, q, src, p);  // non-neighbours matter: visit every candidate
   } else if (kKind == kLambda) {
     visit_window_masked(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // saves its masks
-  } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) &&
-             window_chunks(g, a.cs, a.n, q) <= kMaskWords) {
+  } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) && chunks <= kMaskWords) {
     visit_window_saved(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // lambda's masks
   } else {
     visit_window_masked(g, a.cs, a.n, q, src, p, nullptr, 0, i, hq);
@@ -1002,7 +1004,6 @@ __device__ __forceinline__ void stage_init(StageState& st) {
 // stage_sparse > 0); the other carries no staging code.
 template <int kKind, bool kStage>
 __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
-  pdl_enter();
   using P = typename PassOf<kKind>::type;
   __shared__ uint32_t q_mask[kMaxQueueSparse * kSparseThreads];
   __shared__ int q_base[kMaxQueueSparse * kSparseThreads];
@@ -1021,7 +1022,8 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
   const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
   const int3 q = cell_of(a.c, g, xi);
-  const int total = valid ? window_total(g, a.cs, a.n, q) : 0;
+  int chunks = 0;
+  const int total = valid ? window_total_chunks(g, a.cs, a.n, q, chunks) : 0;
   // a window over dense_window candidates that its grouped cells bring back
   // under it is walked here, group by group (no masks)
   const bool grouped = valid && total > a.c.dense_window && a.c.keps2 > 0.f;
@@ -1055,14 +1057,13 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   }
   if (active) {
     P p(a, g, xi, i, exact);
-    if (!grouped && !exact && a.c.queue_sparse > 1 && window_chunks(g, a.cs, a.n, q) <= a.c.queue_sparse)
-      hq.cap = a.c.queue_sparse;
+    if (!grouped && !exact && chunks <= a.c.queue_sparse) hq.cap = a.c.queue_sparse;
     if (grouped)
       visit_window_grouped(g, a, q, FromGlobal{a.X}, p, 0, entries, hq);
     else if (kStage && staged)
-      sparse_visit<kKind>(a, g, q, FromStage{stage, st.D}, p, exact, i, hq);
+      sparse_visit<kKind>(a, g, q, FromStage{stage, st.D}, p, exact, i, chunks, hq);
     else
-      sparse_visit<kKind>(a, g, q, FromGlobal{a.X}, p, exact, i, hq);
+      sparse_visit<kKind>(a, g, q, FromGlobal{a.X}, p, exact, i, chunks, hq);
     p.finish(a);
   }
   if (kStage && cap > 0) stage_drain(st, phase);
@@ -1072,7 +1073,6 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
 // stage_dense > 0); the other carries no staging code.
 template <int kKind, bool kStage>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
-  pdl_enter();
   using P = typename PassOf<kKind>::type;
   __shared__ float part[kDenseWarps][kMaxFields][32];
   __shared__ uint32_t q_mask[kMaxQueueDense * kDenseThreads];
@@ -1155,7 +1155,6 @@ k_reorder(const uint32_t* __restrict__ perm, const float4* __restrict__ pos,
           uint32_t* __restrict__ flags, const uint32_t* __restrict__ skeys,
           const uint32_t* __restrict__ cs, uint32_t* __restrict__ cell_flags, int* __restrict__ grp_cell,
           int* __restrict__ grp_off, int* __restrict__ grp_item_off, int* __restrict__ grp_item_slot) {
-  pdl_enter();
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint32_t key = skeys[k];
@@ -1343,7 +1342,6 @@ __device__ __forceinline__ bool last_item(const GroupArgs& a, const Item& it, in
 // sum.w = its density), h_rank, ng, and clears the claimed entries.
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_group_insert(GroupArgs a) {
-  pdl_enter();
   __shared__ int sh[80];
   __shared__ int s_last;
   __shared__ int s_buf[2 * kGroupList];
@@ -1491,7 +1489,6 @@ __device__ __forceinline__ float group_dev(const GroupArgs& a, const Item& it, i
 // (lambda: sum = (lambda_rep, sum dev); xsph: sum.xyz) and clears gmax / acc.
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_group_devmax(GroupArgs a) {
-  pdl_enter();
   constexpr int C = kWhat == kGroupsLambda ? 1 : 3;
   __shared__ int s_last, s_flag;
   const int items = (int)a.flags[kGroupItems];
@@ -1536,7 +1533,6 @@ __global__ void __launch_bounds__(kGroupThreads) k_group_devmax(GroupArgs a) {
 
 template <int kWhat>
 __global__ void __launch_bounds__(kGroupThreads) k_group_devsum(GroupArgs a) {
-  pdl_enter();
   constexpr int C = kWhat == kGroupsLambda ? 1 : 3;
   __shared__ int s_last;
   const int items = (int)a.flags[kGroupItems];
@@ -1601,7 +1597,6 @@ k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cel
             const int* __restrict__ grp_n, const int* __restrict__ grp_off, const int* __restrict__ grp_id,
             const int* __restrict__ grp_hash, const int* __restrict__ grp_rep, int np, int n,
             int* __restrict__ follow, int* __restrict__ blocks, uint32_t* __restrict__ flags) {
-  pdl_enter();
   __shared__ int sh[80];
   __shared__ int s_last;
   if (flags[kGroupCount] == 0u) {  // no grouped cell this step: every particle computes, in order
@@ -1655,7 +1650,6 @@ k_work_mark(const uint32_t* __restrict__ skeys, const uint32_t* __restrict__ cel
 __global__ void __launch_bounds__(kWorkThreads)
 k_work_list(const int* __restrict__ follow, const int* __restrict__ blocks, int n, int* __restrict__ list,
             const uint32_t* __restrict__ flags) {
-  pdl_enter();
   __shared__ int sh[80];
   if (flags[kWorkIdentity]) return;
   const int i = blockIdx.x * kWorkThreads + threadIdx.x;
@@ -1673,7 +1667,6 @@ k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __re
          const uint32_t* __restrict__ iid_s, float4* __restrict__ npos, float4* __restrict__ vel,
          float4* __restrict__ pos, uint32_t* __restrict__ iid, const uint32_t* __restrict__ skeys,
          uint32_t* __restrict__ cell_flags, uint32_t* __restrict__ flags) {
-  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || flags[kWorkIdentity]) return;
   const int r = follow[i];
@@ -1711,7 +1704,6 @@ k_follow(const int* __restrict__ follow, int n, StepConsts c, const float4* __re
 // particle), so the arbitrary ranks leave results bitwise reproducible.
 __global__ void __launch_bounds__(256) k_bucket_count(PassArgs a, uint32_t* __restrict__ bcnt,
                                                       uint2* __restrict__ bent) {
-  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int count = work_count(a);
   if (t == 0) a.flags[kBucketCount] = (uint32_t)count;
@@ -1725,7 +1717,6 @@ __global__ void __launch_bounds__(256) k_bucket_count(PassArgs a, uint32_t* __re
 
 __global__ void __launch_bounds__(256) k_bucket_scatter(PassArgs a, const uint32_t* __restrict__ bstart,
                                                         const uint2* __restrict__ bent, int* __restrict__ bucket) {
-  pdl_enter();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= work_count(a)) return;
   const uint2 e = bent[t];
@@ -1771,10 +1762,10 @@ cudaError_t launch_groups(const StepConsts& c, const SolverScratch& s, const flo
   if (n < kGroupCell) return cudaSuccess;  // no cell can hold kGroupCell particles
   const GroupArgs a = group_args(s, X, V, n);
   const int grid = c.dense_grid;
-  if constexpr (kWhat != kGroupsLambda) PBF_LAUNCH(k_group_insert<kWhat>, grid, kGroupThreads, 0, stream, a);
+  if constexpr (kWhat != kGroupsLambda) k_group_insert<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
   if constexpr (kWhat != kGroupsPos) {
-    PBF_LAUNCH(k_group_devmax<kWhat>, grid, kGroupThreads, 0, stream, a);
-    PBF_LAUNCH(k_group_devsum<kWhat>, grid, kGroupThreads, 0, stream, a);
+    k_group_devmax<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
+    k_group_devsum<kWhat><<<grid, kGroupThreads, 0, stream>>>(a);
   }
   return cudaGetLastError();
 }
@@ -1815,9 +1806,9 @@ cudaError_t bucket_by_cell(PassArgs& a, const SolverScratch& s, int n, cudaStrea
   cudaError_t e = cudaMemsetAsync(s.bcnt, 0, sizeof(uint32_t) * (a.c.cells + 1), stream);
   if (e != cudaSuccess) return e;
   const int blocks = (n + 255) / 256;
-  PBF_LAUNCH(k_bucket_count, blocks, 256, 0, stream, a, s.bcnt, s.bent);
+  k_bucket_count<<<blocks, 256, 0, stream>>>(a, s.bcnt, s.bent);
   if ((e = exclusive_scan(s.bcnt, s.bstart, a.c.cells + 1, s.bpart, stream)) != cudaSuccess) return e;
-  PBF_LAUNCH(k_bucket_scatter, blocks, 256, 0, stream, a, s.bstart, s.bent, s.bucket);
+  k_bucket_scatter<<<blocks, 256, 0, stream>>>(a, s.bstart, s.bent, s.bucket);
   a.list = s.bucket;
   a.count_word = kBucketCount;
   a.identity_word = -1;
@@ -1839,14 +1830,14 @@ cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
   if (a.dense_all) {
     // else the sparse kernel has nothing to do
   } else if (sparse_smem) {
-    PBF_LAUNCH((k_sparse<kKind, true>), sparse_blocks, kSparseThreads, sparse_smem, stream, a);
+    k_sparse<kKind, true><<<sparse_blocks, kSparseThreads, sparse_smem, stream>>>(a);
   } else {
-    PBF_LAUNCH((k_sparse<kKind, false>), sparse_blocks, kSparseThreads, 0, stream, a);
+    k_sparse<kKind, false><<<sparse_blocks, kSparseThreads, 0, stream>>>(a);
   }
   if (dense_smem)
-    PBF_LAUNCH((k_dense<kKind, true>), a.c.dense_grid, kDenseThreads, dense_smem, stream, a);
+    k_dense<kKind, true><<<a.c.dense_grid, kDenseThreads, dense_smem, stream>>>(a);
   else
-    PBF_LAUNCH((k_dense<kKind, false>), a.c.dense_grid, kDenseThreads, 0, stream, a);
+    k_dense<kKind, false><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -1876,7 +1867,7 @@ cudaError_t reorder(const StepConsts& c, const uint32_t* perm, const float4* pos
   cudaError_t e = cudaMemsetAsync(s.cell_flags, 0, sizeof(uint32_t) * (c.cells + 1), stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(s.flags, 0, sizeof(uint32_t) * kNumFlags, stream);
   if (e != cudaSuccess) return e;
-  PBF_LAUNCH(k_reorder, (n + 255) / 256, 256, 0, stream, perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
+  k_reorder<<<(n + 255) / 256, 256, 0, stream>>>(perm, pos, vel, iid, n, c, s.xs, s.xa, s.iid_s,
                                                   s.flags, s.keys_sorted, s.cell_start, s.cell_flags,
                                                   s.grp_cell, s.grp_off, s.grp_item_off, s.grp_item_slot);
   return cudaGetLastError();
@@ -1891,17 +1882,17 @@ bool use_work_list(const StepConsts& c, int n) { return n >= kGroupCell && c.kep
 
 cudaError_t launch_work_list(const SolverScratch& s, int n, cudaStream_t stream) {
   const int blocks = (n + kWorkThreads - 1) / kWorkThreads;
-  PBF_LAUNCH(k_work_mark, blocks, kWorkThreads, 0, stream, s.keys_sorted, s.cell_flags, s.grp_n, s.grp_off, s.grp_id,
+  k_work_mark<<<blocks, kWorkThreads, 0, stream>>>(s.keys_sorted, s.cell_flags, s.grp_n, s.grp_off, s.grp_id,
                                                    s.grp_hash, s.grp_rep, s.grp_pool, n, s.work_follow,
                                                    s.work_blocks, s.flags);
-  PBF_LAUNCH(k_work_list, blocks, kWorkThreads, 0, stream, s.work_follow, s.work_blocks, n, s.work_list, s.flags);
+  k_work_list<<<blocks, kWorkThreads, 0, stream>>>(s.work_follow, s.work_blocks, n, s.work_list, s.flags);
   return cudaGetLastError();
 }
 
 template <int kKind>
 cudaError_t launch_follow(const StepConsts& c, const SolverScratch& s, const float4* X, int n, float4* T,
                           float4* pos, float4* npos, float4* vel, uint32_t* iid, cudaStream_t stream) {
-  PBF_LAUNCH(k_follow<kKind>, (n + 255) / 256, 256, 0, stream, s.work_follow, n, c, X, s.lambda, s.rho, T, s.xs, s.iid_s,
+  k_follow<kKind><<<(n + 255) / 256, 256, 0, stream>>>(s.work_follow, n, c, X, s.lambda, s.rho, T, s.xs, s.iid_s,
                                                        npos, vel, pos, iid, s.keys_sorted, s.cell_flags, s.flags);
   return cudaGetLastError();
 }
@@ -2005,7 +1996,6 @@ struct VortEta {
 __global__ void __launch_bounds__(128)
 k_vort_omega(StepConsts c, Geometry G, const float4* __restrict__ X, const float4* __restrict__ U,
              const uint32_t* __restrict__ cs, int n, float4* __restrict__ W) {
-  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = X[i];
@@ -2018,7 +2008,6 @@ k_vort_omega(StepConsts c, Geometry G, const float4* __restrict__ X, const float
 __global__ void __launch_bounds__(128)
 k_vort_force(StepConsts c, Geometry G, const float4* __restrict__ X, const float4* __restrict__ W,
              const uint32_t* __restrict__ cs, int n, float4* __restrict__ U) {
-  pdl_enter();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 xi = X[i];
@@ -2042,8 +2031,8 @@ k_vort_force(StepConsts c, Geometry G, const float4* __restrict__ X, const float
 cudaError_t launch_vorticity(const StepConsts& c, const Geometry& G, const float4* X, const uint32_t* cs, int n,
                              const SolverScratch& s, float4* NV, cudaStream_t stream) {
   const int blocks = (n + 127) / 128;
-  PBF_LAUNCH(k_vort_omega, blocks, 128, 0, stream, c, G, X, NV, cs, n, s.xb);
-  PBF_LAUNCH(k_vort_force, blocks, 128, 0, stream, c, G, X, s.xb, cs, n, NV);
+  k_vort_omega<<<blocks, 128, 0, stream>>>(c, G, X, NV, cs, n, s.xb);
+  k_vort_force<<<blocks, 128, 0, stream>>>(c, G, X, s.xb, cs, n, NV);
   return cudaGetLastError();
 }
 
