@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define PBF_ABI_VERSION 3
+#define PBF_ABI_VERSION 4
 
 /* Largest max_particles of a solver, and largest total of a batch: 2^27.
  * The solver's per-particle tables are indexed with 32-bit integers, the

@@ -1353,8 +1353,8 @@ namespace {
 // Candidate choices timed by pbf_autotune / pbf_batch_autotune.
 constexpr int kTuneWindows[] = {64, 128, 256, 512, 1024, 2048};
 constexpr int kTuneSplits[] = {1, 2, 4, 8};
-constexpr int kTuneQueueSparse[] = {1, 16};
-constexpr int kTuneQueueDense[] = {1, 8};
+constexpr int kTuneQueueSparse[] = {1, 10, 16};
+constexpr int kTuneQueueDense[] = {1, 4, 8};
 constexpr int kTuneStageSparse[] = {0, 1024, 2048};
 constexpr int kTuneStageDense[] = {0, 1536, 3072};
 
@@ -1491,8 +1491,8 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
     }
   };
   sweep(&TuneChoice::split, kTuneSplits, 4);
-  if (!best_ch.all) sweep(&TuneChoice::queue_sparse, kTuneQueueSparse, 2);
-  sweep(&TuneChoice::queue_dense, kTuneQueueDense, 2);
+  if (!best_ch.all) sweep(&TuneChoice::queue_sparse, kTuneQueueSparse, 3);
+  sweep(&TuneChoice::queue_dense, kTuneQueueDense, 3);
   if (!best_ch.all) sweep(&TuneChoice::stage_sparse, kTuneStageSparse, 3);
   sweep(&TuneChoice::stage_dense, kTuneStageDense, 3);
   for (void* q : {(void*)p[0], (void*)p[1], (void*)v[0], (void*)v[1], (void*)id})

@@ -300,7 +300,8 @@ enum ErrorBit : uint32_t {
 };
 
 // Largest stage (slots, 16 bytes each) a neighbour-pass block may ask for;
-// the pass kernels allow that much dynamic shared memory (set_pass_kernel_attributes).
+// the staged pass kernels allow that much dynamic shared memory beside their
+// hit queue (set_pass_kernel_attributes).
 constexpr int kStageMax = 4096;
 cudaError_t set_pass_kernel_attributes();
 
@@ -336,9 +337,6 @@ constexpr int kDefaultDenseWindow = 512;
 constexpr int kDenseAllBelow = 131072;
 // Slots a block of the sparse / dense pass kernel stages in shared memory
 // (defaults; 0: no staging; pbf_autotune can override, up to kStageMax).
-// Sparse: 16 KB of dynamic shared memory beside the 16 KB hit queue; dense:
-// 24 KB beside the queue and partial sums -- both under the 48 KB a launch
-// gets without the kernel attribute.
 constexpr int kDefaultStageSparse = 0;
 constexpr int kDefaultStageDense = 0;
 // Hit-queue capacities (chunks per thread; 1: the pair body right after each

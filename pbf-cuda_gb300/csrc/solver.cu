@@ -1005,10 +1005,14 @@ __device__ __forceinline__ void stage_init(StageState& st) {
 template <int kKind, bool kStage>
 __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   using P = typename PassOf<kKind>::type;
-  __shared__ uint32_t q_mask[kMaxQueueSparse * kSparseThreads];
-  __shared__ int q_base[kMaxQueueSparse * kSparseThreads];
   __shared__ StageState st;
-  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_sparse slots (kStage)
+  // dynamic shared memory: the hit queue (a.c.queue_sparse chunks per thread),
+  // then the stage (a.c.stage_sparse slots, kStage only); the queue is sized
+  // per launch so that a small queue leaves the SM's L1 its capacity
+  extern __shared__ __align__(16) float4 dyn_smem[];
+  uint32_t* q_mask = reinterpret_cast<uint32_t*>(dyn_smem);
+  int* q_base = reinterpret_cast<int*>(q_mask + a.c.queue_sparse * kSparseThreads);
+  float4* stage = dyn_smem + a.c.queue_sparse * kSparseThreads / 2;
   if (a.dense_all) return;
   const int count = work_count(a);
   if ((int)(blockIdx.x * kSparseThreads) >= count) return;  // uniform over the block
@@ -1075,10 +1079,13 @@ template <int kKind, bool kStage>
 __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   using P = typename PassOf<kKind>::type;
   __shared__ float part[kDenseWarps][kMaxFields][32];
-  __shared__ uint32_t q_mask[kMaxQueueDense * kDenseThreads];
-  __shared__ int q_base[kMaxQueueDense * kDenseThreads];
   __shared__ StageState st;
-  extern __shared__ __align__(16) float4 stage[];  // a.c.stage_dense slots (kStage)
+  // dynamic shared memory: the hit queue (a.c.queue_dense chunks per thread),
+  // then the stage (a.c.stage_dense slots, kStage only)
+  extern __shared__ __align__(16) float4 dyn_smem[];
+  uint32_t* q_mask = reinterpret_cast<uint32_t*>(dyn_smem);
+  int* q_base = reinterpret_cast<int*>(q_mask + a.c.queue_dense * kDenseThreads);
+  float4* stage = dyn_smem + a.c.queue_dense * kDenseThreads / 2;
   static_assert(P::kFields <= kMaxFields, "partial-sum fields");
   HitQueue hq(q_mask + threadIdx.x, q_base + threadIdx.x, kDenseThreads, a.c.queue_dense);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -1824,20 +1831,23 @@ void use_buckets(PassArgs& a, const SolverScratch& s) {
 
 template <int kKind>
 cudaError_t run_pass(const PassArgs& a, cudaStream_t stream) {
+  // dynamic shared memory: the hit queue (8 bytes per chunk and thread), then the stage
+  const size_t sparse_queue = (size_t)8 * a.c.queue_sparse * kSparseThreads;
+  const size_t dense_queue = (size_t)8 * a.c.queue_dense * kDenseThreads;
   const size_t sparse_smem = sizeof(float4) * (size_t)max(a.c.stage_sparse, 0);
   const size_t dense_smem = sizeof(float4) * (size_t)max(a.c.stage_dense, 0);
   const int sparse_blocks = (a.n + kSparseThreads - 1) / kSparseThreads;
   if (a.dense_all) {
     // else the sparse kernel has nothing to do
   } else if (sparse_smem) {
-    k_sparse<kKind, true><<<sparse_blocks, kSparseThreads, sparse_smem, stream>>>(a);
+    k_sparse<kKind, true><<<sparse_blocks, kSparseThreads, sparse_queue + sparse_smem, stream>>>(a);
   } else {
-    k_sparse<kKind, false><<<sparse_blocks, kSparseThreads, 0, stream>>>(a);
+    k_sparse<kKind, false><<<sparse_blocks, kSparseThreads, sparse_queue, stream>>>(a);
   }
   if (dense_smem)
-    k_dense<kKind, true><<<a.c.dense_grid, kDenseThreads, dense_smem, stream>>>(a);
+    k_dense<kKind, true><<<a.c.dense_grid, kDenseThreads, dense_queue + dense_smem, stream>>>(a);
   else
-    k_dense<kKind, false><<<a.c.dense_grid, kDenseThreads, 0, stream>>>(a);
+    k_dense<kKind, false><<<a.c.dense_grid, kDenseThreads, dense_queue, stream>>>(a);
   return cudaGetLastError();
 }
 
@@ -1851,10 +1861,12 @@ cudaError_t allow_stage(int bytes) {
 
 }  // namespace
 
-// Lets the pass kernels take up to kStageMax staged slots of dynamic shared
-// memory (the current device; call before any capture).
+// Lets the staged pass kernels take their largest hit queue and up to
+// kStageMax staged slots of dynamic shared memory (the current device; call
+// before any capture).
 cudaError_t set_pass_kernel_attributes() {
-  const int bytes = (int)sizeof(float4) * kStageMax;
+  const int queue = 8 * max(kMaxQueueSparse * kSparseThreads, kMaxQueueDense * kDenseThreads);
+  const int bytes = (int)sizeof(float4) * kStageMax + queue;
   cudaError_t e = allow_stage<kLambda>(bytes);
   if (e == cudaSuccess) e = allow_stage<kDeltaP>(bytes);
   if (e == cudaSuccess) e = allow_stage<kDeltaPFinal>(bytes);

@@ -121,7 +121,7 @@ def test_argument_errors_need_no_gpu(pbf):
     t = pbf.PbfTuning()
     assert L.pbf_set_tuning(None, ctypes.byref(t)) == pbf.PBF_ERR_INVALID_ARG
     assert L.pbf_get_tuning(None, ctypes.byref(t)) == pbf.PBF_ERR_INVALID_ARG
-    assert L.pbf_abi_version() == 3
+    assert L.pbf_abi_version() == 4
     assert L.pbf_status_string(pbf.PBF_ERR_CAPACITY) == b"capacity exceeded"
     with pytest.raises(pbf.PbfError) as e:
         pbf.check(pbf.PBF_ERR_TIMEOUT, "x")
