@@ -281,7 +281,7 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   for (int a = 0; a < 3; ++a) c.g[a] = -p.g * p.up[a];
   c.geom = make_geom(p, ulim, llim, dims, 0);
   c.cells = dims[0] * dims[1] * dims[2];
-  c.dense_grid = 4 * (num_sms > 0 ? num_sms : 1);
+  c.dense_grid = pbf::kDenseBlocksPerSm * (num_sms > 0 ? num_sms : 1);
   c.dense_window = pbf::kDefaultDenseWindow;
   c.dense_all = -1;
   c.order = 1;

@@ -334,6 +334,11 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
 // Candidates above which a warp takes the dense kernel, and the particle
 // count below which every warp does (defaults; pbf_autotune can override).
 constexpr int kDefaultDenseWindow = 512;
+// Blocks of the dense kernel per SM (its grid is this many times the SM count).
+#ifndef PBF_DENSE_BLOCKS_PER_SM
+#define PBF_DENSE_BLOCKS_PER_SM 4
+#endif
+constexpr int kDenseBlocksPerSm = PBF_DENSE_BLOCKS_PER_SM;
 constexpr int kDenseAllBelow = 131072;
 // Slots a block of the sparse / dense pass kernel stages in shared memory
 // (defaults; 0: no staging; pbf_autotune can override, up to kStageMax).

@@ -287,6 +287,16 @@ struct HitQueue {
   }
   template <class P, class Src>
   __device__ __forceinline__ void push(uint32_t m, int tag, const Src& src, P& p) {
+    if (cap == 1) {  // no queue: the chunk's hits right away, straight from registers
+      while (m) {
+        const int bit = __ffs(m) - 1;
+        m &= m - 1u;
+        int j;
+        const float4 xj = src.untag(tag, bit, j);
+        p.visit(xj, j);
+      }
+      return;
+    }
     if (!m) return;
     mask[n * stride] = m;
     base[n * stride] = tag;
@@ -1073,10 +1083,15 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
   if (kStage && cap > 0) stage_drain(st, phase);
 }
 
+// PBF_DENSE_BLOCKS_PER_SM (a build-time tuning macro, pbf_internal.cuh): the
+// dense kernel's resident blocks per SM, which its grid is sized for and its
+// registers are capped to.
+#define PBF_DENSE_BOUNDS __launch_bounds__(kDenseThreads, PBF_DENSE_BLOCKS_PER_SM)
+
 // kStage: the variant that stages each item's column runs (launched when
 // stage_dense > 0); the other carries no staging code.
 template <int kKind, bool kStage>
-__global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
+__global__ void PBF_DENSE_BOUNDS k_dense(PassArgs a) {
   using P = typename PassOf<kKind>::type;
   __shared__ float part[kDenseWarps][kMaxFields][32];
   __shared__ StageState st;
@@ -1099,9 +1114,10 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
   // kSplit warps share an item (each walks one contiguous part of every
   // lane's window); the block runs kDenseWarps / kSplit items at a time.  The
   // staged variant gives each item the whole block.
-  const int split = kStage ? kDenseWarps : a.c.dense_split;
-  const int slots = kDenseWarps / split;
-  const int slot = warp / split, sub = warp % split;
+  const int split = kStage ? kDenseWarps : a.c.dense_split;  // 1, 2, 4 or 8
+  const int split_log2 = 31 - __clz(split);
+  const int slots = kDenseWarps >> split_log2;
+  const int slot = warp >> split_log2, sub = warp & (split - 1);
   // no grouped cell this step: windows are walked as 9 column runs (the same
   // candidates in the same order as cell by cell, with fewer table reads)
   const bool groups = a.c.keps2 > 0.f && a.flags[kGroupCount] != 0u;
@@ -1130,8 +1146,8 @@ __global__ void __launch_bounds__(kDenseThreads) k_dense(PassArgs a) {
     }
     if (valid) {
       const int total = groups ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
-      const int lo = (int)((long long)total * sub / split);
-      const int hi = (int)((long long)total * (sub + 1) / split);
+      const int lo = (int)(((long long)total * sub) >> split_log2);
+      const int hi = (int)(((long long)total * (sub + 1)) >> split_log2);
       P p(a, g, xi, i, exact);
       // a staged window holds no grouped cell: its runs are walked as runs
       if (kStage && staged)
