@@ -412,7 +412,7 @@ def tune(sim, st, n, args):
         return {**sim.tuning(), "set": "--dense-window / --order"}
     if not args.tune:
         return None
-    t = sim.autotune(st.pos, st.vel, st.iid, n, steps=3)
+    t = sim.autotune(st.pos, st.vel, st.iid, n, steps=6)
     keys = ("dense_window", "dense_all", "order", "dense_split", "queue_sparse", "queue_dense", "stage_sparse",
             "stage_dense")
     return {**{k: int(t[k]) for k in keys}, "trial_ms_per_step": round(float(t["ms_per_step"]), 4),

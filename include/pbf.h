@@ -295,7 +295,7 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
  * default: every particle dense below 131072 particles); order 1, 0 or -1
  * (the default, 1); bwd_lanes 0 (the default), 8, 16 or 32; stage_sparse and
  * stage_dense 0 (off) to 4096 slots, or -1 (the default); queue_sparse 1-16,
- * queue_dense 1-8 and dense_split 1, 2, 4 or 8, or 0 (the defaults: 16, 8,
+ * queue_dense 1-8 and dense_split 1, 2, 4 or 8, or 0 (the defaults: 1, 1,
  * 8).  ms fields are ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);

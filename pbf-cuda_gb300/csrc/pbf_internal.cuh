@@ -288,7 +288,9 @@ enum StepFlag {
   kWorkDone = 8,             // blocks of the work-list count finished (0 between uses)
   kWorkIdentity = 9,         // 1: no grouped cell this step, the passes take every particle in order
   kBucketCount = 10,         // particles in the current buckets
-  kNumFlags = 11
+  kItemCount0 = 11,          // dense-kernel batches handed out, by pass parity (work queue)
+  kItemCount1 = 12,
+  kNumFlags = 13
 };
 
 // One more word after the step flags, cleared only when the host reads it:
@@ -349,8 +351,8 @@ constexpr int kDefaultStageDense = 0;
 // override, queues up to kMaxQueue* chunks).
 constexpr int kMaxQueueSparse = 16;
 constexpr int kMaxQueueDense = 8;
-constexpr int kDefaultQueueSparse = 16;
-constexpr int kDefaultQueueDense = 8;
+constexpr int kDefaultQueueSparse = 1;
+constexpr int kDefaultQueueDense = 1;
 constexpr int kDefaultDenseSplit = 8;
 
 // Vorticity confinement after XSPH, on its output NV (positions X = npos):

@@ -82,6 +82,8 @@ struct PassArgs {
   int n;
   int counter;            // flags word holding this pass's dense-list length
   int next_counter;       // the other one, cleared for the next pass
+  int item_counter;       // flags word handing out this pass's dense batches
+  int next_item_counter;  // the other one, cleared for the next pass
   int dense_all;          // every warp takes the dense kernel (small n)
   uint32_t* flags;
   uint32_t* dense;
@@ -1106,7 +1108,10 @@ __global__ void PBF_DENSE_BOUNDS k_dense(PassArgs a) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cap = kStage ? a.c.stage_dense : 0;
   if (kStage && threadIdx.x == 0 && cap > 0) stage_init(st);
-  if (blockIdx.x == 0 && threadIdx.x == 0) a.flags[a.next_counter] = 0u;  // its pass has finished
+  if (blockIdx.x == 0 && threadIdx.x == 0) {  // their pass has finished
+    a.flags[a.next_counter] = 0u;
+    a.flags[a.next_item_counter] = 0u;
+  }
   // the slots the sparse kernel listed, or all of them, 32 per item
   const int work = work_count(a);
   const uint32_t listed = a.dense_all ? (uint32_t)work : a.flags[a.counter];
@@ -1121,11 +1126,17 @@ __global__ void PBF_DENSE_BOUNDS k_dense(PassArgs a) {
   // no grouped cell this step: windows are walked as 9 column runs (the same
   // candidates in the same order as cell by cell, with fewer table reads)
   const bool groups = a.c.keps2 > 0.f && a.flags[kGroupCount] != 0u;
-  const uint32_t per_round = gridDim.x * (uint32_t)slots;
-  const uint32_t rounds = (count + per_round - 1) / per_round;
+  // batches are handed out one block-load at a time by a counter, so a block
+  // that drew light batches takes more (batches cost from a few hundred to
+  // many thousand candidates); which block computes a batch changes nothing
+  __shared__ uint32_t s_first;
   uint32_t phase = 0u;
-  for (uint32_t rd = 0; rd < rounds; ++rd) {  // the same count for every warp of the block
-    const uint32_t item = (rd * gridDim.x + blockIdx.x) * (uint32_t)slots + (uint32_t)slot;
+  for (;;) {
+    if (threadIdx.x == 0) s_first = atomicAdd(&a.flags[a.item_counter], (uint32_t)slots);
+    __syncthreads();  // also: every thread has read the previous s_first
+    const uint32_t first = s_first;
+    if (first >= count) break;  // uniform over the block
+    const uint32_t item = first + (uint32_t)slot;
     const uint32_t e = item * 32 + lane;
     const bool valid = item < count && e < listed;
     const int t = valid ? (int)(a.dense_all ? e : a.dense[e]) : 0;
@@ -1804,6 +1815,8 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.dense_all = c.dense_all >= 0 ? c.dense_all : n < kDenseAllBelow;
   a.counter = kDenseCount0 + (pass & 1);
   a.next_counter = kDenseCount0 + ((pass + 1) & 1);
+  a.item_counter = kItemCount0 + (pass & 1);
+  a.next_item_counter = kItemCount0 + ((pass + 1) & 1);
   a.flags = s.flags;
   a.dense = s.dense;
   a.masks = s.masks;

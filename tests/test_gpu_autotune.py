@@ -11,7 +11,7 @@ from test_gpu_parity import TOL_X, ref_params
 pytestmark = pytest.mark.gpu
 
 # the library's defaults of the tuning fields beyond window, dense-for-all, order and lanes
-STAGE_DEFAULT = {"stage_sparse": 0, "stage_dense": 0, "queue_sparse": 16, "queue_dense": 8, "dense_split": 8}
+STAGE_DEFAULT = {"stage_sparse": 0, "stage_dense": 0, "queue_sparse": 1, "queue_dense": 1, "dense_split": 8}
 
 
 def test_autotune_single(pbf, oracle, cuda):

@@ -26,7 +26,7 @@ pytestmark = pytest.mark.gpu
 
 OFF = {"stage_sparse": 0, "stage_dense": 0}
 CHOICES = [{"stage_sparse": 1024, "stage_dense": 0}, {"stage_sparse": 0, "stage_dense": 1536},
-           {"stage_sparse": 2048, "stage_dense": 4096}, {"queue_sparse": 1, "queue_dense": 1},
+           {"stage_sparse": 2048, "stage_dense": 4096}, {"queue_sparse": 16, "queue_dense": 8},
            {"queue_sparse": 4, "queue_dense": 2}]
 
 
