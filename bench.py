@@ -413,8 +413,8 @@ def tune(sim, st, n, args):
     if not args.tune:
         return None
     t = sim.autotune(st.pos, st.vel, st.iid, n, steps=6)
-    keys = ("dense_window", "dense_all", "order", "dense_split", "queue_sparse", "queue_dense", "stage_sparse",
-            "stage_dense")
+    keys = ("dense_window", "dense_all", "order", "dense_split", "dense_interleave", "queue_sparse", "queue_dense",
+            "stage_sparse", "stage_dense")
     return {**{k: int(t[k]) for k in keys}, "trial_ms_per_step": round(float(t["ms_per_step"]), 4),
             "trial_ms_per_step_default": round(float(t["ms_default"]), 4)}
 

@@ -283,6 +283,8 @@ typedef struct pbf_tuning {
   int dense_split;    /* warps of the dense kernel that split one batch of 32 particles'
                          windows: 1, 2, 4 or 8 (a block of 8 warps takes 8 / dense_split
                          batches at a time) */
+  int dense_interleave; /* 1: those warps take every dense_split-th chunk of 32 candidates of a
+                           window; 0: one contiguous part each (-1: the default, 0) */
 } pbf_tuning;
 
 pbf_status pbf_autotune(pbf_solver* s, const void* pos, const void* vel, const uint32_t* iid, int n, int steps,
@@ -296,7 +298,7 @@ pbf_status pbf_batch_autotune(pbf_batch* b, const void* pos, const void* vel, co
  * (the default, 1); bwd_lanes 0 (the default), 8, 16 or 32; stage_sparse and
  * stage_dense 0 (off) to 4096 slots, or -1 (the default); queue_sparse 1-16,
  * queue_dense 1-8 and dense_split 1, 2, 4 or 8, or 0 (the defaults: 1, 1,
- * 8).  ms fields are ignored on set and 0 on get. */
+ * 8); dense_interleave 0, 1 or -1 (the default, 0).  ms fields are ignored on set and 0 on get. */
 pbf_status pbf_set_tuning(pbf_solver* s, const pbf_tuning* t);
 pbf_status pbf_get_tuning(const pbf_solver* s, pbf_tuning* t);
 /* The same for a batch (bwd_lanes is ignored: a batch has no reverse pass). */

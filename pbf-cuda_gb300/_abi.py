@@ -141,7 +141,8 @@ class PbfTuning(ctypes.Structure):
     _fields_ = [("dense_window", ctypes.c_int), ("dense_all", ctypes.c_int),
                 ("ms_per_step", ctypes.c_float), ("ms_default", ctypes.c_float), ("order", ctypes.c_int),
                 ("bwd_lanes", ctypes.c_int), ("stage_sparse", ctypes.c_int), ("stage_dense", ctypes.c_int),
-                ("queue_sparse", ctypes.c_int), ("queue_dense", ctypes.c_int), ("dense_split", ctypes.c_int)]
+                ("queue_sparse", ctypes.c_int), ("queue_dense", ctypes.c_int), ("dense_split", ctypes.c_int),
+                ("dense_interleave", ctypes.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -126,6 +126,7 @@ struct pbf_solver {
   int tune_queue_sparse;  // hit-queue chunks per sparse / dense thread; 0: the defaults
   int tune_queue_dense;
   int tune_split;         // dense warps per item; 0: the default
+  int tune_interleave;    // dense warps take interleaved chunks; -1: the default
 };
 
 namespace {
@@ -290,6 +291,7 @@ pbf::StepConsts make_consts(const pbf_params& p, const float ulim[3], const floa
   c.queue_sparse = pbf::kDefaultQueueSparse;
   c.queue_dense = pbf::kDefaultQueueDense;
   c.dense_split = pbf::kDefaultDenseSplit;
+  c.dense_interleave = pbf::kDefaultDenseInterleave;
   return c;
 }
 
@@ -491,6 +493,7 @@ pbf_status pbf_create(const pbf_params* params, const float ulim[3], const float
   s->tune_order = -1;
   s->tune_stage_sparse = -1;
   s->tune_stage_dense = -1;
+  s->tune_interleave = -1;
   s->params = *params;
   std::memcpy(s->ulim, ulim, sizeof(s->ulim));
   std::memcpy(s->llim, llim, sizeof(s->llim));
@@ -788,6 +791,7 @@ pbf_status pbf_step(pbf_solver* s, void* pos, void* npos, void* vel, void* nvel,
   if (s->tune_queue_sparse > 0) P.c.queue_sparse = s->tune_queue_sparse;
   if (s->tune_queue_dense > 0) P.c.queue_dense = s->tune_queue_dense;
   if (s->tune_split > 0) P.c.dense_split = s->tune_split;
+  if (s->tune_interleave >= 0) P.c.dense_interleave = s->tune_interleave;
   P.G = pbf::Geometry{nullptr, nullptr};
   P.grid = &s->grid;
   P.sol = &s->sol;
@@ -1075,6 +1079,7 @@ struct pbf_batch {
   int tune_queue_sparse = 0;
   int tune_queue_dense = 0;
   int tune_split = 0;
+  int tune_interleave = -1;
 };
 
 namespace {
@@ -1265,6 +1270,7 @@ pbf_status pbf_batch_step(pbf_batch* b, void* pos, void* npos, void* vel, void* 
   if (b->tune_queue_sparse > 0) P.c.queue_sparse = b->tune_queue_sparse;
   if (b->tune_queue_dense > 0) P.c.queue_dense = b->tune_queue_dense;
   if (b->tune_split > 0) P.c.dense_split = b->tune_split;
+  if (b->tune_interleave >= 0) P.c.dense_interleave = b->tune_interleave;
   P.G = pbf::Geometry{b->d_geom, b->d_sid};
   P.grid = &b->grid;
   P.sol = &b->sol;
@@ -1353,6 +1359,7 @@ namespace {
 // Candidate choices timed by pbf_autotune / pbf_batch_autotune.
 constexpr int kTuneWindows[] = {64, 128, 256, 512, 1024, 2048};
 constexpr int kTuneSplits[] = {1, 2, 4, 8};
+constexpr int kTuneInterleave[] = {0, 1};
 constexpr int kTuneQueueSparse[] = {1, 10, 16};
 constexpr int kTuneQueueDense[] = {1, 4, 8};
 constexpr int kTuneStageSparse[] = {0, 1024, 2048};
@@ -1361,30 +1368,31 @@ constexpr int kTuneStageDense[] = {0, 1536, 3072};
 // One configuration of the neighbour passes (the fields of pbf_tuning that
 // pbf_autotune times).
 struct TuneChoice {
-  int window, all, order, split, queue_sparse, queue_dense, stage_sparse, stage_dense;
+  int window, all, order, split, queue_sparse, queue_dense, stage_sparse, stage_dense, interleave;
   bool operator==(const TuneChoice& o) const {
     return window == o.window && all == o.all && order == o.order && split == o.split &&
            queue_sparse == o.queue_sparse && queue_dense == o.queue_dense && stage_sparse == o.stage_sparse &&
-           stage_dense == o.stage_dense;
+           stage_dense == o.stage_dense && interleave == o.interleave;
   }
 };
 
 TuneChoice default_choice(int n) {
   return TuneChoice{pbf::kDefaultDenseWindow, n < pbf::kDenseAllBelow ? 1 : 0, 1, pbf::kDefaultDenseSplit,
                     pbf::kDefaultQueueSparse, pbf::kDefaultQueueDense, pbf::kDefaultStageSparse,
-                    pbf::kDefaultStageDense};
+                    pbf::kDefaultStageDense, pbf::kDefaultDenseInterleave};
 }
 
 // The tuning fields a solver or batch keeps (0 / -1: the defaults).
 struct TuneState {
   int window = 0, all = -1, order = -1, split = 0, queue_sparse = 0, queue_dense = 0, stage_sparse = -1,
-      stage_dense = -1;
+      stage_dense = -1, interleave = -1;
 };
 
 template <class T>
 TuneState tune_state(const T* h) {
-  return TuneState{h->tune_window,  h->tune_all,          h->tune_order,        h->tune_split,
-                   h->tune_queue_sparse, h->tune_queue_dense, h->tune_stage_sparse, h->tune_stage_dense};
+  return TuneState{h->tune_window,       h->tune_all,         h->tune_order,
+                   h->tune_split,        h->tune_queue_sparse, h->tune_queue_dense,
+                   h->tune_stage_sparse, h->tune_stage_dense,  h->tune_interleave};
 }
 
 template <class T>
@@ -1397,11 +1405,12 @@ void set_tune_state(T* h, const TuneState& t) {
   h->tune_queue_dense = t.queue_dense;
   h->tune_stage_sparse = t.stage_sparse;
   h->tune_stage_dense = t.stage_dense;
+  h->tune_interleave = t.interleave;
 }
 
 TuneState state_of(const TuneChoice& c) {
-  return TuneState{c.window, c.all, c.order, c.split, c.queue_sparse, c.queue_dense, c.stage_sparse,
-                   c.stage_dense};
+  return TuneState{c.window,       c.all,          c.order,        c.split,     c.queue_sparse,
+                   c.queue_dense,  c.stage_sparse, c.stage_dense,  c.interleave};
 }
 
 // pbf_tuning fields of a tune state (defaults resolved).
@@ -1414,6 +1423,7 @@ void fill_tuning(const TuneState& t, pbf_tuning* out) {
   out->queue_dense = t.queue_dense > 0 ? t.queue_dense : pbf::kDefaultQueueDense;
   out->stage_sparse = t.stage_sparse >= 0 ? t.stage_sparse : pbf::kDefaultStageSparse;
   out->stage_dense = t.stage_dense >= 0 ? t.stage_dense : pbf::kDefaultStageDense;
+  out->dense_interleave = t.interleave >= 0 ? t.interleave : pbf::kDefaultDenseInterleave;
 }
 
 // Runs `steps` steps per candidate on copies of (pos, vel, iid) through
@@ -1491,6 +1501,7 @@ pbf_status autotune(int n, const void* pos, const void* vel, const uint32_t* iid
     }
   };
   sweep(&TuneChoice::split, kTuneSplits, 4);
+  if (best_ch.split > 1) sweep(&TuneChoice::interleave, kTuneInterleave, 2);
   if (!best_ch.all) sweep(&TuneChoice::queue_sparse, kTuneQueueSparse, 3);
   sweep(&TuneChoice::queue_dense, kTuneQueueDense, 3);
   if (!best_ch.all) sweep(&TuneChoice::stage_sparse, kTuneStageSparse, 3);
@@ -1529,12 +1540,14 @@ pbf_status check_tuning(const pbf_tuning* t) {
   if (t->dense_split != 0 && t->dense_split != 1 && t->dense_split != 2 && t->dense_split != 4 &&
       t->dense_split != 8)
     return fail(PBF_ERR_INVALID_ARG, "dense_split must be 0, 1, 2, 4 or 8 (got %d)", t->dense_split);
+  if (t->dense_interleave < -1 || t->dense_interleave > 1)
+    return fail(PBF_ERR_INVALID_ARG, "dense_interleave must be -1, 0 or 1 (got %d)", t->dense_interleave);
   return PBF_OK;
 }
 
 TuneState state_of(const pbf_tuning* t) {
-  return TuneState{t->dense_window, t->dense_all,   t->order,        t->dense_split,
-                   t->queue_sparse, t->queue_dense, t->stage_sparse, t->stage_dense};
+  return TuneState{t->dense_window, t->dense_all,    t->order,        t->dense_split,     t->queue_sparse,
+                   t->queue_dense,  t->stage_sparse, t->stage_dense,  t->dense_interleave};
 }
 
 }  // namespace

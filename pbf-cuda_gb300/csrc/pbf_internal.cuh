@@ -63,6 +63,7 @@ struct StepConsts {
   int queue_sparse;        // hit-queue chunks per thread of the sparse / dense kernel (1: none)
   int queue_dense;
   int dense_split;         // warps of the dense kernel sharing one item's windows: 1, 2, 4 or 8
+  int dense_interleave;    // 1: those warps take every dense_split-th chunk; 0: contiguous parts
   SceneGeom geom;          // the box of a single-scene step
 };
 
@@ -354,6 +355,7 @@ constexpr int kMaxQueueDense = 8;
 constexpr int kDefaultQueueSparse = 1;
 constexpr int kDefaultQueueDense = 1;
 constexpr int kDefaultDenseSplit = 8;
+constexpr int kDefaultDenseInterleave = 0;
 
 // Vorticity confinement after XSPH, on its output NV (positions X = npos):
 // omega_i = sum_j (u_j - u_i) x g_ij and eta_i = sum_j |omega_j| g_ij over

@@ -387,13 +387,17 @@ __device__ __forceinline__ void visit_window_masked(const SceneGeom& g,
 // positions saved (visit_window_masked with save): p.visit() on the set bits,
 // in order, through the hit queue.  The saved hits are a superset of p's
 // (p.visit re-tests).
+// chunks: the window's chunk count (at most kMaskWords); each chunk's mask is
+// loaded two chunks ahead of its use, so its latency overlaps the pair work.
 template <class P, class Src>
 __device__ __forceinline__ void visit_window_saved(const SceneGeom& g,
                                                    const uint32_t* __restrict__ cs, int n, int3 q,
                                                    const Src& src, P& p,
                                                    const uint32_t* __restrict__ masks, int stride,
-                                                   int i, HitQueue& hq) {
+                                                   int i, int chunks, HitQueue& hq) {
   int chunk = 0;
+  uint32_t m0 = chunks > 0 ? __ldg(masks + i) : 0u;
+  uint32_t m1 = chunks > 1 ? __ldg(masks + stride + i) : 0u;
   for (int dx = -1; dx <= 1; ++dx) {
     const int x = q.x + dx;
     if (x < 0 || x >= g.dims[0]) continue;
@@ -403,8 +407,12 @@ __device__ __forceinline__ void visit_window_saved(const SceneGeom& g,
       const int r = 3 * (dx + 1) + (dy + 1);
       int s, e;
       column_run(g, cs, n, x, y, q.z, s, e);
-      for (int j0 = s; j0 < e; j0 += 32, ++chunk)
-        hq.push(__ldg(masks + chunk * stride + i), src.tag(j0, r), src, p);
+      for (int j0 = s; j0 < e; j0 += 32, ++chunk) {
+        const uint32_t m = m0;
+        m0 = m1;
+        m1 = chunk + 2 < chunks ? __ldg(masks + (chunk + 2) * stride + i) : 0u;
+        hq.push(m, src.tag(j0, r), src, p);
+      }
     }
   }
   hq.flush(src, p);
@@ -430,6 +438,37 @@ __device__ __forceinline__ void visit_window_chunk(const SceneGeom& g, const uin
       const int a = max(v_lo, v0), b = min(v_hi, v0 + len);
       if (a < b) visit_run(src, s + (a - v0), s + (b - v0), r, p, p.skip_misses(), hq);
       v0 += len;
+    }
+  }
+  hq.flush(src, p);
+}
+
+// Part `part` of `parts` (a power of two) of the window, interleaved: the
+// window's chunks of up to 32 consecutive candidates (per run, in visiting
+// order) are numbered 0, 1, 2, ..., and chunk c belongs to part c mod parts.
+// Parts of a window then hold about equal shares of its near and far
+// candidates, so the warps that split a window finish together.  The caller
+// flushes nothing: hq is flushed here.
+template <class P, class Src>
+__device__ __forceinline__ void visit_window_strided(const SceneGeom& g, const uint32_t* __restrict__ cs, int n,
+                                                     int3 q, const Src& src, P& p, int part, int parts,
+                                                     HitQueue& hq) {
+  int c0 = 0;  // chunks of the window before this run
+  for (int dx = -1; dx <= 1; ++dx) {
+    const int x = q.x + dx;
+    if (x < 0 || x >= g.dims[0]) continue;
+    for (int dy = -1; dy <= 1; ++dy) {
+      const int y = q.y + dy;
+      if (y < 0 || y >= g.dims[1]) continue;
+      const int r = 3 * (dx + 1) + (dy + 1);
+      int s, e;
+      column_run(g, cs, n, x, y, q.z, s, e);
+      const int nch = (e - s + 31) >> 5;
+      for (int k = (part - c0) & (parts - 1); k < nch; k += parts) {
+        const int jb = s + 32 * k;
+        visit_run(src, jb, min(jb + 32, e), r, p, p.skip_misses(), hq);
+      }
+      c0 += nch;
     }
   }
   hq.flush(src, p);
@@ -988,7 +1027,7 @@ __device__ __forceinline__ void sparse_visit(const PassArgs& a, const SceneGeom&
   } else if (kKind == kLambda) {
     visit_window_masked(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // saves its masks
   } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) && chunks <= kMaskWords) {
-    visit_window_saved(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // lambda's masks
+    visit_window_saved(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, chunks, hq);  // lambda's masks
   } else {
     visit_window_masked(g, a.cs, a.n, q, src, p, nullptr, 0, i, hq);
   }
@@ -1160,13 +1199,21 @@ __global__ void PBF_DENSE_BOUNDS k_dense(PassArgs a) {
       const int lo = (int)(((long long)total * sub) >> split_log2);
       const int hi = (int)(((long long)total * (sub + 1)) >> split_log2);
       P p(a, g, xi, i, exact);
-      // a staged window holds no grouped cell: its runs are walked as runs
-      if (kStage && staged)
-        visit_window_chunk(g, a.cs, a.n, q, FromStage{stage, st.D}, p, lo, hi, hq);
-      else if (groups)
+      // a staged window holds no grouped cell: its runs are walked as runs;
+      // dense_interleave: the warps take every split-th chunk instead of
+      // one contiguous part (windows without grouped cells)
+      if (kStage && staged) {
+        if (a.c.dense_interleave)
+          visit_window_strided(g, a.cs, a.n, q, FromStage{stage, st.D}, p, sub, split, hq);
+        else
+          visit_window_chunk(g, a.cs, a.n, q, FromStage{stage, st.D}, p, lo, hi, hq);
+      } else if (groups) {
         visit_window_grouped(g, a, q, FromGlobal{a.X}, p, lo, hi, hq);
-      else
+      } else if (a.c.dense_interleave) {
+        visit_window_strided(g, a.cs, a.n, q, FromGlobal{a.X}, p, sub, split, hq);
+      } else {
         visit_window_chunk(g, a.cs, a.n, q, FromGlobal{a.X}, p, lo, hi, hq);
+      }
       p.store(&part[warp][0][lane], 32);
     }
     __syncthreads();

@@ -43,17 +43,19 @@ def _check_state(t: torch.Tensor, name: str, n: int, cols: Optional[int]) -> Non
 
 
 def _tuning(dense_window, dense_all, order, bwd_lanes, stage_sparse, stage_dense, queue_sparse, queue_dense,
-            dense_split) -> PbfTuning:
+            dense_split, dense_interleave) -> PbfTuning:
     t = PbfTuning()
     t.dense_window, t.dense_all, t.order, t.bwd_lanes = int(dense_window), int(dense_all), int(order), int(bwd_lanes)
     t.stage_sparse, t.stage_dense = int(stage_sparse), int(stage_dense)
     t.queue_sparse, t.queue_dense, t.dense_split = int(queue_sparse), int(queue_dense), int(dense_split)
+    t.dense_interleave = int(dense_interleave)
     return t
 
 
 def _tuning_dict(t: PbfTuning) -> dict:
     return {k: getattr(t, k) for k in ("dense_window", "dense_all", "order", "bwd_lanes", "stage_sparse",
-                                       "stage_dense", "queue_sparse", "queue_dense", "dense_split")}
+                                       "stage_dense", "queue_sparse", "queue_dense", "dense_split",
+                                       "dense_interleave")}
 
 
 class Simulator:
@@ -169,14 +171,14 @@ class Simulator:
 
     def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, bwd_lanes: int = 0,
                    stage_sparse: int = -1, stage_dense: int = -1, queue_sparse: int = 0, queue_dense: int = 0,
-                   dense_split: int = 0) -> None:
+                   dense_split: int = 0, dense_interleave: int = -1) -> None:
         """The neighbour passes' choices for the following steps (dense window,
         dense-for-all, particle order, shared-memory stages, hit queues, dense
         split) and the reverse pass's lanes per particle (pbf_set_tuning); 0 /
         -1: the defaults (stage_*: 0 turns staging off)."""
         check(self._L.pbf_set_tuning(self._h, ctypes.byref(_tuning(
             dense_window, dense_all, order, bwd_lanes, stage_sparse, stage_dense, queue_sparse, queue_dense,
-            dense_split))), "pbf_set_tuning")
+            dense_split, dense_interleave))), "pbf_set_tuning")
 
     def tuning(self) -> dict:
         t = PbfTuning()
@@ -311,11 +313,12 @@ class Ensemble:
         check(self._L.pbf_batch_set_limits(self._h, int(scene), _vec3(ulim), _vec3(llim)), "pbf_batch_set_limits")
 
     def set_tuning(self, dense_window: int = 0, dense_all: int = -1, order: int = -1, stage_sparse: int = -1,
-                   stage_dense: int = -1, queue_sparse: int = 0, queue_dense: int = 0, dense_split: int = 0) -> None:
+                   stage_dense: int = -1, queue_sparse: int = 0, queue_dense: int = 0, dense_split: int = 0,
+                   dense_interleave: int = -1) -> None:
         """The neighbour passes' choices for the following steps (pbf_batch_set_tuning)."""
         check(self._L.pbf_batch_set_tuning(self._h, ctypes.byref(_tuning(
             dense_window, dense_all, order, 0, stage_sparse, stage_dense, queue_sparse, queue_dense,
-            dense_split))), "pbf_batch_set_tuning")
+            dense_split, dense_interleave))), "pbf_batch_set_tuning")
 
     def tuning(self) -> dict:
         t = PbfTuning()

@@ -11,7 +11,8 @@ from test_gpu_parity import TOL_X, ref_params
 pytestmark = pytest.mark.gpu
 
 # the library's defaults of the tuning fields beyond window, dense-for-all, order and lanes
-STAGE_DEFAULT = {"stage_sparse": 0, "stage_dense": 0, "queue_sparse": 1, "queue_dense": 1, "dense_split": 8}
+STAGE_DEFAULT = {"stage_sparse": 0, "stage_dense": 0, "queue_sparse": 1, "queue_dense": 1, "dense_split": 8,
+                 "dense_interleave": 0}
 
 
 def test_autotune_single(pbf, oracle, cuda):
@@ -87,7 +88,8 @@ def test_set_tuning_round_trip(pbf, oracle, cuda):
         assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32, **STAGE_DEFAULT}
         for bad in ((16, 0), (256, 2), (256, -2), (0, -1, 2), (0, -1, -2), (0, -1, 1, 4), (0, -1, 1, 0, 4097),
                     (0, -1, 1, 0, -2), (0, -1, 1, 0, 0, 4097), (0, -1, 1, 0, -1, -1, 17),
-                    (0, -1, 1, 0, -1, -1, 0, 9), (0, -1, 1, 0, -1, -1, 0, 0, 3)):
+                    (0, -1, 1, 0, -1, -1, 0, 9), (0, -1, 1, 0, -1, -1, 0, 0, 3),
+                    (0, -1, 1, 0, -1, -1, 0, 0, 0, 2)):
             with pytest.raises(pbf.PbfError):
                 sim.set_tuning(*bad)
         assert sim.tuning() == {"dense_window": 128, "dense_all": 0, "order": 0, "bwd_lanes": 32, **STAGE_DEFAULT}

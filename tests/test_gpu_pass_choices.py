@@ -112,8 +112,8 @@ def test_staged_step_matches_fp64(pbf, oracle, cuda):
     assert np.abs(npos.cpu().numpy()[:, :3] - r["npos"][:, :3]).max() <= TOL_X
 
 
-@pytest.mark.parametrize("split", [1, 2, 4, 8])
-def test_dense_split_step_matches_fp64(pbf, oracle, cuda, split):
+@pytest.mark.parametrize("split, interleave", [(1, 0), (2, 0), (4, 0), (8, 0), (2, 1), (8, 1)])
+def test_dense_split_step_matches_fp64(pbf, oracle, cuda, split, interleave):
     import torch
 
     sc = pbf.scenes.dam_break(seed=7)
@@ -124,8 +124,8 @@ def test_dense_split_step_matches_fp64(pbf, oracle, cuda, split):
     iid = torch.arange(n, dtype=torch.int32, device="cuda")
     npos, nvel = torch.empty_like(pos), torch.empty_like(vel)
     with pbf.Simulator(p, sc.ulim, sc.llim, n) as sim:
-        sim.set_tuning(dense_all=1, dense_split=split)
-        assert sim.tuning()["dense_split"] == split
+        sim.set_tuning(dense_all=1, dense_split=split, dense_interleave=interleave)
+        assert sim.tuning()["dense_split"] == split and sim.tuning()["dense_interleave"] == interleave
         sim.step(pos, npos, vel, nvel, iid, n)
         torch.cuda.synchronize()
     r = oracle.step(p, sc.ulim, sc.llim, sc.pos.astype(np.float64), np.zeros((n, 4)), np.arange(n, dtype=np.uint32),
