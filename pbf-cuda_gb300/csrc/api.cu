@@ -55,6 +55,35 @@ struct GraphCache {
   }
 };
 
+// Executable graphs of recent reverse passes.  A reverse pass's launches
+// depend only on its arguments (the taped step's constants and record, the
+// scratch, the lanes) and the caller's adjoint buffers, so a call whose key
+// matches a cached graph replays it.  A checkpointed rollout reverses the same
+// tape slots into the same buffers segment after segment, so its calls hit.
+struct BackwardKey {
+  pbf::BackwardArgs a;
+  pbf::BackwardTape t;
+  const void* perm;
+  const void* bufs[5];
+};
+
+struct BackwardCache {
+  static constexpr int kEntries = 48;
+  struct Entry {
+    BackwardKey key;
+    bool valid = false;
+    cudaGraphExec_t exec = nullptr;
+  } e[kEntries];
+  int next = 0;
+  void clear() {
+    for (Entry& x : e) {
+      if (x.exec) cudaGraphExecDestroy(x.exec);
+      x = Entry();
+    }
+    next = 0;
+  }
+};
+
 StepKey make_key(const pbf::StepConsts& c, void* pos, void* npos, void* vel, void* nvel, void* iid, int n,
                  int niter) {
   StepKey k;
@@ -97,6 +126,7 @@ struct pbf_solver {
   cudaStream_t cap_stream;
   cudaGraphExec_t exec;
   GraphCache cache;
+  BackwardCache bw_cache;  // graphs of reverse passes (pbf_backward)
   // the tape (pbf_tape_enable): a stack of taped steps, each record holding
   // what the step's reverse pass needs, and the reverse pass's scratch
   int tape_depth;            // records the stack holds; 0: tape off
@@ -393,6 +423,7 @@ void free_all(pbf_solver* s) {
     if (e) cudaEventDestroy(e);
   if (s->exec) cudaGraphExecDestroy(s->exec);
   s->cache.clear();
+  s->bw_cache.clear();
   if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
   void* tape[] = {s->tape_mem, s->bw4, s->bw1, s->bw8, s->wall_part, s->bw_sc};
   for (void* p : tape)
@@ -865,6 +896,7 @@ pbf_status pbf_tape_enable(pbf_solver* s, int depth) {
     }
   }
   if (depth > s->tape_cap || iters > s->tape_iters) {
+    s->bw_cache.clear();  // its graphs point into the old records
     if (s->tape_mem) cudaFree(s->tape_mem);
     s->tape_mem = nullptr;
     s->tape_cap = 0;
@@ -918,14 +950,65 @@ pbf_status pbf_backward(pbf_solver* s, const void* g_npos, const void* g_nvel, v
   a.kcell = s->bw8 + np;
   a.wall_part = s->wall_part;
   pbf::BackwardTape t;
+  std::memset(&t, 0, sizeof(t));  // unused slots included: keys compare as bytes
   t.niter = m.niter;
   float4* X = (float4*)(rec + tl.x);
   float* L = (float*)(rec + tl.l);
   for (int k = 0; k <= t.niter; ++k) t.X[k] = X + np * k;
   for (int k = 0; k < t.niter; ++k) t.lambda[k] = L + np * k;
-  PBF_CUDA(pbf::backward(a, t, (const uint32_t*)(rec + tl.perm), g_npos, g_nvel, g_pos, g_vel, g_lim,
-                         (cudaStream_t)stream),
-           "pbf_backward");
+  const uint32_t* perm = (const uint32_t*)(rec + tl.perm);
+  cudaStream_t st_ = (cudaStream_t)stream;
+  if (!s->use_graph) {
+    PBF_CUDA(pbf::backward(a, t, perm, g_npos, g_nvel, g_pos, g_vel, g_lim, st_), "pbf_backward");
+    s->tape_top = slot;
+    return PBF_OK;
+  }
+  // as one CUDA graph: replayed from the cache, or captured into its oldest entry
+  BackwardKey key;
+  std::memset(&key, 0, sizeof(key));
+  key.a = a;
+  key.t = t;
+  key.perm = perm;
+  const void* bufs[5] = {g_npos, g_nvel, g_pos, g_vel, g_lim};
+  for (int k = 0; k < 5; ++k) key.bufs[k] = bufs[k];
+  for (BackwardCache::Entry& x : s->bw_cache.e) {
+    if (x.valid && std::memcmp(&x.key, &key, sizeof(key)) == 0) {
+      PBF_CUDA(cudaGraphLaunch(x.exec, st_), "pbf_backward: graph launch");
+      s->tape_top = slot;
+      return PBF_OK;
+    }
+  }
+  BackwardCache::Entry& x = s->bw_cache.e[s->bw_cache.next];
+  s->bw_cache.next = (s->bw_cache.next + 1) % BackwardCache::kEntries;
+  x.valid = false;
+  PBF_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeThreadLocal), "pbf_backward: begin capture");
+  const cudaError_t be = pbf::backward(a, t, perm, g_npos, g_nvel, g_pos, g_vel, g_lim, s->cap_stream);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(s->cap_stream, &g);
+  if (be != cudaSuccess || ce != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return cuda_fail(be != cudaSuccess ? be : ce, "pbf_backward: capture");
+  }
+  if (x.exec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(x.exec, g, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(x.exec);
+      x.exec = nullptr;
+    }
+  }
+  if (!x.exec) {
+    const cudaError_t ie = cudaGraphInstantiate(&x.exec, g, 0);
+    if (ie != cudaSuccess) {
+      cudaGraphDestroy(g);
+      x.exec = nullptr;
+      return cuda_fail(ie, "pbf_backward: graph instantiate");
+    }
+  }
+  cudaGraphDestroy(g);
+  PBF_CUDA(cudaGraphLaunch(x.exec, st_), "pbf_backward: graph launch");
+  x.key = key;
+  x.valid = true;
   s->tape_top = slot;
   return PBF_OK;
 }

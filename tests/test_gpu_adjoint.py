@@ -222,3 +222,42 @@ def test_backward_is_bitwise_reproducible(pbf, oracle, cuda):
     g_pos, g_vel = runs[0][0], runs[0][1]
     close(g_pos[:, :3], want["pos"][:, :3], "g_pos")
     close(g_vel[:, :3], want["vel"][:, :3], "g_vel")
+
+
+def test_backward_graph_replay_matches_eager(pbf, cuda):
+    """The reverse pass as a CUDA graph -- captured on the first call, replayed
+    from the solver's cache when the same tape slot is reversed into the same
+    buffers again -- gives bitwise the adjoints of the same pass launched kernel
+    by kernel (pbf_use_graphs(s, 0))."""
+    import torch
+
+    _, pos, vel, p, a, b = setup(pbf, seed=12, n=(12, 12, 12), speed=3.0)
+    ulim, llim = (1.2, 1.2, 1.2), (0.0, 0.0, 0.0)
+    n = len(pos)
+    d_pos0 = torch.from_numpy(pos.copy()).cuda()
+    d_vel0 = torch.from_numpy(vel.copy()).cuda()
+    d_pos, d_vel = torch.empty_like(d_pos0), torch.empty_like(d_vel0)
+    npos, nvel = torch.empty_like(d_pos0), torch.empty_like(d_vel0)
+    iid = torch.empty(n, dtype=torch.int32, device="cuda")
+    g_npos = torch.from_numpy(a).cuda()
+    g_nvel = torch.from_numpy(b).cuda()
+    g_pos, g_vel = torch.empty_like(g_npos), torch.empty_like(g_nvel)
+    g_lim = torch.empty(6, dtype=torch.float32, device="cuda")
+    L = pbf.lib()
+    runs = []
+    with pbf.Simulator(p, ulim, llim, n) as sim:
+        sim.tape(True)
+        for graphs in (True, True, False):
+            sim.use_graphs(graphs)
+            d_pos.copy_(d_pos0)
+            d_vel.copy_(d_vel0)
+            iid.copy_(torch.arange(n, dtype=torch.int32, device="cuda"))
+            sim.step(d_pos, npos, d_vel, nvel, iid, n)
+            pbf.check(L.pbf_backward(sim._h, g_npos.data_ptr(), g_nvel.data_ptr(), g_pos.data_ptr(),
+                                     g_vel.data_ptr(), g_lim.data_ptr(), None), "pbf_backward")
+            torch.cuda.synchronize()
+            runs.append((g_pos.cpu().numpy().copy(), g_vel.cpu().numpy().copy(), g_lim.cpu().numpy().copy()))
+    assert np.isfinite(runs[0][0]).all() and np.abs(runs[0][0]).max() > 0
+    for other in runs[1:]:
+        for x, y in zip(runs[0], other):
+            assert np.array_equal(x.view(np.uint32), y.view(np.uint32))
