@@ -263,7 +263,12 @@ constexpr int kCellSlotShift = 8;
 // reference's sum with its terms grouped: results differ from it by
 // rounding only.
 constexpr int kGroupCell = 512;
-constexpr int kGroupChunk = 8192;  // particles of a grouped cell per work item
+// PBF_GROUP_CHUNK (a build-time tuning macro): particles of a grouped cell per
+// work item of the group-table kernels.
+#ifndef PBF_GROUP_CHUNK
+#define PBF_GROUP_CHUNK 8192
+#endif
+constexpr int kGroupChunk = PBF_GROUP_CHUNK;
 inline size_t group_slots(int max_particles) { return (size_t)max_particles / kGroupCell + 1; }
 inline size_t group_items(int max_particles) {
   return (size_t)max_particles / kGroupChunk + group_slots(max_particles) + 1;
