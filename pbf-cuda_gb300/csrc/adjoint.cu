@@ -610,13 +610,27 @@ k_bwd_out(BackwardArgs a, const uint32_t* __restrict__ perm, float4* __restrict_
   g_vel[p] = make_float4(a.c.dt * gs.x, a.c.dt * gs.y, a.c.dt * gs.z, 0.f);
 }
 
-// Sums the blocks' wall adjoints in block order into g_lim[6] (accumulating).
-__global__ void k_bwd_wall(const float* __restrict__ part, int blocks, float* __restrict__ g_lim) {
-  const int k = threadIdx.x;
-  if (k >= 6) return;
-  float sum = 0.f;
-  for (int b = 0; b < blocks; ++b) sum += part[b * 6 + k];
-  g_lim[k] += sum;
+// Sums the blocks' wall adjoints into g_lim[6] (accumulating) in a fixed
+// order: thread t of one block adds the parts of blocks t, t + kWallThreads,
+// ... in turn, then the threads' sums are added pairwise in a fixed tree.
+constexpr int kWallThreads = 256;
+__global__ void __launch_bounds__(kWallThreads)
+k_bwd_wall(const float* __restrict__ part, int blocks, float* __restrict__ g_lim) {
+  __shared__ float s[6][kWallThreads];
+  float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int b = threadIdx.x; b < blocks; b += kWallThreads)
+#pragma unroll
+    for (int k = 0; k < 6; ++k) acc[k] += part[b * 6 + k];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) s[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int w = kWallThreads / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+#pragma unroll
+      for (int k = 0; k < 6; ++k) s[k][threadIdx.x] += s[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 6) g_lim[threadIdx.x] += s[threadIdx.x][0];
 }
 
 // ---- density grid ---------------------------------------------------------------------
@@ -736,7 +750,7 @@ cudaError_t run_backward(BackwardArgs a, const BackwardTape& t, const uint32_t* 
     const float4* X = t.X[k];
     const float* lam = t.lambda[k];
     k_bwd_dp1<L><<<blocks, kThreads, 0, stream>>>(a, X, lam);  // also the packed cells of X_k
-    k_bwd_wall<<<1, 32, 0, stream>>>(a.wall_part, blocks, g_lim);
+    k_bwd_wall<<<1, kWallThreads, 0, stream>>>(a.wall_part, blocks, g_lim);
     k_bwd_dp2<L><<<blocks, kThreads, 0, stream>>>(a, X, lam);
     k_bwd_acc<<<acc_blocks, 256, 0, stream>>>(a);
     k_bwd_fix<true><<<blocks256, 256, 0, stream>>>(a);
