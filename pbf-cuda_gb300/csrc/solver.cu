@@ -354,8 +354,8 @@ __device__ __forceinline__ void visit_run(const Src& src, int j0, int j1, int r,
 // ascending order, through the hit queue.  p.visit() leaves non-hits
 // untouched, so the result is that of visit_window.
 //
-// save_masks: store chunk k's mask at masks[k * stride + i] (k < kMaskWords)
-// for the next pass over the same positions.
+// save_masks: store chunk k's mask at masks[k * stride + i] (k < kMaskWords;
+// i: the particle's mask slot) for the next pass over the same positions.
 template <class P, class Src>
 __device__ __forceinline__ void visit_window_masked(const SceneGeom& g,
                                                     const uint32_t* __restrict__ cs, int n,
@@ -1019,17 +1019,21 @@ __device__ __forceinline__ void stage_drain(StageState& st, uint32_t phase) {
 // ---- kernels ------------------------------------------------------------------------
 
 // The plain (not grouped) walk of a sparse-kernel particle's window.
+// t: the particle's thread slot in the pass's list, which indexes its saved
+// masks (the lambda and delta_p passes of an iteration take the same list, so
+// a particle keeps its slot; consecutive threads then store and load
+// consecutive words).
 template <int kKind, class P, class Src>
 __device__ __forceinline__ void sparse_visit(const PassArgs& a, const SceneGeom& g, int3 q, const Src& src,
-                                             P& p, bool exact, int i, int chunks, HitQueue& hq) {
+                                             P& p, bool exact, int t, int chunks, HitQueue& hq) {
   if (exact) {
     visit_window(g, a.cs, a.n, q, src, p);  // non-neighbours matter: visit every candidate
   } else if (kKind == kLambda) {
-    visit_window_masked(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, hq);  // saves its masks
+    visit_window_masked(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, t, hq);  // saves its masks
   } else if ((kKind == kDeltaP || kKind == kDeltaPFinal) && chunks <= kMaskWords) {
-    visit_window_saved(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, i, chunks, hq);  // lambda's masks
+    visit_window_saved(g, a.cs, a.n, q, src, p, a.masks, a.mask_stride, t, chunks, hq);  // lambda's masks
   } else {
-    visit_window_masked(g, a.cs, a.n, q, src, p, nullptr, 0, i, hq);
+    visit_window_masked(g, a.cs, a.n, q, src, p, nullptr, 0, t, hq);
   }
 }
 
@@ -1116,9 +1120,9 @@ __global__ void PBF_SPARSE_BOUNDS k_sparse(PassArgs a) {
     if (grouped)
       visit_window_grouped(g, a, q, FromGlobal{a.X}, p, 0, entries, hq);
     else if (kStage && staged)
-      sparse_visit<kKind>(a, g, q, FromStage{stage, st.D}, p, exact, i, chunks, hq);
+      sparse_visit<kKind>(a, g, q, FromStage{stage, st.D}, p, exact, t, chunks, hq);
     else
-      sparse_visit<kKind>(a, g, q, FromGlobal{a.X}, p, exact, i, chunks, hq);
+      sparse_visit<kKind>(a, g, q, FromGlobal{a.X}, p, exact, t, chunks, hq);
     p.finish(a);
   }
   if (kStage && cap > 0) stage_drain(st, phase);
