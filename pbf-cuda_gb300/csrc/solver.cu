@@ -19,16 +19,20 @@
 // Each pass is two kernels.  The sparse kernel gives every particle one
 // thread and walks its window in a compact loop (fluid at rest: ~200
 // candidates; a window whose grouped cells -- see pbf_internal.cuh -- bring
-// it under dense_window entries is walked group by group).  A warp in which
-// some window still exceeds dense_window entries (particles piled into a few
-// cells) instead appends itself to a dense list and returns; the dense
-// kernel then gives each listed warp a block of kDenseWarps warps, each
-// walking one contiguous chunk of every lane's window, and adds the chunks'
-// partial sums in chunk order in shared memory.  Steps of fewer than
-// kDenseAllBelow particles send every warp to the dense kernel by default
-// (one thread per particle would leave most SMs idle).  Both orders are
-// fixed, so results stay deterministic; they differ from the reference's
-// sequential sums only by rounding.
+// it under dense_window entries is walked group by group).  A particle whose
+// window still exceeds dense_window entries (particles piled into a few
+// cells) instead appends itself to a dense list; the persistent dense kernel
+// takes the list in batches of 32 particles from a counter, splits each
+// batch's windows over dense_split warps (each walking one part of every
+// lane's window) and adds the parts' partial sums in part order in shared
+// memory.  Steps of fewer than kDenseAllBelow particles send every particle
+// to the dense kernel by default (one thread per particle would leave most
+// SMs idle).  Both orders are fixed, so results stay deterministic; they
+// differ from the reference's sequential sums only by rounding.  The walks
+// test chunks of 32 candidates into hit masks and run the pair body on the
+// hits, optionally through a hit queue; each kernel has a variant that
+// stages its block's column runs in shared memory by bulk asynchronous
+// copies.  Neither changes any sum.
 //
 // Particles piled onto one position (a grouped cell's position group) have
 // bitwise the same window, position and, within a step, lambda: their lambda
