@@ -157,7 +157,10 @@ k_hash(const float4* __restrict__ pos, const float4* __restrict__ vel, int n, St
   const int3 q = cell_of(c, g, x);
   const uint32_t key = (uint32_t)cell_index(g, q.x, q.y, q.z);
   keys[i] = key;
-  atomicAdd(&cell_count[key], 1u);
+  // one atomic per cell and warp (the particles are in last step's cell order,
+  // so a warp's lanes mostly share a few cells)
+  const unsigned same = __match_any_sync(__activemask(), key);
+  if ((threadIdx.x & 31) == __ffs(same) - 1) atomicAdd(&cell_count[key], (uint32_t)__popc(same));
 }
 
 // ---- stable LSD radix sort of (key, index) ------------------------------------

@@ -187,7 +187,7 @@ extern "C" pbf_status pbf_step_noalloc(const pbf_params* params, const float uli
   g.cell_start = (uint32_t*)(base + kOffStart);
   g.radix_counts = (uint32_t*)(base + kOffRadix);
   g.scan_partials = (uint32_t*)(base + kOffPartials);
-  pbf::SolverScratch s;
+  pbf::SolverScratch s = {};  // fields this step does not use stay null
   s.xs = (float4*)(base + kOffXs);
   s.xa = (float4*)(base + kOffXa);
   s.xb = (float4*)(base + kOffXb);
