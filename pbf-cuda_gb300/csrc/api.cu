@@ -401,11 +401,6 @@ cudaError_t alloc_buckets(pbf::SolverScratch& sol, size_t np, size_t nc) {
   if (e == cudaSuccess) e = alloc(&sol.bent, np);
   if (e == cudaSuccess) e = alloc(&sol.bucket, np);
   if (e == cudaSuccess) e = alloc(&sol.bpart, (size_t)pbf::kMaxScanPartials);
-#if PBF_DENSE_NO_BARRIERS
-  if (e == cudaSuccess) e = alloc(&sol.dpart, pbf::dense_part_floats((int)np));
-  if (e == cudaSuccess) e = alloc(&sol.ddone, pbf::dense_batches((int)np));
-  if (e == cudaSuccess) e = cudaMemset(sol.ddone, 0, sizeof(uint32_t) * pbf::dense_batches((int)np));
-#endif
   return e;
 }
 
@@ -419,7 +414,7 @@ void free_all(pbf_solver* s) {
                   s->sol.grp_max, s->sol.grp_acc, s->sol.grp_list, s->sol.grp_list_n, s->sol.grp_done,
                   s->sol.grp_zero, s->sol.grp_item_off, s->sol.grp_item_slot, s->sol.work_list,
                   s->sol.work_follow, s->sol.work_blocks, s->sol.bcnt, s->sol.bstart, s->sol.bent,
-                  s->sol.bucket, s->sol.bpart, s->sol.dpart, s->sol.ddone};
+                  s->sol.bucket, s->sol.bpart};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (cudaEvent_t& e : s->ev)
@@ -1182,7 +1177,7 @@ void batch_free(pbf_batch* b) {
                   b->sol.grp_max, b->sol.grp_acc, b->sol.grp_list, b->sol.grp_list_n, b->sol.grp_done,
                   b->sol.grp_zero, b->sol.grp_item_off, b->sol.grp_item_slot, b->sol.work_list,
                   b->sol.work_follow, b->sol.work_blocks, b->sol.bcnt, b->sol.bstart, b->sol.bent,
-                  b->sol.bucket, b->sol.bpart, b->sol.dpart, b->sol.ddone, b->d_geom, b->d_sid};
+                  b->sol.bucket, b->sol.bpart, b->d_geom, b->d_sid};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->exec) cudaGraphExecDestroy(b->exec);

@@ -225,18 +225,7 @@ struct SolverScratch {
   uint2* bent;         // [max_particles] (current cell, rank in it) of each computing particle
   int* bucket;         // [max_particles] the computing particles, bucket by bucket
   uint32_t* bpart;     // [kMaxScanPartials] scan partials
-  // the dense kernel's parts of each batch of 32 listed particles (when it
-  // runs without block barriers): partial sums, and parts finished per batch
-  // (0 between passes); null: the dense kernel sums its parts in shared memory
-  float* dpart;        // [dense_batches(max_particles)][8 parts][kDenseFields][32]
-  uint32_t* ddone;     // [dense_batches(max_particles)]
 };
-
-// Batches of 32 listed particles the dense kernel can take, and the partial
-// sums a part of one holds (the largest pass's fields).
-constexpr int kDenseFields = 6;
-inline size_t dense_batches(int max_particles) { return (size_t)max_particles / 32 + 2; }
-inline size_t dense_part_floats(int max_particles) { return dense_batches(max_particles) * 8 * kDenseFields * 32; }
 
 // Lambda and delta_p results are the same for every particle of a position
 // group (same position: same window, same candidates in the same order; a
@@ -353,12 +342,6 @@ cudaError_t launch_xsph(const StepConsts& c, const Geometry& G, const float4* X,
 // Candidates above which a warp takes the dense kernel, and the particle
 // count below which every warp does (defaults; pbf_autotune can override).
 constexpr int kDefaultDenseWindow = 512;
-// PBF_DENSE_NO_BARRIERS (a build-time switch): the dense kernel's warps take
-// (batch, part) tasks on their own and exchange partial sums through global
-// memory instead of block barriers and shared memory.
-#ifndef PBF_DENSE_NO_BARRIERS
-#define PBF_DENSE_NO_BARRIERS 0
-#endif
 // Blocks of the dense kernel per SM (its grid is this many times the SM count).
 #ifndef PBF_DENSE_BLOCKS_PER_SM
 #define PBF_DENSE_BLOCKS_PER_SM 4

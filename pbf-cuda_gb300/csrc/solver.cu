@@ -88,8 +88,6 @@ struct PassArgs {
   int next_counter;       // the other one, cleared for the next pass
   int item_counter;       // flags word handing out this pass's dense batches
   int next_item_counter;  // the other one, cleared for the next pass
-  float* dpart;           // the dense kernel's parts of each batch (null: in shared memory)
-  uint32_t* ddone;        // parts finished per batch
   int dense_all;          // every warp takes the dense kernel (small n)
   uint32_t* flags;
   uint32_t* dense;
@@ -1175,65 +1173,6 @@ __global__ void PBF_DENSE_BOUNDS k_dense(PassArgs a) {
   // no grouped cell this step: windows are walked as 9 column runs (the same
   // candidates in the same order as cell by cell, with fewer table reads)
   const bool groups = a.c.keps2 > 0.f && a.flags[kGroupCount] != 0u;
-  if (!kStage && a.dpart) {
-    // without block barriers: each warp takes (batch, part) tasks from a
-    // counter on its own, writes the part's sums to global memory, and the
-    // warp that finishes a batch's last part adds its parts in part order
-    // (the same sums as the shared-memory path) and finishes the batch
-    static_assert(P::kFields <= kDenseFields, "partial-sum fields");
-    const uint32_t tasks = count << split_log2;
-    for (;;) {
-      uint32_t task = 0u;
-      if (lane == 0) task = atomicAdd(&a.flags[a.item_counter], 1u);
-      task = __shfl_sync(kFull, task, 0);
-      if (task >= tasks) break;
-      const uint32_t batch = task >> split_log2;
-      const int part = (int)(task & (uint32_t)(split - 1));
-      const uint32_t e = batch * 32 + lane;
-      const bool valid = e < listed;
-      const int t = valid ? (int)(a.dense_all ? e : a.dense[e]) : 0;
-      const int i = valid ? work_particle(a, t) : 0;
-      const float4 xi = valid ? a.X[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-      const SceneGeom g = geom_of(a.c, a.G, valid ? i : 0);
-      const int3 q = cell_of(a.c, g, xi);
-      const bool exact = valid && exact_path(kKind, a, g, q, i);
-      float* out = a.dpart + ((size_t)batch * kDenseWarps + part) * kDenseFields * 32 + lane;
-      if (valid) {
-        const int total = groups ? window_total_grouped(g, a, q) : window_total(g, a.cs, a.n, q);
-        const int lo = (int)(((long long)total * part) >> split_log2);
-        const int hi = (int)(((long long)total * (part + 1)) >> split_log2);
-        P p(a, g, xi, i, exact);
-        if (groups)
-          visit_window_grouped(g, a, q, FromGlobal{a.X}, p, lo, hi, hq);
-        else if (a.c.dense_interleave)
-          visit_window_strided(g, a.cs, a.n, q, FromGlobal{a.X}, p, part, split, hq);
-        else
-          visit_window_chunk(g, a.cs, a.n, q, FromGlobal{a.X}, p, lo, hi, hq);
-        p.store(out, 32);
-      }
-      __threadfence();  // this part's sums, before the count that lets another warp read them
-      __syncwarp();
-      uint32_t done = 0u;
-      if (lane == 0) done = atomicAdd(&a.ddone[batch], 1u);
-      done = __shfl_sync(kFull, done, 0);
-      if (done == (uint32_t)split - 1) {
-        __threadfence();
-        if (valid) {
-          P p(a, g, xi, i, exact);
-          for (int k = 0; k < split; ++k) {
-            const float* src = a.dpart + ((size_t)batch * kDenseWarps + k) * kDenseFields * 32 + lane;
-            float f[kDenseFields];
-#pragma unroll
-            for (int m = 0; m < P::kFields; ++m) f[m] = __ldcg(src + m * 32);  // other SMs wrote them
-            p.add(f, 1);
-          }
-          p.finish(a);
-        }
-        if (lane == 0) a.ddone[batch] = 0u;  // for the next pass
-      }
-    }
-    return;
-  }
   // batches are handed out one block-load at a time by a counter, so a block
   // that drew light batches takes more (batches cost from a few hundred to
   // many thousand candidates); which block computes a batch changes nothing
@@ -1942,8 +1881,6 @@ PassArgs base_args(const StepConsts& c, const Geometry& G, const float4* X, cons
   a.next_item_counter = kItemCount0 + ((pass + 1) & 1);
   a.flags = s.flags;
   a.dense = s.dense;
-  a.dpart = s.dpart;
-  a.ddone = s.ddone;
   a.masks = s.masks;
   a.mask_stride = s.mask_stride;
   a.cell_flags = s.cell_flags;
