@@ -261,8 +261,9 @@ __device__ __forceinline__ void visit_window(const SceneGeom& g, const uint32_t*
 // loop, so the warp pays max-over-lanes of the hits of the whole queued span.
 // Hits are visited in the order they were queued -- the window's visiting
 // order -- so the sums are bitwise those of visiting each chunk's hits right
-// away.  The capacity (chunks queued per thread before a flush) is a template
-// parameter of the kernel (1: the body right after each chunk).
+// away.  The capacity (chunks queued per thread before a flush) comes from
+// the step's tuning (StepConsts::queue_sparse / queue_dense); capacity 1 runs
+// each chunk's hits right away, straight from registers.
 struct HitQueue {
   uint32_t* mask;  // this thread's column: entry k at mask[k * stride]
   int* base;       // where queued chunk k starts (Src::tag)
