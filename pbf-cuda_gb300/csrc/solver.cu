@@ -675,6 +675,9 @@ struct DeltaPPass {
     return !(r2 >= c.h2) && !(r2 < c.keps2) && j != i;
   }
   __device__ __forceinline__ void visit(float4 xj, int j) {
+    // lambda_j first: its load overlaps the distance test (a visited candidate
+    // is almost always a neighbour, so the load is rarely wasted)
+    const float lj = __ldg(lambda + j);
     const float ex = xi.x - xj.x, ey = xi.y - xj.y, ez = xi.z - xj.z;
     const float r2 = dist2(ex, ey, ez);
     if (!(r2 >= c.h2) && !(r2 < c.keps2) && j != i) {  // NaN-inclusive, as the reference
@@ -682,13 +685,13 @@ struct DeltaPPass {
       const float corr = c.coef_corr * pow_corr(c, wgt);
       const float ir = rsqrtf(r2);
       const float t = c.h - r2 * ir;
-      const float f = (li + __ldg(lambda + j) + corr) * (c.spiky_coef * t * t * ir);
+      const float f = (li + lj + corr) * (c.spiky_coef * t * t * ir);
       ax = fmaf(f, ex, ax);
       ay = fmaf(f, ey, ay);
       az = fmaf(f, ez, az);
     } else if (exact && j != i) {
       // zero gradient: (lambda_i + lambda_j + s_corr) * 0 is NaN iff a lambda is not finite
-      poison |= !isfinite(li) || !isfinite(__ldg(lambda + j));
+      poison |= !isfinite(li) || !isfinite(lj);
     }
   }
   // `cnt` particles at xg with lambda_j summing to cnt sum.x + sum.y (each
@@ -774,18 +777,20 @@ struct XsphPass {
     return !(dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z) >= c.h2);
   }
   __device__ __forceinline__ void visit(float4 xj, int j) {
+    // v_j and rho_j first: their loads overlap the distance test (a visited
+    // candidate is almost always a neighbour)
+    const float4 vj = __ldg(V + j);
+    const float rj = __ldg(rho + j);
     const float r2 = dist2(xi.x - xj.x, xi.y - xj.y, xi.z - xj.z);
     if (!(r2 >= c.h2)) {  // NaN-inclusive, as getPoly6
-      const float4 vj = __ldg(V + j);
-      const float w2 = 2.f * poly6_inside(c, r2) / (ri + __ldg(rho + j));
+      const float w2 = 2.f * poly6_inside(c, r2) / (ri + rj);
       ax = fmaf(vj.x - vi.x, w2, ax);
       ay = fmaf(vj.y - vi.y, w2, ay);
       az = fmaf(vj.z - vi.z, w2, az);
     } else if (exact) {
       // W = 0: 2 (v_j - v_i) * 0 / (rho_i + rho_j) is NaN iff the velocity
       // difference is not finite or the denominator is 0 or NaN
-      const float4 vj = __ldg(V + j);
-      const float den = ri + __ldg(rho + j);
+      const float den = ri + rj;
       const bool bad_den = !(den != 0.f) || isnan(den);
       px |= bad_den || !isfinite(vj.x - vi.x);
       py |= bad_den || !isfinite(vj.y - vi.y);
