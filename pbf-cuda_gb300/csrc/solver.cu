@@ -875,6 +875,10 @@ __device__ __forceinline__ bool exact_path(int kind, const PassArgs& a, const Sc
 // memory as before.  The wait is bounded: past kStageSpins polls the block
 // records kErrStageTimeout, stops staging and reads global memory (same
 // results), and waits once more (bounded) for the copy before it exits.
+// On GB300 the staged variants measured slower than the L1 path on every
+// workload tried (the candidates are L1-resident already, and the stage costs
+// resident blocks and a wait per block), so the default stages are 0 and
+// pbf_autotune turns them on only where its trial steps find them faster.
 
 constexpr int kStageSpins = 1 << 20;
 
